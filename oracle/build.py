@@ -1,0 +1,67 @@
+"""Build the CPU oracle (and, where the reference sources are mounted, the
+reference's own C implementation of the path).
+
+TEST INFRASTRUCTURE ONLY: the libraries built here are checkers for the CUDA
+path (tests/, __graft_entry__.smoke(), bench.py's cpu_baseline and reference
+legs).  Nothing in the product library links or loads them.
+
+* ``oracle/_build/liboracle.so`` -- ``oracle/oracle.c`` (this project's own
+  restatement), ``gcc -O3 -fopenmp``.
+* ``oracle/_ref/sw_align_ref.so`` -- ``clustkit/csrc/sw_align.c`` compiled
+  straight from the reference checkout (read in place, never copied), with the
+  reference's own build line (clustkit/csrc/sw_align.c:10) minus
+  ``-march=native``.  Built only when the reference checkout exists.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF_OUT = HERE / "_ref"
+# Location of the reference checkout; only this build script reads it.
+REF_SRC = Path(os.environ.get("CLUSTKIT_REFERENCE", "/root/reference")) / "clustkit" / "csrc" / "sw_align.c"
+
+CFLAGS = ["-O3", "-fopenmp", "-shared", "-fPIC", "-std=c11"]
+
+
+def _needs(out: Path, src: Path) -> bool:
+    return not out.exists() or out.stat().st_mtime < src.stat().st_mtime
+
+
+def build_oracle(verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    src = HERE / "oracle.c"
+    out = BUILD / "liboracle.so"
+    if _needs(out, src):
+        cmd = ["gcc", *CFLAGS, "-o", str(out), str(src)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    return out
+
+
+def build_reference(verbose: bool = False) -> Path | None:
+    """Compile the reference's sw_align.c into oracle/_ref/ if the checkout is present."""
+    if not REF_SRC.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    out = REF_OUT / "sw_align_ref.so"
+    if _needs(out, REF_SRC):
+        cmd = ["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-o", str(out), str(REF_SRC)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    return out
+
+
+def main() -> None:
+    print(build_oracle(verbose=True))
+    print(build_reference(verbose=True))
+
+
+if __name__ == "__main__":
+    main()
