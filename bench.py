@@ -1,0 +1,434 @@
+"""Benchmark: banded Smith-Waterman over clustkit's Align-phase candidate pairs.
+
+Workload (one "step"): the Align phase of the 50,000-sequence clustering set --
+5,000 synthetic families x 10 (median length 350, clipped 30..2000), k=5 /
+s=128 MinHash sketches, LSH with clustkit's high-sensitivity parameters at
+t=0.3 (b=1, L=512), clustkit's Jaccard pre-filter, pairs ordered by min(i,j)
+as compute_pairwise_alignment orders them, then banded SW (band width 100,
+BLOSUM62, gaps -11/-1) over every remaining pair with per-pair score, identity
+numerator/denominator and pass/fail.  Data are seeded synthetic (no public
+dataset); the sequences and pair list are built once, before timing.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints one JSON line: value = GCUPS of the batched engine with inputs
+resident in HBM (device pointers, CUDA events per step on the launching
+stream, L2 flushed between steps outside the timed events); e2e = the same
+through the host-buffer C entry point ck_sw_batch (H2D of the step's inputs
+from pinned memory and D2H of its outputs inside the timed region).  The
+plain engine (one unbinned launch) is timed beside it.  The reference arm
+times clustkit's CPU implementation (its own C compiled from source when that
+library was built in this checkout, else this repo's C restatement) on the
+host cores, on a bounded sample of the same pairs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+BAND_WIDTH = 100
+THRESHOLD = 0.3
+WORKLOAD = {"workload": "align-50k: 5000 families x 10, median 350 [30,2000], k=5 s=128, "
+                        "LSH b=1 L=512 (t=0.3 high), Jaccard pre-filter, SW bw=100 BLOSUM62 -11/-1",
+            "n_sequences": 50000, "threshold": THRESHOLD, "band_width": BAND_WIDTH,
+            "l2": "flushed between timed steps (256 MiB write, outside the step events)"}
+OPS_PER_CELL = 6  # max-plus lane ops of the score recurrence: E, F: viaddmax+add; H: vimax3+add
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------- workload
+def build_workload(use_gpu: bool, quick: bool = False):
+    from clustkit_gb300 import synth
+    from clustkit_gb300.lsh import auto_lsh_params, lsh_candidates
+    n_fam = 500 if quick else 5000
+    t0 = time.time()
+    s = synth.generate_families(n_fam, 10, median=350, lo=30, hi=2000, seed=2)
+    t1 = time.time()
+    if use_gpu:
+        from clustkit_gb300.sketch import sketch_flat
+        sk = sketch_flat(s.flat, s.offsets, s.lengths, 5, 128)
+    else:
+        import oracle
+        sk = oracle.sketches(s.flat, s.offsets, s.lengths, 5, 128)
+    lp = auto_lsh_params(THRESHOLD, "high", 5)
+    cand = lsh_candidates(sk, lp["num_tables"], lp["num_bands"], 42)
+    t2 = time.time()
+    floor = max(0.001, 0.3 * THRESHOLD ** 5)
+    if use_gpu:
+        from clustkit_gb300.pairwise import _jaccard_prefilter
+        keep = _jaccard_prefilter(cand, sk, THRESHOLD)
+    else:
+        import oracle
+        m = len(cand)
+        keep = None
+        rng = np.random.RandomState(0)
+        idx = rng.choice(m, size=min(2000, m), replace=False)
+        if float(np.mean(oracle.jaccard(cand[idx], sk) < floor)) >= 0.05:
+            keep = oracle.jaccard(cand, sk) >= floor
+    pairs = cand if keep is None else cand[keep]
+    pairs = pairs[np.argsort(np.minimum(pairs[:, 0], pairs[:, 1]), kind="mergesort")]
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+    log(f"workload: {s.n} seqs ({t1 - t0:.1f}s), {len(cand)} LSH candidates ({t2 - t1:.1f}s), "
+        f"{len(pairs)} after Jaccard pre-filter")
+    return s, pairs, len(cand)
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+            os.unlink(self.path)
+        except OSError:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        busy = [v for v in sm if mx and v > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- dist
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def shard(pairs: np.ndarray, world: int, rank: int) -> np.ndarray:
+    """Weak scaling: every rank aligns its own full-size replica of the pair
+    list (the path has no exchange step, so ranks never communicate data)."""
+    return pairs
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ----------------------------------------------------------------------------- CPU baselines
+def cpu_baseline(s, pairs, target_s: float = 12.0, use_ref: bool = True):
+    import oracle
+    from clustkit_gb300.blosum import BLOSUM62
+    from clustkit_gb300.cells import pair_cells
+    threads = os.cpu_count() or 1
+    kind = "reference" if (use_ref and oracle.ref_available()) else "port"
+    rng = np.random.default_rng(0)
+    sample = pairs[rng.permutation(len(pairs))]
+
+    def run(p):
+        t = time.perf_counter()
+        if kind == "reference":
+            oracle.ref_sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=threads)
+        else:
+            oracle.set_num_threads(threads)
+            oracle.sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+        return time.perf_counter() - t
+
+    n = min(len(sample), 2000)
+    dt = run(sample[:n])
+    n = int(min(len(sample), max(n, n * target_s / max(dt, 1e-3))))
+    p = sample[:n]
+    dt = run(p)
+    cells = int(pair_cells(p, s.lengths, BAND_WIDTH).sum())
+    return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
+            "pairs_per_s": n / dt,
+            "sample": f"{n} random pairs of the workload ({cells} cells), {threads} threads, {dt:.1f}s"}
+
+
+# ----------------------------------------------------------------------------- arms
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from clustkit_gb300.cells import pair_cells
+    s, pairs, n_cand = build_workload(use_gpu=False, quick=args.quick)
+    import oracle
+    from clustkit_gb300.blosum import BLOSUM62
+    threads = os.cpu_count() or 1
+    kind = "reference" if oracle.ref_available() else "port"
+    rng = np.random.default_rng(1)
+    order = rng.permutation(len(pairs))
+    # size one step to ~4 s of host work
+    probe = pairs[order[:1000]]
+    t = time.perf_counter()
+    oracle.set_num_threads(threads)
+    oracle.sw_batch(probe, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+    dt = time.perf_counter() - t
+    per_step = int(min(len(pairs), max(1000, 1000 * 4.0 / max(dt, 1e-3))))
+
+    def step(k):
+        sel = order[(k * per_step) % len(pairs):][:per_step]
+        p = pairs[sel] if len(sel) == per_step else pairs[order[:per_step]]
+        t0 = time.perf_counter()
+        if kind == "reference":
+            oracle.ref_sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=threads)
+        else:
+            oracle.sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+        return time.perf_counter() - t0, int(pair_cells(p, s.lengths, BAND_WIDTH).sum()), len(p)
+
+    for k in range(args.warmup):
+        step(k)
+    tt = cc = pp = 0
+    for k in range(args.steps):
+        dt, c, n = step(args.warmup + k)
+        tt += dt; cc += c; pp += n
+    gcups = cc / tt / 1e9
+    line = {"metric": "banded-SW GCUPS (Align phase, 50k-sequence clustering set)", "value": gcups,
+            "unit": "GCUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+            "config": dict(WORKLOAD, sample=f"{per_step} random pairs per step"),
+            "impl": "reference", "pairs_per_s": pp / tt,
+            "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": kind,
+                             "sample": f"{per_step} pairs per step of {len(pairs)}"},
+            "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from clustkit_gb300 import _lib
+    from clustkit_gb300.blosum import BLOSUM62
+    from clustkit_gb300.cells import pair_cells
+    from clustkit_gb300.pairwise import ENGINE_BATCHED, ENGINE_PLAIN, PASS_CPU
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = _lib.load()
+    _lib.require_gpu()
+    s, pairs, n_cand = build_workload(use_gpu=True, quick=args.quick)
+    pairs = shard(pairs, world, rank)
+    M = len(pairs)
+    cells = int(pair_cells(pairs, s.lengths, BAND_WIDTH).sum())
+    dev = torch.device("cuda", local)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_pairs, d_flat, d_off, d_len = T(pairs), T(s.flat), T(s.offsets), T(s.lengths)
+    out = {k: torch.empty(M, dtype=dt, device=dev) for k, dt in
+           (("sims", torch.float32), ("scores", torch.int32), ("matches", torch.int32),
+            ("shorter", torch.int32), ("mask", torch.uint8))}
+    sub = np.ascontiguousarray(BLOSUM62)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def launch(engine):
+        st = lib.ck_sw_batch_device(
+            d_pairs.data_ptr(), M, d_flat.data_ptr(), len(s.flat), d_off.data_ptr(), d_len.data_ptr(),
+            s.n, BAND_WIDTH, sub.ctypes.data, THRESHOLD, None, PASS_CPU, engine,
+            out["sims"].data_ptr(), out["scores"].data_ptr(), out["matches"].data_ptr(),
+            out["shorter"].data_ptr(), out["mask"].data_ptr(), stream.cuda_stream)
+        _lib.check(st)
+
+    def timed(engine, steps, warmup, kernel_times=None):
+        for _ in range(warmup):
+            launch(engine)
+        _lib.check(lib.ck_sw_status_device(stream.cuda_stream))
+        torch.cuda.synchronize()
+        barrier(world)
+        total = 0.0
+        launches = 0
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(k & 0xFF)  # evict L2 between steps (outside the step events)
+            ev[k][0].record(stream)
+            launch(engine)
+            ev[k][1].record(stream)
+            launches += _lib.sw_counters()["launches"]
+            if kernel_times is not None:
+                ms = np.zeros(1, np.float32)
+                _lib.check(lib.ck_sw_last_kernel_ms(ms.ctypes.data))
+                kernel_times.append(float(ms[0]))
+        torch.cuda.synchronize()
+        barrier(world)
+        total = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        _lib.check(lib.ck_sw_status_device(stream.cuda_stream))
+        return max_over_ranks(total, world), launches
+
+    # ---- batched engine, device-resident inputs (value)
+    clocks = ClockSampler(local)
+    lib.ck_sw_profile(1)
+    kt = []
+    clocks.start()
+    t_batched, launches = timed(ENGINE_BATCHED, args.steps, args.warmup, kt)
+    clk = clocks.stop()
+    lib.ck_sw_profile(0)
+    res_b = {k: v.cpu().numpy() for k, v in out.items()}
+    # ---- plain engine (the plain GPU form), same pairs
+    plain_steps = max(1, min(args.steps, 3))
+    lib.ck_sw_profile(1)
+    kt_plain = []
+    t_plain, _ = timed(ENGINE_PLAIN, plain_steps, 1, kt_plain)
+    lib.ck_sw_profile(0)
+    res_p = {k: v.cpu().numpy() for k, v in out.items()}
+    engines_agree = all(np.array_equal(res_b[k], res_p[k]) for k in res_b)
+
+    # ---- parity against the oracle on a sample
+    import oracle
+    rng = np.random.default_rng(7)
+    samp = rng.choice(M, size=min(M, 3000), replace=False)
+    ref = oracle.sw_batch(pairs[samp], s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+    oracle_ok = all(np.array_equal(res_b[k][samp], ref[k]) for k in ("scores", "matches", "shorter")) \
+        and np.array_equal(res_b["sims"][samp], ref["sims"])
+
+    # ---- e2e through the host-buffer C entry point, pinned host memory
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    h_pairs, h_flat, h_off, h_len = pin(pairs), pin(s.flat), pin(s.offsets), pin(s.lengths)
+    h_out = {k: pin(np.empty(M, dt)) for k, dt in (("sims", np.float32), ("scores", np.int32),
+                                                   ("matches", np.int32), ("shorter", np.int32),
+                                                   ("mask", np.uint8))}
+
+    def host_call():
+        _lib.check(lib.ck_sw_batch(
+            h_pairs.ctypes.data, M, h_flat.ctypes.data, len(h_flat), h_off.ctypes.data, h_len.ctypes.data,
+            s.n, BAND_WIDTH, sub.ctypes.data, THRESHOLD, None, PASS_CPU, ENGINE_BATCHED,
+            h_out["sims"].ctypes.data, h_out["scores"].ctypes.data, h_out["matches"].ctypes.data,
+            h_out["shorter"].ctypes.data, h_out["mask"].ctypes.data))
+
+    for _ in range(max(1, args.warmup)):
+        host_call()
+    barrier(world)
+    e2e_t = 0.0
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_call()
+        e2e_t += time.perf_counter() - t0
+    e2e_t = max_over_ranks(e2e_t, world)
+    e2e_ok = all(np.array_equal(h_out[k], res_b[k]) for k in res_b)
+    h2d = pairs.nbytes + s.flat.nbytes + s.offsets.nbytes + s.lengths.nbytes
+    d2h = M * (4 + 4 + 4 + 4 + 1)
+
+    # ---- roofline (integer issue bound) and CPU baseline
+    peak = np.zeros(1, np.float64)
+    rates = {}
+    for which, name in ((0, "viaddmax_s32"), (1, "vimax3_s32"), (2, "iadd_s32"), (3, "viaddmax_s16x2")):
+        _lib.check(lib.ck_probe_int_rate(which, peak.ctypes.data))
+        rates[name] = float(peak[0])
+    p_int32 = max(rates["viaddmax_s32"], rates["iadd_s32"], rates["vimax3_s32"])
+    kernel_s = float(np.mean(kt)) / 1e3 if kt and min(kt) > 0 else t_batched / args.steps
+    gcups_kernel = cells / kernel_s / 1e9
+    achieved = gcups_kernel * OPS_PER_CELL  # Gop/s
+    cpu = cpu_baseline(s, pairs) if (rank == 0 and not args.no_cpu) else None
+
+    gcups = world * cells / t_batched * args.steps / 1e9
+    line = {
+        "metric": "banded-SW GCUPS (Align phase, 50k-sequence clustering set)",
+        "value": gcups, "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_batched / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded families; no public dataset)",
+        "config": dict(WORKLOAD, pairs=M, lsh_candidates=n_cand, cells_per_step=cells,
+                       engine="batched (length-sorted persistent strip kernel, R=16)"),
+        "pairs_per_s": world * M / t_batched * args.steps,
+        "plain": {"value": world * cells / t_plain * plain_steps / 1e9, "unit": "GCUPS",
+                  "pairs_per_s": world * M / t_plain * plain_steps,
+                  "kernel_ms": float(np.mean(kt_plain)) if kt_plain else None, "steps": plain_steps},
+        "speedup_vs_plain": (cells / (t_batched / args.steps)) / (cells / (t_plain / plain_steps)),
+        "bit_exact": {"batched_vs_plain_all_pairs": bool(engines_agree),
+                      "vs_oracle_sample": bool(oracle_ok), "e2e_vs_device": bool(e2e_ok),
+                      "oracle_sample_pairs": int(len(samp))},
+        "e2e": {"value": world * cells / e2e_t * args.steps / 1e9, "unit": "GCUPS",
+                "pairs_per_s": world * M / e2e_t * args.steps,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "api": "ck_sw_batch (host buffers, pinned)"},
+        "roofline": {"bound": "int", "achieved": achieved, "peak": p_int32 / 1e9, "unit": "Gop/s",
+                     "frac": achieved / (p_int32 / 1e9), "traffic": None,
+                     "basis": f"{OPS_PER_CELL} int32 max-plus lane-ops per cell x cells / strip-kernel "
+                              f"event time; peak = measured int32 DPX/ALU lane-op rate (in-repo probe)",
+                     "kernel": "sw_strip_kernel<16>", "kernel_ms": kernel_s * 1e3,
+                     "gcups_kernel": gcups_kernel, "gcups_roof": p_int32 / 1e9 / OPS_PER_CELL,
+                     "probe_gops": {k: v / 1e9 for k, v in rates.items()},
+                     "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL)},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--quick", action="store_true", help="10x smaller workload (smoke-testing the bench)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

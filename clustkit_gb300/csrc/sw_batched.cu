@@ -1,0 +1,414 @@
+// sw_batched.cu -- length-binned, persistent, register-strip Smith-Waterman.
+//
+// Same results as clustkit/csrc/sw_align.c:25-266, organised for the GPU:
+//
+//  1. prep: per pair, the geometry (shorter side = rows), the band cell count
+//     and a sort key (rows, columns); pairs the packed lanes cannot hold
+//     (rows > 8191, residue codes > 20) go to a fallback list.
+//  2. sort: pairs are ordered by descending (rows, columns), so a warp's 32
+//     pairs have near-identical shapes and the longest work is issued first.
+//  3. strip kernel: persistent CTAs; each warp takes the next 32 sorted pairs
+//     from a global ticket counter and every lane aligns one pair.  A lane
+//     sweeps its pair in strips of R rows: the strip's R rows live in
+//     registers and advance one column at a time, so per column only the
+//     row above the strip is read from (and the strip's last row written to)
+//     a per-lane circular window in global scratch.
+//  4. the plain kernel runs the fallback list, plus any pair whose score
+//     reached the packed lane's limit (re-run exactly in plain int32).
+//
+// Packed key.  Each DP value is one int32
+//     key = score * 2^16 + prio * 2^14 + tie * 2^13 + matches
+// with matches in 13 bits (<= 8191 rows), a 2-bit priority (zero 3, diag 2,
+// E 1, F 0) and a tie bit (gap extension 1, gap opening 0).  Signed integer
+// max over keys then orders candidates exactly as clustkit's comparisons do
+// (score first, then H's 0 > diag > E > F priority, then E/F's preference for
+// extension on ties) and carries the match count of the winner for free.  The
+// BLOSUM62 increment of a cell is a table of keys: s(a,b) * 2^16 + 2 * 2^14 +
+// (a == b), looked up in shared memory, replicated per lane so that the 32
+// lanes of a warp always hit 32 different banks.  Per cell:
+//     diag = max(Hdiag + inc, ZERO)          (__viaddmax_s32)
+//     E    = max(E_up - 2^16, H_up + OPEN_E) (__viaddmax_s32)
+//     F    = max(F_left - 2^16, H_left + OPEN_F)
+//     H    = max(diag, E, F)                 (__vimax3_s32)
+// and H's priority/tie bits are cleared before it feeds other cells.
+// The first row-major cell holding the best score is tracked per row (strict
+// '>' along the row) and the rows are merged in row order after each strip.
+// Scores use the key's top 16 bits; a pair whose best score comes within 24
+// of 32767 is re-run on the plain kernel, so no overflow reaches the output.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <cstring>
+
+#include "ck_common.cuh"
+
+namespace ck {
+
+namespace key {
+constexpr int32_t TBIT = 1 << 13;
+constexpr int32_t PU = 1 << 14;
+constexpr int32_t KU = 1 << 16;
+constexpr int32_t CLEAN = ~(TBIT | 3 * PU);
+constexpr int32_t ZKEY = 3 * PU;
+constexpr int32_t OPEN_E = GAP_OPEN * KU + 1 * PU;
+constexpr int32_t OPEN_F = GAP_OPEN * KU;
+constexpr int32_t EXT = GAP_EXTEND * KU;
+constexpr int32_t NEG_E = -16 * KU + 1 * PU + TBIT;
+constexpr int32_t NEG_F = -16 * KU + TBIT;
+constexpr int32_t ROWS_MAX = (1 << 13) - 1;
+constexpr int32_t SCORE_LIMIT = 32767 - 24;
+constexpr int32_t MATCH_MASK = (1 << 13) - 1;
+}  // namespace key
+
+constexpr int STRIP_THREADS = 256;
+constexpr int INC_ENTRIES = N_CODES * N_CODES;           // 441
+constexpr size_t INC_SMEM = (size_t)INC_ENTRIES * 32 * 4;  // replicated per lane
+
+// ----------------------------------------------------------------- tables
+__global__ void build_inc_kernel(const int8_t *sub, int32_t *inc) {
+    int t = threadIdx.x + blockIdx.x * blockDim.x;
+    if (t >= INC_ENTRIES) return;
+    int a = t / N_CODES, b = t % N_CODES;
+    int s = (a < 20 && b < 20) ? (int)sub[a * 20 + b] : -4;
+    inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0);
+}
+
+// 1 when every residue code of the sequence is <= 20.
+__global__ void seq_codes_kernel(const uint8_t *flat, const int64_t *offsets,
+                                 const int32_t *lengths, int64_t n, int64_t flat_len,
+                                 uint8_t *ok) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n;
+         q += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        int64_t o = offsets[q];
+        int32_t L = lengths[q];
+        bool good = true;
+        if (o < 0 || L < 0 || o + L > flat_len) good = false;
+        else
+            for (int32_t t = lane; t < L; t += 32) good &= flat[o + t] <= 20;
+        good = __all_sync(0xffffffffu, good);
+        if (lane == 0) ok[q] = good;
+    }
+}
+
+// Closed-form count of the band cells of a pair (the cells clustkit's loop
+// visits): rows i in [1, la] with columns max(1, i+h-w) .. min(lb, i+h+w).
+__host__ __device__ inline int64_t sum_min(int64_t a, int64_t b, int64_t c, int64_t L) {
+    // sum_{i=a}^{b} min(L, i + c)
+    if (b < a) return 0;
+    int64_t t = L - c;  // i <= t  <=>  i + c <= L
+    int64_t s = 0;
+    int64_t e1 = b < t ? b : t;
+    if (e1 >= a) s += (e1 - a + 1) * (a + e1) / 2 + (e1 - a + 1) * c;
+    int64_t s2 = a > t + 1 ? a : t + 1;
+    if (b >= s2) s += (b - s2 + 1) * L;
+    return s;
+}
+__host__ __device__ inline int64_t sum_max(int64_t a, int64_t b, int64_t c, int64_t L) {
+    // sum_{i=a}^{b} max(L, i + c)
+    if (b < a) return 0;
+    int64_t t = L - c;  // i <= t  <=>  i + c <= L  -> value L
+    int64_t s = 0;
+    int64_t e1 = b < t ? b : t;
+    if (e1 >= a) s += (e1 - a + 1) * L;
+    int64_t s2 = a > t + 1 ? a : t + 1;
+    if (b >= s2) s += (b - s2 + 1) * (s2 + b) / 2 + (b - s2 + 1) * c;
+    return s;
+}
+__host__ __device__ inline int64_t band_cells_closed(int32_t la, int32_t lb, int32_t w, int32_t h) {
+    if (la <= 0 || lb <= 0) return 0;
+    int64_t c1 = (int64_t)h - w, c2 = (int64_t)h + w;
+    int64_t ilo = 1 - c2 > 1 ? 1 - c2 : 1;           // i + c2 >= 1
+    int64_t ihi = (int64_t)lb - c1 < la ? (int64_t)lb - c1 : la;  // i + c1 <= lb
+    if (ihi < ilo) return 0;
+    return sum_min(ilo, ihi, c2, lb) - sum_max(ilo, ihi, c1, 1) + (ihi - ilo + 1);
+}
+
+// ----------------------------------------------------------------- prep
+__global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, const uint8_t *__restrict__ seq_ok,
+                               uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
+                               int32_t *__restrict__ fallback, int32_t *__restrict__ counters,
+                               unsigned long long *__restrict__ cells, int32_t *err) {
+    // counters[0] = eligible, counters[1] = fallback count
+    int64_t local_cells = 0;
+    int32_t elig = 0;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < M;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        PairGeom g = pair_geometry(in, p, err);
+        uint32_t k = 0;
+        if (!g.valid) {
+            write_result(out, in, p, 0, 0, 0, 0, 0);
+        } else if (g.la == 0 || cupy_ratio_skip(in, g.la, g.lb)) {
+            write_result(out, in, p, 0, 0, g.la, g.la, g.lb);
+        } else {
+            local_cells += band_cells_closed(g.la, g.lb, g.w, g.h);
+            if (g.la <= key::ROWS_MAX && seq_ok[g.a_idx] && seq_ok[g.b_idx]) {
+                int32_t cb = g.lb < key::ROWS_MAX ? g.lb : key::ROWS_MAX;
+                k = ((uint32_t)g.la << 13) | (uint32_t)cb;
+                elig++;
+            } else {
+                int32_t pos = atomicAdd(&counters[1], 1);
+                fallback[pos] = (int32_t)p;
+            }
+        }
+        keys[p] = k;
+        vals[p] = (uint32_t)p;
+    }
+    for (int o = 16; o; o >>= 1) {
+        local_cells += __shfl_xor_sync(0xffffffffu, local_cells, o);
+        elig += __shfl_xor_sync(0xffffffffu, elig, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (local_cells) atomicAdd(cells, (unsigned long long)local_cells);
+        if (elig) atomicAdd(&counters[0], elig);
+    }
+}
+
+// ----------------------------------------------------------------- strip kernel
+template <int R, bool MASKED>
+__device__ __forceinline__ void strip_column(
+    int32_t j, int32_t (&hc)[R], int32_t (&fT)[R], int32_t (&best)[R], int32_t (&thr)[R],
+    const uint32_t (&arow)[R], int32_t &hd0, const char *s_inc, int2 *win, int32_t wmask,
+    const uint8_t *B, int32_t lo0, uint32_t w2, int32_t alive) {
+    using namespace key;
+    int2 *slot = win + (size_t)(j & wmask) * 32;
+    const int2 bnd = *slot;
+    int32_t hu = bnd.x, eu = bnd.y;
+    const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
+    int32_t hdiag = hd0;
+    hd0 = hu;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int32_t inc = *(const int32_t *)(s_inc + arow[r] + bcol);
+        const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
+        const int32_t eT = __viaddmax_s32(eu, EXT, hu + OPEN_E) | TBIT;
+        const int32_t fTn = __viaddmax_s32(fT[r], EXT, hc[r] + OPEN_F) | TBIT;
+        int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
+        int32_t eo = eT, fo = fTn;
+        if (MASKED) {
+            const bool in = (r < alive) && ((uint32_t)(j - r - lo0) <= w2);
+            hn = in ? hn : 0;
+            eo = in ? eT : NEG_E;
+            fo = in ? fTn : NEG_F;
+        }
+        if (hn > thr[r]) {
+            best[r] = hn;
+            thr[r] = hn | (KU - 1);
+        }
+        hdiag = hc[r];
+        hc[r] = hn;
+        fT[r] = fo;
+        hu = hn;
+        eu = eo;
+    }
+    *slot = make_int2(hu, eu);
+}
+
+template <int R>
+__device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
+                                  int2 *win, int32_t W, int32_t lane, int32_t *fallback,
+                                  int32_t *fallback_count, int32_t *err) {
+    using namespace key;
+    PairGeom g = pair_geometry(in, p, err);
+    const int32_t la = g.la, lb = g.lb, w = g.w, h = g.h;
+    const uint8_t *A = in.flat + in.offsets[g.a_idx];
+    const uint8_t *B = in.flat + in.offsets[g.b_idx];
+    const int32_t wmask = W - 1;
+    const uint32_t w2 = 2u * (uint32_t)w;
+
+    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E);
+
+    int32_t gbest = 0;
+    for (int32_t i0 = 1; i0 <= la; i0 += R) {
+        const int32_t lo0 = i0 + h - w;  // unclipped first column of row i0
+        const int32_t J0 = lo0 < 1 ? 1 : lo0;
+        const int32_t hi_last = i0 + R - 1 + h + w;
+        const int32_t J1 = hi_last < lb ? hi_last : lb;
+        if (J0 > lb) break;
+        if (J1 < J0) continue;
+
+        int32_t hc[R], fT[R], best[R], thr[R];
+        uint32_t arow[R];
+        const int32_t gthr = gbest | (KU - 1);
+        const int32_t alive = la - i0 + 1 < R ? la - i0 + 1 : R;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            hc[r] = 0;
+            fT[r] = NEG_F;
+            best[r] = 0;
+            thr[r] = gthr;
+            const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : 0u;
+            arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
+        }
+        int32_t hd0 = (J0 >= 2) ? win[(size_t)((J0 - 1) & wmask) * 32].x : 0;
+
+        // interior columns: every row of the strip is alive and inside its band
+        int32_t I0 = lo0 + R - 1;
+        if (I0 < J0) I0 = J0;
+        int32_t I1 = i0 + h + w;
+        if (I1 > J1) I1 = J1;
+        if (alive == R && I0 <= I1) {
+            for (int32_t j = J0; j < I0; ++j)
+                strip_column<R, true>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+#pragma unroll 2
+            for (int32_t j = I0; j <= I1; ++j)
+                strip_column<R, false>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+            for (int32_t j = I1 + 1; j <= J1; ++j)
+                strip_column<R, true>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+        } else {
+            for (int32_t j = J0; j <= J1; ++j)
+                strip_column<R, true>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+        }
+        // rows merge in row order: strict '>' keeps the earliest row on ties
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (best[r] > (gbest | (KU - 1))) gbest = best[r];
+        // the columns right of this strip's band read as out-of-band for the next strip
+        const int32_t fill_end = J1 + R < lb ? J1 + R : lb;
+        for (int32_t j = J1 + 1; j <= fill_end; ++j)
+            win[(size_t)(j & wmask) * 32] = make_int2(0, NEG_E);
+    }
+    const int32_t score = gbest >> 16;
+    if (score >= SCORE_LIMIT) {
+        int32_t pos = atomicAdd(fallback_count, 1);
+        fallback[pos] = (int32_t)p;
+        atomicAdd(fallback_count + 2, 1);  // re-run counter
+        return;
+    }
+    write_result(out, in, p, score, gbest & MATCH_MASK, la, la, lb);
+}
+
+template <int R>
+__global__ void __launch_bounds__(STRIP_THREADS, 2)
+sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
+                const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
+                int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
+                int32_t *__restrict__ fallback, int32_t *__restrict__ fallback_count,
+                int32_t *err) {
+    extern __shared__ int32_t s_inc[];
+    for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
+    __syncthreads();
+    const int32_t lane = threadIdx.x & 31;
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int2 *win = window + (size_t)gwarp * (size_t)W * 32 + lane;
+    const int32_t n_elig = counters[0];
+    const int32_t n_groups = (n_elig + 31) >> 5;
+    for (;;) {
+        __syncwarp();
+        int32_t grp = 0;
+        if (lane == 0) grp = atomicAdd(ticket, 1);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= n_groups) break;
+        const int32_t q = grp * 32 + lane;
+        if (q < n_elig)
+            align_pair_strips<R>(in, out, (int64_t)order[q], (const char *)s_inc, win, W, lane,
+                                 fallback, fallback_count, err);
+    }
+}
+
+// ----------------------------------------------------------------- driver
+static int32_t pow2_at_least(int64_t x) {
+    int32_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+template <int R>
+static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *order,
+                             const int32_t *counters, const int32_t *inc, int32_t wmax,
+                             int32_t *ticket, int32_t *fallback, int32_t *fb_count,
+                             int32_t *err, cudaStream_t st, SwCounters *ctr) {
+    int32_t status = CK_OK;
+    auto kern = sw_strip_kernel<R>;
+    CK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)INC_SMEM));
+    int per_sm = 0;
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, STRIP_THREADS, INC_SMEM));
+    if (per_sm < 1) per_sm = 1;
+    const int32_t W = pow2_at_least(2 * (int64_t)wmax + 2 * R + 2);
+    // one window of W columns per lane; keep the total under 8 GiB
+    const size_t per_block = (size_t)STRIP_THREADS * (size_t)W * sizeof(int2);
+    int blocks = sm_count() * per_sm;
+    const size_t cap = (size_t)8 << 30;
+    if ((size_t)blocks * per_block > cap) blocks = (int)(cap / per_block);
+    if (blocks < 1) blocks = 1;
+    int2 *window = (int2 *)scratch(SLOT_WINDOW, (size_t)blocks * per_block, &status);
+    if (!window) return status;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
+    kern<<<blocks, STRIP_THREADS, INC_SMEM, st>>>(in, out, order, counters, inc, window, W, ticket,
+                                                  fallback, fb_count, err);
+    CK_CUDA(cudaGetLastError());
+    if (ev1) CK_CUDA(cudaEventRecord(ev1, st));
+    if (ctr) ctr->launches += 1;
+    return CK_OK;
+}
+
+int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int8_t *d_sub,
+                          int32_t *d_err, cudaStream_t st, SwCounters *ctr, bool read_counters) {
+    int32_t status = CK_OK;
+    if (M >= (int64_t)INT32_MAX) {
+        set_error(CK_ERR_UNSUPPORTED, "more than 2^31-1 pairs in one call");
+        return CK_ERR_UNSUPPORTED;
+    }
+    // counters: [0] eligible, [1] fallback list length, [2] ticket, [3] overflow re-runs,
+    // [4..5] cells (u64)
+    int32_t *cnt = (int32_t *)scratch(SLOT_COUNTERS, 256, &status);
+    if (!cnt) return status;
+    CK_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
+    unsigned long long *cells = (unsigned long long *)(cnt + 4);
+
+    uint8_t *ok = (uint8_t *)scratch(SLOT_SEQ_OK, (size_t)(in.n_seqs > 0 ? in.n_seqs : 1), &status);
+    if (!ok) return status;
+    if (in.n_seqs > 0) {
+        int64_t want = (in.n_seqs * 32 + 255) / 256;
+        int blocks = (int)(want < 8 * (int64_t)sm_count() ? want : 8 * (int64_t)sm_count());
+        seq_codes_kernel<<<blocks, 256, 0, st>>>(in.flat, in.offsets, in.lengths, in.n_seqs,
+                                                in.flat_len, ok);
+        CK_CUDA(cudaGetLastError());
+    }
+    int32_t *inc = (int32_t *)scratch(SLOT_INC, INC_ENTRIES * sizeof(int32_t), &status);
+    if (!inc) return status;
+    build_inc_kernel<<<(INC_ENTRIES + 127) / 128, 128, 0, st>>>(d_sub, inc);
+    CK_CUDA(cudaGetLastError());
+
+    const size_t n = (size_t)(M > 0 ? M : 1);
+    uint32_t *k0 = (uint32_t *)scratch(SLOT_SORT_KEYS, n * 4, &status);
+    uint32_t *v0 = (uint32_t *)scratch(SLOT_SORT_VALS, n * 4, &status);
+    uint32_t *k1 = (uint32_t *)scratch(SLOT_SORT_KEYS_ALT, n * 4, &status);
+    uint32_t *v1 = (uint32_t *)scratch(SLOT_SORT_VALS_ALT, n * 4, &status);
+    int32_t *fb = (int32_t *)scratch(SLOT_FALLBACK, n * 4, &status);
+    if (!k0 || !v0 || !k1 || !v1 || !fb) return status;
+    if (ctr) ctr->launches += 2;
+    if (M > 0) {
+        int64_t want = (M + 255) / 256;
+        int blocks = (int)(want < 16 * (int64_t)sm_count() ? want : 16 * (int64_t)sm_count());
+        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, d_err);
+        CK_CUDA(cudaGetLastError());
+        cub::DoubleBuffer<uint32_t> dk(k0, k1), dv(v0, v1);
+        size_t temp = 0;
+        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, temp, dk, dv, (int)M, 0, 26, st));
+        void *tmp = scratch(SLOT_SORT_TEMP, temp > 0 ? temp : 1, &status);
+        if (!tmp) return status;
+        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, dk, dv, (int)M, 0, 26, st));
+        int32_t wmax = 0;
+        CK_TRY(widest_band(in, st, &wmax));
+        CK_TRY(launch_strips<16>(in, out, dv.Current(), cnt, inc, wmax, cnt + 2, fb, cnt + 1,
+                                 d_err, st, ctr));
+        if (ctr) ctr->launches += 1;
+    }
+    // plain kernel over the fallback list (its length is read on the device)
+    CK_TRY(sw_plain_launch(in, out, M, fb, cnt + 1, d_err, st, ctr));
+    if (read_counters && ctr) {
+        int32_t hcnt[8];
+        CK_CUDA(cudaMemcpyAsync(hcnt, cnt, 32, cudaMemcpyDeviceToHost, st));
+        CK_CUDA(cudaStreamSynchronize(st));
+        unsigned long long c = 0;
+        memcpy(&c, hcnt + 4, sizeof(c));
+        ctr->batched += hcnt[0];
+        ctr->plain += hcnt[1];
+        ctr->rerun += hcnt[3];
+        ctr->cells += (int64_t)c;
+    }
+    return CK_OK;
+}
+
+}  // namespace ck

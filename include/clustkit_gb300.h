@@ -1,0 +1,161 @@
+/*
+ * clustkit_gb300.h -- C ABI of libckgpu.so, the GB300 (sm_103a) Align-phase
+ * and sketch engine for clustkit.
+ *
+ * Conventions
+ *   - Every ck_* entry point returns an int status (CK_OK on success) and
+ *     never aborts; ck_last_error() returns a message for the calling thread.
+ *   - Host-buffer entry points copy inputs to the GPU, run, copy outputs back
+ *     and return after the results are in the caller's buffers.
+ *   - *_device entry points take device pointers and a cudaStream_t (passed as
+ *     void*, NULL = the legacy default stream) and return once the work is
+ *     enqueued; results are ready when that stream is synchronised.  Input
+ *     errors found on the GPU are reported through ck_sw_status_device().
+ *   - Pair lists are int32 [M][2]; sequences use clustkit's compact layout
+ *     (clustkit/io.py:35-131): uint8 codes `flat`, int64 `offsets[N]`,
+ *     int32 `lengths[N]`.  Protein codes are 0..19, unknown residues 20.
+ *   - Reference paths are relative to the clustkit project root.
+ */
+#ifndef CLUSTKIT_GB300_H
+#define CLUSTKIT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define CK_OK                    0
+#define CK_ERR_INVALID_ARGUMENT  1  /* NULL pointer, negative size, bad enum value   */
+#define CK_ERR_OUT_OF_RANGE      2  /* pair index, offset or length outside the inputs */
+#define CK_ERR_CUDA              3  /* CUDA runtime failure (message in ck_last_error) */
+#define CK_ERR_OUT_OF_MEMORY     4
+#define CK_ERR_UNSUPPORTED       5  /* parameter outside what the kernels implement   */
+#define CK_ERR_NO_DEVICE         6
+
+/* --------------------------------------------------- pass / fail rules
+ * clustkit decides pass/fail differently on each of its three SW paths; the
+ * rule is chosen per call so every one of them can be reproduced exactly.
+ * identity = (float)matches / (float)shorter, 0 when score <= 0.            */
+#define CK_PASS_CPU    0  /* identity >= t           (clustkit/pairwise.py:107, C path)     */
+#define CK_PASS_NUMBA  1  /* score > 0 && identity>=t (clustkit/pairwise.py:679 and :1182)  */
+#define CK_PASS_CUPY   2  /* shorter/longer >= t (else not aligned) && identity >= t
+                             (clustkit/pairwise.py:1246-1252, :1393-1400)                   */
+#define CK_PASS_SCORE  3  /* score > 0                (clustkit/csrc/sw_align.c:260)        */
+
+/* --------------------------------------------------------- SW engines */
+#define CK_SW_BATCHED  0  /* length-binned persistent strip kernel + work queue (default);
+                             pairs it cannot take run on the plain kernel                  */
+#define CK_SW_PLAIN    1  /* one unbinned launch per chunk, one thread per pair             */
+
+int32_t ck_version(void);
+const char *ck_last_error(void);
+/* status of the last call made through the clustkit-compatible entry points
+ * below (they return void, as clustkit's own C functions do) */
+int32_t ck_last_status(void);
+int32_t ck_device_count(void);
+
+/* ------------------------------------------------ clustkit-compatible ABI
+ * Same symbol names, argument lists and output meaning as clustkit's C
+ * extension, so clustkit's ctypes loader (clustkit/pairwise.py:41-66) can
+ * bind this library in place of csrc/sw_align.so unchanged.
+ *
+ * batch_sw_align_c: replaces clustkit/csrc/sw_align.c:182-195.  Host buffers.
+ *   out_sims = identity, out_scores = best local score, out_mask = score > 0.
+ *   The GPU path is always used; on failure the outputs are zeroed and
+ *   ck_last_status()/ck_last_error() describe the error.
+ * sw_set_num_threads: replaces clustkit/csrc/sw_align.c:19-21.  Accepted and
+ *   ignored (the work runs on the GPU).                                      */
+void batch_sw_align_c(const int32_t *pairs, const uint8_t *flat_sequences,
+                      const int64_t *offsets, const int32_t *lengths, int32_t M,
+                      int32_t band_width, const int8_t *sub_matrix, float threshold,
+                      const int32_t *diag_hints, float *out_sims, int32_t *out_scores,
+                      uint8_t *out_mask);
+void sw_set_num_threads(int32_t n);
+
+/* ------------------------------------------------------------- SW batch
+ * ck_sw_batch: banded Smith-Waterman over a candidate-pair list
+ * (clustkit/csrc/sw_align.c:25-266, same recurrence, tie rules and band as
+ * clustkit).  Host buffers.
+ *   n_seqs, flat_len  sizes of lengths/offsets and flat (bounds are checked)
+ *   band_width        half-width; <= 0, or a longer side <= 50, means full matrix
+ *   sub_matrix        20x20 int8, row = residue of the shorter sequence
+ *   diag_hints        NULL, or per-pair band-centre offsets (sw_align.c:237-256)
+ *   pass_rule         CK_PASS_*; engine CK_SW_*
+ *   outputs           any may be NULL: out_sims (float identity), out_scores,
+ *                     out_matches (identity numerator), out_shorter
+ *                     (denominator), out_mask (uint8 pass/fail under pass_rule) */
+int32_t ck_sw_batch(const int32_t *pairs, int64_t M, const uint8_t *flat, int64_t flat_len,
+                    const int64_t *offsets, const int32_t *lengths, int64_t n_seqs,
+                    int32_t band_width, const int8_t *sub_matrix, float threshold,
+                    const int32_t *diag_hints, int32_t pass_rule, int32_t engine,
+                    float *out_sims, int32_t *out_scores, int32_t *out_matches,
+                    int32_t *out_shorter, uint8_t *out_mask);
+
+/* Device-pointer form of ck_sw_batch.  Scratch memory is managed by the
+ * library per device.  Errors detected on the GPU (pair index or sequence
+ * extent out of range) are latched in a per-device flag read by
+ * ck_sw_status_device(). */
+int32_t ck_sw_batch_device(const int32_t *d_pairs, int64_t M, const uint8_t *d_flat,
+                           int64_t flat_len, const int64_t *d_offsets,
+                           const int32_t *d_lengths, int64_t n_seqs, int32_t band_width,
+                           const int8_t *sub_matrix_host, float threshold,
+                           const int32_t *d_diag_hints, int32_t pass_rule, int32_t engine,
+                           float *d_sims, int32_t *d_scores, int32_t *d_matches,
+                           int32_t *d_shorter, uint8_t *d_mask, void *stream);
+/* Synchronises `stream`, returns CK_OK or CK_ERR_OUT_OF_RANGE for the GPU
+ * checks of the ck_*_device calls since the previous ck_sw_status_device on
+ * this device, and clears the flag. */
+int32_t ck_sw_status_device(void *stream);
+
+/* Work counters of the last ck_sw_batch / ck_sw_batch_device call on this
+ * thread: out[0] pairs, out[1] DP cells (the band cells clustkit computes),
+ * out[2] pairs taken by the batched kernel, out[3] pairs run on the plain
+ * kernel, out[4] pairs re-run after a score overflowed the packed lane,
+ * out[5] kernel launches issued. */
+int32_t ck_sw_last_counters(int64_t *out6);
+
+/* Kernel timing for measurement: after ck_sw_profile(1), every SW call
+ * records CUDA events on its stream around its dominant kernel (the strip
+ * kernel for CK_SW_BATCHED, the plain kernel for CK_SW_PLAIN);
+ * ck_sw_last_kernel_ms waits for the last one and returns its duration in
+ * milliseconds (-1 if none was recorded). */
+int32_t ck_sw_profile(int32_t enable);
+int32_t ck_sw_last_kernel_ms(float *out_ms);
+
+/* ------------------------------------------------------------- sketches
+ * Bottom-s MinHash sketches (clustkit/sketch.py:17-183): k-mer value in base
+ * `alphabet` (20 protein, 4 nucleotide), hash fmix64(value ^ seed), the s
+ * smallest hashes sorted, UINT64_MAX padding, s zeros when length < k.
+ * out is uint64 [N][s].  1 <= k <= 32, 1 <= s <= 4096. */
+int32_t ck_sketch(const uint8_t *flat, int64_t flat_len, const int64_t *offsets,
+                  const int32_t *lengths, int64_t N, int32_t k, int32_t s,
+                  int32_t alphabet, uint64_t seed, uint64_t *out);
+int32_t ck_sketch_device(const uint8_t *d_flat, int64_t flat_len, const int64_t *d_offsets,
+                         const int32_t *d_lengths, int64_t N, int32_t k, int32_t s,
+                         int32_t alphabet, uint64_t seed, uint64_t *d_out, void *stream);
+
+/* -------------------------------------------------------------- Jaccard
+ * Merge-walk Jaccard of sorted sketches (clustkit/pairwise.py:1564-1612) and
+ * the pre-filter mask sims >= floor (clustkit/pairwise.py:949-1001, float32
+ * comparison).  sketches uint64 [N][s]; out_sims float [M]; out_mask uint8
+ * [M] (may be NULL). */
+int32_t ck_jaccard(const int32_t *pairs, int64_t M, const uint64_t *sketches, int64_t N,
+                   int32_t s, float floor, float *out_sims, uint8_t *out_mask);
+int32_t ck_jaccard_device(const int32_t *d_pairs, int64_t M, const uint64_t *d_sketches,
+                          int64_t N, int32_t s, float floor, float *d_sims,
+                          uint8_t *d_mask, void *stream);
+
+/* ---------------------------------------------------- measurement probe
+ * Sustained lane-operation rate of one integer instruction class on the
+ * current device, used as the roofline denominator of the SW kernels.
+ * which: 0 = __viaddmax_s32, 1 = __vimax3_s32, 2 = 32-bit add (IADD3),
+ * 3 = __viaddmax_s16x2 (2 lane-ops per instruction).  Writes lane-ops/s. */
+int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLUSTKIT_GB300_H */

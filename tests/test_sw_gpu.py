@@ -1,0 +1,218 @@
+"""GPU Smith-Waterman (both engines) against the reference's outputs and the oracle.
+
+Bit-exact integer parity: scores, identity numerator and denominator, the
+float32 identity (matches/shorter, correctly rounded) and pass/fail.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from clustkit_gb300 import synth
+from clustkit_gb300.blosum import BLOSUM62
+from clustkit_gb300.pairwise import (ENGINE_BATCHED, ENGINE_PLAIN, PASS_CPU, PASS_CUPY, PASS_NUMBA,
+                                     PASS_SCORE, batch_sw)
+
+pytestmark = pytest.mark.gpu
+ENGINES = [ENGINE_BATCHED, ENGINE_PLAIN]
+
+
+def _same(gpu, ref, keys=("scores", "matches", "shorter")):
+    for k in keys:
+        assert np.array_equal(gpu[k], ref[k]), k
+    assert np.array_equal(gpu["sims"].view(np.uint32), ref["sims"].view(np.uint32))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("bw", [0, 1, 2, 3, 8, 16, 32, 50, 64, 100, 128, 1000])
+def test_golden_reference_c(ck, golden, engine, bw):
+    g = golden("sw_golden.npz")
+    r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62, 0.0,
+                 pass_rule=PASS_SCORE, engine=engine)
+    assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
+    assert np.array_equal(r["sims"].view(np.uint32), g[f"bw{bw}_sims"].view(np.uint32))
+    assert np.array_equal(r["mask"], g[f"bw{bw}_mask"].astype(bool))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("bw", [8, 32, 100])
+def test_golden_diagonal_hints(ck, golden, engine, bw):
+    g = golden("sw_golden.npz")
+    r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62,
+                 diag_hints=g["hints"], engine=engine)
+    assert np.array_equal(r["scores"], g[f"hint_bw{bw}_scores"])
+    assert np.array_equal(r["sims"], g[f"hint_bw{bw}_sims"])
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_golden_numba_twin(ck, golden, engine):
+    g = golden("sw_golden.npz")
+    idx = g["twin_idx"]
+    r = batch_sw(g["pairs"][idx], g["flat"], g["offsets"], g["lengths"], int(g["twin_bw"]),
+                 BLOSUM62, 0.5, pass_rule=PASS_NUMBA, engine=engine)
+    assert np.array_equal(r["scores"], g["twin_scores"])
+    assert np.array_equal(r["sims"], g["twin_sims"])
+    assert np.array_equal(r["mask"], g["twin_mask"] & (g["twin_sims"] >= np.float32(0.5)))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("bw,median,hi,dist", [(100, 300, 800, "lognormal"), (32, 350, 2000, "lognormal"),
+                                               (16, 200, 3000, "pareto"), (64, 120, 400, "lognormal")])
+def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist):
+    s = synth.generate_families(30, 8, median=median, lo=30, hi=hi, seed=bw + median,
+                                length_dist=dist)
+    pairs = synth.mixed_pairs(s, 4000, seed=bw, min_ratio=0.0)
+    ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
+    r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, 0.3, engine=engine)
+    _same(r, ref)
+    assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
+
+
+def test_engines_agree_and_counters(ck):
+    s = synth.generate_families(40, 10, median=350, lo=30, hi=2000, seed=9)
+    pairs = synth.mixed_pairs(s, 20000, seed=2)
+    a = batch_sw(pairs, s.flat, s.offsets, s.lengths, 100, engine=ENGINE_BATCHED)
+    c = ck.sw_counters()
+    b = batch_sw(pairs, s.flat, s.offsets, s.lengths, 100, engine=ENGINE_PLAIN)
+    _same(a, b)
+    assert c["pairs"] == len(pairs)
+    assert c["batched"] == len(pairs) and c["plain"] == 0
+    assert c["cells"] > 0
+
+
+def test_long_rows_and_unknown_codes_use_fallback(ck):
+    rng = np.random.default_rng(4)
+    seqs = [rng.integers(0, 20, 8300).astype(np.uint8),   # rows > 8191 -> plain kernel
+            rng.integers(0, 20, 8250).astype(np.uint8),
+            rng.integers(0, 26, 400).astype(np.uint8),    # codes > 20 -> plain kernel
+            rng.integers(0, 20, 390).astype(np.uint8),
+            rng.integers(0, 20, 3000).astype(np.uint8)]
+    seqs[1][:4000] = seqs[0][:4000]
+    seqs[4][:2000] = seqs[0][:2000]
+    lengths = np.array([len(x) for x in seqs], np.int32)
+    offsets = np.concatenate([[0], np.cumsum(lengths[:-1])]).astype(np.int64)
+    flat = np.concatenate(seqs)
+    pairs = np.array([[0, 1], [1, 0], [2, 3], [3, 2], [0, 4], [4, 1], [2, 2], [0, 0]], np.int32)
+    for bw in (32, 100):
+        ref = oracle.sw_batch(pairs, flat, offsets, lengths, bw, BLOSUM62)
+        r = batch_sw(pairs, flat, offsets, lengths, bw, BLOSUM62)
+        _same(r, ref)
+    c = ck.sw_counters()
+    assert c["plain"] >= 5
+
+
+def test_score_overflow_reruns_exactly(ck):
+    # a W-rich self-alignment of 3200 rows scores 11*... > 32767 -> packed lane overflow guard
+    seq = np.full(3300, 18, np.uint8)  # W
+    seq[::5] = 4
+    lengths = np.array([3300, 3300], np.int32)
+    offsets = np.array([0, 3300], np.int64)
+    flat = np.concatenate([seq, seq])
+    pairs = np.array([[0, 1], [1, 0], [0, 0]], np.int32)
+    ref = oracle.sw_batch(pairs, flat, offsets, lengths, 100, BLOSUM62)
+    assert ref["scores"].max() > 32767
+    r = batch_sw(pairs, flat, offsets, lengths, 100, BLOSUM62)
+    _same(r, ref)
+
+
+@pytest.mark.parametrize("rule", [PASS_CPU, PASS_NUMBA, PASS_CUPY, PASS_SCORE])
+@pytest.mark.parametrize("t", [0.0, 0.3, 0.5, 0.9])
+def test_pass_rules(ck, rule, t):
+    s = synth.generate_families(20, 6, median=200, lo=20, hi=600, seed=13)
+    pairs = synth.mixed_pairs(s, 3000, seed=21)
+    ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, 50, BLOSUM62)
+    r = batch_sw(pairs, s.flat, s.offsets, s.lengths, 50, BLOSUM62, t, pass_rule=rule)
+    tf = np.float32(t)
+    if rule == PASS_CPU:
+        want = ref["sims"] >= tf
+    elif rule == PASS_NUMBA:
+        want = (ref["scores"] > 0) & (ref["sims"] >= tf)
+    elif rule == PASS_SCORE:
+        want = ref["scores"] > 0
+    else:
+        li, lj = s.lengths[pairs[:, 0]], s.lengths[pairs[:, 1]]
+        ratio = np.minimum(li, lj).astype(np.float32) / np.maximum(li, lj).astype(np.float32)
+        aligned = ~((np.maximum(li, lj) > 0) & (ratio < tf))
+        want = aligned & (ref["scores"] > 0) & (ref["sims"] >= tf)
+        # pairs that fail the ratio are not aligned (clustkit/pairwise.py:1246-1252)
+        assert np.all(r["sims"][~aligned] == 0)
+        _same({k: v[aligned] for k, v in r.items()}, {k: v[aligned] for k, v in ref.items()},
+              keys=("scores", "matches"))
+    assert np.array_equal(r["mask"], want)
+
+
+def test_empty_and_degenerate_inputs(ck):
+    r = batch_sw(np.zeros((0, 2), np.int32), np.zeros(0, np.uint8), np.zeros(0, np.int64),
+                 np.zeros(0, np.int32))
+    assert r["sims"].shape == (0,)
+    flat = np.array([1, 2, 3], np.uint8)
+    offsets = np.array([0, 0, 3], np.int64)
+    lengths = np.array([3, 0, 0], np.int32)
+    pairs = np.array([[0, 1], [1, 2], [0, 0], [2, 0]], np.int32)
+    r = batch_sw(pairs, flat, offsets, lengths, 100)
+    ref = oracle.sw_batch(pairs, flat, offsets, lengths, 100, BLOSUM62)
+    _same(r, ref)
+
+
+def test_out_of_range_inputs_report_errors(ck):
+    from clustkit_gb300._lib import CK_ERR_OUT_OF_RANGE, CkError
+    flat = np.arange(20, dtype=np.uint8)
+    offsets = np.array([0, 10], np.int64)
+    lengths = np.array([10, 10], np.int32)
+    with pytest.raises(CkError) as e:
+        batch_sw(np.array([[0, 2]], np.int32), flat, offsets, lengths)
+    assert e.value.status == CK_ERR_OUT_OF_RANGE
+    with pytest.raises(CkError) as e:
+        batch_sw(np.array([[0, 1]], np.int32), flat, offsets, np.array([10, 11], np.int32))
+    assert e.value.status == CK_ERR_OUT_OF_RANGE
+    # the library stays usable after reporting
+    r = batch_sw(np.array([[0, 1]], np.int32), flat, offsets, lengths)
+    assert r["shorter"][0] == 10
+
+
+def test_clustkit_compatible_symbol(ck, golden):
+    """batch_sw_align_c with clustkit's own ctypes argtypes (clustkit/pairwise.py:50-58)."""
+    g = golden("sw_golden.npz")
+    lib = ck.load()
+    pairs = np.ascontiguousarray(g["pairs"].reshape(-1), np.int32)
+    M = len(pairs) // 2
+    sims = np.empty(M, np.float32)
+    scores = np.empty(M, np.int32)
+    mask = np.empty(M, np.uint8)
+    sub = np.ascontiguousarray(BLOSUM62)
+    lib.sw_set_num_threads(8)
+    lib.batch_sw_align_c(pairs.ctypes.data, g["flat"].ctypes.data, g["offsets"].ctypes.data,
+                         g["lengths"].ctypes.data, M, 100, sub.ctypes.data, ctypes.c_float(0.5),
+                         None, sims.ctypes.data, scores.ctypes.data, mask.ctypes.data)
+    assert lib.ck_last_status() == 0
+    assert np.array_equal(scores, g["bw100_scores"])
+    assert np.array_equal(sims, g["bw100_sims"])
+    assert np.array_equal(mask, g["bw100_mask"])
+
+
+def test_device_pointer_entry_point(ck):
+    torch = pytest.importorskip("torch")
+    s = synth.generate_families(20, 8, median=300, lo=50, hi=800, seed=31)
+    pairs = synth.mixed_pairs(s, 5000, seed=8)
+    ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, 100, BLOSUM62)
+    dev = torch.device("cuda:0")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_pairs, d_flat, d_off, d_len = t(pairs), t(s.flat), t(s.offsets), t(s.lengths)
+    M = len(pairs)
+    d_sims = torch.empty(M, dtype=torch.float32, device=dev)
+    d_scores = torch.empty(M, dtype=torch.int32, device=dev)
+    d_matches = torch.empty(M, dtype=torch.int32, device=dev)
+    sub = np.ascontiguousarray(BLOSUM62)
+    lib = ck.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    for engine in ENGINES:
+        st = lib.ck_sw_batch_device(d_pairs.data_ptr(), M, d_flat.data_ptr(), len(s.flat),
+                                    d_off.data_ptr(), d_len.data_ptr(), s.n, 100, sub.ctypes.data,
+                                    0.5, None, PASS_CPU, engine, d_sims.data_ptr(),
+                                    d_scores.data_ptr(), d_matches.data_ptr(), None, None, stream)
+        assert st == 0
+        assert lib.ck_sw_status_device(stream) == 0
+        assert np.array_equal(d_scores.cpu().numpy(), ref["scores"])
+        assert np.array_equal(d_matches.cpu().numpy(), ref["matches"])
+        assert np.array_equal(d_sims.cpu().numpy(), ref["sims"])
