@@ -260,6 +260,8 @@ def run_ours(args, world, rank, local):
         dist.init_process_group("nccl")
     lib = _lib.load()
     _lib.require_gpu()
+    if args.rows:
+        _lib.set_config(_lib.CFG_ROWS_PER_STRIP, args.rows)
     s, pairs, n_cand = build_workload(use_gpu=True, quick=args.quick)
     pairs = shard(pairs, world, rank)
     M = len(pairs)
@@ -317,6 +319,14 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     lib.ck_sw_profile(0)
     res_b = {k: v.cpu().numpy() for k, v in out.items()}
+    sweep = {}
+    if args.sweep:
+        keep_rows = _lib.get_config(_lib.CFG_ROWS_PER_STRIP)
+        for rows in (8, 16, 24):
+            _lib.set_config(_lib.CFG_ROWS_PER_STRIP, rows)
+            t_r, _ = timed(ENGINE_BATCHED, 3, 1)
+            sweep[rows] = cells / (t_r / 3) / 1e9
+        _lib.set_config(_lib.CFG_ROWS_PER_STRIP, keep_rows)
     # ---- plain engine (the plain GPU form), same pairs
     plain_steps = max(1, min(args.steps, 3))
     lib.ck_sw_profile(1)
@@ -366,10 +376,12 @@ def run_ours(args, world, rank, local):
     # ---- roofline (integer issue bound) and CPU baseline
     peak = np.zeros(1, np.float64)
     rates = {}
-    for which, name in ((0, "viaddmax_s32"), (1, "vimax3_s32"), (2, "iadd_s32"), (3, "viaddmax_s16x2")):
+    for which, name in ((0, "viaddmax_s32"), (1, "vimax3_s32"), (2, "iadd3_s32"), (3, "viaddmax_s16x2"),
+                        (4, "lop3_b32"), (5, "imad_s32")):
         _lib.check(lib.ck_probe_int_rate(which, peak.ctypes.data))
         rates[name] = float(peak[0])
-    p_int32 = max(rates["viaddmax_s32"], rates["iadd_s32"], rates["vimax3_s32"])
+    # the recurrence's max-plus ops are DPX instructions: their measured rate is the roof
+    p_int32 = rates["viaddmax_s32"]
     kernel_s = float(np.mean(kt)) / 1e3 if kt and min(kt) > 0 else t_batched / args.steps
     gcups_kernel = cells / kernel_s / 1e9
     achieved = gcups_kernel * OPS_PER_CELL  # Gop/s
@@ -404,6 +416,8 @@ def run_ours(args, world, rank, local):
                      "probe_gops": {k: v / 1e9 for k, v in rates.items()},
                      "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL)},
         "cpu_baseline": cpu,
+        "rows_per_strip": _lib.get_config(_lib.CFG_ROWS_PER_STRIP),
+        "sweep_gcups_by_rows": sweep or None,
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -422,6 +436,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="10x smaller workload (smoke-testing the bench)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24); 0 = library default")
+    ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip setting")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

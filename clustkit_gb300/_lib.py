@@ -23,6 +23,7 @@ CK_ERR_NO_DEVICE = 6
 
 PASS_CPU, PASS_NUMBA, PASS_CUPY, PASS_SCORE = 0, 1, 2, 3
 ENGINE_BATCHED, ENGINE_PLAIN = 0, 1
+CFG_ROWS_PER_STRIP = 0
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -49,6 +50,8 @@ SIGNATURES = {
     "ck_probe_int_rate": (_I32, [_I32, _P]),
     "ck_sw_profile": (_I32, [_I32]),
     "ck_sw_last_kernel_ms": (_I32, [_P]),
+    "ck_sw_set_config": (_I32, [_I32, _I32]),
+    "ck_sw_get_config": (_I32, [_I32, _P]),
 }
 
 
@@ -105,3 +108,13 @@ def sw_counters() -> dict:
     check(load().ck_sw_last_counters(out.ctypes.data))
     keys = ("pairs", "cells", "batched", "plain", "rerun", "launches")
     return {k: int(v) for k, v in zip(keys, out)}
+
+
+def set_config(key: int, value: int) -> None:
+    check(load().ck_sw_set_config(int(key), int(value)))
+
+
+def get_config(key: int) -> int:
+    v = np.zeros(1, np.int32)
+    check(load().ck_sw_get_config(int(key), v.ctypes.data))
+    return int(v[0])

@@ -356,6 +356,22 @@ int32_t ck_sw_last_kernel_ms(float *out_ms) {
     return CK_OK;
 }
 
+int32_t ck_sw_set_config(int32_t key, int32_t value) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    if (key == CK_CFG_ROWS_PER_STRIP) return sw_set_rows_per_strip(value);
+    set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
+    return CK_ERR_INVALID_ARGUMENT;
+}
+
+int32_t ck_sw_get_config(int32_t key, int32_t *value) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!value) return CK_ERR_INVALID_ARGUMENT;
+    if (key == CK_CFG_ROWS_PER_STRIP) { *value = sw_rows_per_strip(); return CK_OK; }
+    set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
+    return CK_ERR_INVALID_ARGUMENT;
+}
+
 int32_t ck_sw_status_device(void *stream) {
     std::lock_guard<std::mutex> lock(g_mutex);
     return read_and_clear_error((cudaStream_t)stream);

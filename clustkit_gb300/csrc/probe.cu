@@ -3,9 +3,10 @@
 // roofline denominator for the SW kernels, which are bound by integer issue,
 // not by HBM or tensor throughput.
 //
-// Each thread runs 8 independent dependency chains of one instruction for
-// `iters` iterations (enough independent work per warp to hide the
-// instruction latency), over a grid of 8 CTAs x 1024 threads per SM.
+// Each thread keeps 8 registers and updates each from two others per step
+// (x[q] = op(x[q], x[q+1], x[q+3])), so no chain can be folded at compile
+// time and every warp has 8-way independent work; the grid is 2 CTAs x 1024
+// threads per SM.
 #include "ck_common.cuh"
 
 namespace ck {
@@ -13,18 +14,20 @@ namespace ck {
 template <int WHICH>
 __global__ void __launch_bounds__(1024) probe_kernel(int32_t iters, int32_t seed, int32_t *sink) {
     int32_t x[8];
-    const int32_t b = seed ^ (int32_t)threadIdx.x, c = seed * 3 + 1;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) x[q] = (int32_t)(threadIdx.x * 8 + q) ^ seed;
+    for (int q = 0; q < 8; ++q) x[q] = (int32_t)(threadIdx.x * 8 + q) ^ (seed * (q + 1));
     for (int32_t it = 0; it < iters; ++it) {
 #pragma unroll
         for (int u = 0; u < 16; ++u) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                if (WHICH == 0) x[q] = __viaddmax_s32(x[q], b, c + q);
-                else if (WHICH == 1) x[q] = __vimax3_s32(x[q] - 1, b, c + q);
-                else if (WHICH == 2) x[q] = x[q] + b + q;
-                else x[q] = (int32_t)__viaddmax_s16x2((uint32_t)x[q], (uint32_t)b, (uint32_t)(c + q));
+                const int32_t b = x[(q + 1) & 7], c = x[(q + 3) & 7];
+                if (WHICH == 0) x[q] = __viaddmax_s32(x[q], b, c);
+                else if (WHICH == 1) x[q] = __vimax3_s32(x[q], b, c);
+                else if (WHICH == 2) x[q] = x[q] + b + c;
+                else if (WHICH == 3) x[q] = (int32_t)__viaddmax_s16x2((uint32_t)x[q], (uint32_t)b, (uint32_t)c);
+                else if (WHICH == 4) x[q] = (x[q] & b) ^ c;
+                else x[q] = x[q] * b + c;
             }
         }
     }
@@ -39,7 +42,7 @@ __global__ void __launch_bounds__(1024) probe_kernel(int32_t iters, int32_t seed
 using namespace ck;
 
 extern "C" int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s) {
-    if (!out_ops_per_s || which < 0 || which > 3) {
+    if (!out_ops_per_s || which < 0 || which > 5) {
         set_error(CK_ERR_INVALID_ARGUMENT, "probe: bad argument");
         return CK_ERR_INVALID_ARGUMENT;
     }
@@ -47,7 +50,7 @@ extern "C" int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s) {
     int32_t *sink = (int32_t *)scratch(SLOT_MAXLEN, 64, &status);
     if (!sink) return status;
     const int blocks = sm_count() * 2, threads = 1024;
-    const int32_t iters = 2048;
+    const int32_t iters = 1024;
     cudaEvent_t e0, e1;
     CK_CUDA(cudaEventCreate(&e0));
     CK_CUDA(cudaEventCreate(&e1));
@@ -58,7 +61,9 @@ extern "C" int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s) {
             case 0: probe_kernel<0><<<blocks, threads>>>(iters, rep + 7, sink); break;
             case 1: probe_kernel<1><<<blocks, threads>>>(iters, rep + 7, sink); break;
             case 2: probe_kernel<2><<<blocks, threads>>>(iters, rep + 7, sink); break;
-            default: probe_kernel<3><<<blocks, threads>>>(iters, rep + 7, sink); break;
+            case 3: probe_kernel<3><<<blocks, threads>>>(iters, rep + 7, sink); break;
+            case 4: probe_kernel<4><<<blocks, threads>>>(iters, rep + 7, sink); break;
+            default: probe_kernel<5><<<blocks, threads>>>(iters, rep + 7, sink); break;
         }
         CK_CUDA(cudaGetLastError());
         CK_CUDA(cudaEventRecord(e1, 0));
@@ -71,7 +76,6 @@ extern "C" int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s) {
     cudaEventDestroy(e1);
     const double instr = (double)blocks * threads * iters * 16.0 * 8.0;
     const double lanes = which == 3 ? 2.0 : 1.0;
-    // the vimax3 probe also issues one add per op; count only the max
     *out_ops_per_s = instr * lanes / (best_ms * 1e-3);
     return CK_OK;
 }

@@ -164,24 +164,41 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, const uint8_t *__r
 }
 
 // ----------------------------------------------------------------- strip kernel
+// Registers of one lane for the strip in flight.
+template <int R>
+struct StripRegs {
+    int32_t hc[R];     // H (clean key) of row r at the last column done
+    int32_t fT[R];     // F key (tie bit set) of row r at the last column done
+    uint32_t arow[R];  // byte offset of row r's residue block in the increment table
+    int32_t hd0;       // H(i0 - 1, j - 1): diagonal input of the strip's first row
+    int2 bnd_n;        // window entry (row i0 - 1) prefetched for the next column
+    uint32_t bcol_n;   // residue offset of the next column's b, prefetched
+};
+
+// One column j of a strip: R cells, top to bottom.  The first-max trackers
+// (one per row, in shared memory) are touched only when some lane's column
+// maximum beats the best score its pair had when the strip began, which is
+// the only way any of its rows can record a new first maximum.
 template <int R, bool MASKED>
-__device__ __forceinline__ void strip_column(
-    int32_t j, int32_t (&hc)[R], int32_t (&fT)[R], int32_t (&best)[R], int32_t (&thr)[R],
-    const uint32_t (&arow)[R], int32_t &hd0, const char *s_inc, int2 *win, int32_t wmask,
-    const uint8_t *B, int32_t lo0, uint32_t w2, int32_t alive) {
+__device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
+                                             const char *s_inc, int2 *win, int32_t wmask,
+                                             const uint8_t *B, int32_t lo0, uint32_t w2,
+                                             int32_t alive, int32_t gthr, int32_t *s_best) {
     using namespace key;
+    const int2 bnd = S.bnd_n;
+    const uint32_t bcol = S.bcol_n;
     int2 *slot = win + (size_t)(j & wmask) * 32;
-    const int2 bnd = *slot;
+    S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
+    S.bcol_n = (uint32_t)__ldg(B + jb_next - 1) * 128u;
     int32_t hu = bnd.x, eu = bnd.y;
-    const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
-    int32_t hdiag = hd0;
-    hd0 = hu;
+    int32_t hdiag = S.hd0;
+    S.hd0 = hu;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        const int32_t inc = *(const int32_t *)(s_inc + arow[r] + bcol);
+        const int32_t inc = *(const int32_t *)(s_inc + S.arow[r] + bcol);
         const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
         const int32_t eT = __viaddmax_s32(eu, EXT, hu + OPEN_E) | TBIT;
-        const int32_t fTn = __viaddmax_s32(fT[r], EXT, hc[r] + OPEN_F) | TBIT;
+        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, S.hc[r] + OPEN_F) | TBIT;
         int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
         int32_t eo = eT, fo = fTn;
         if (MASKED) {
@@ -190,23 +207,30 @@ __device__ __forceinline__ void strip_column(
             eo = in ? eT : NEG_E;
             fo = in ? fTn : NEG_F;
         }
-        if (hn > thr[r]) {
-            best[r] = hn;
-            thr[r] = hn | (KU - 1);
-        }
-        hdiag = hc[r];
-        hc[r] = hn;
-        fT[r] = fo;
+        hdiag = S.hc[r];
+        S.hc[r] = hn;
+        S.fT[r] = fo;
         hu = hn;
         eu = eo;
     }
     *slot = make_int2(hu, eu);
+    int32_t cm = S.hc[0];
+#pragma unroll
+    for (int r = 1; r + 1 < R; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
+    if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
+    if (__any_sync(__activemask(), cm > gthr)) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int32_t b = s_best[r * STRIP_THREADS];
+            if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
+        }
+    }
 }
 
 template <int R>
 __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
-                                  int2 *win, int32_t W, int32_t lane, int32_t *fallback,
-                                  int32_t *fallback_count, int32_t *err) {
+                                  int32_t *s_best, int2 *win, int32_t W, int32_t lane,
+                                  int32_t *fallback, int32_t *fallback_count, int32_t *err) {
     using namespace key;
     PairGeom g = pair_geometry(in, p, err);
     const int32_t la = g.la, lb = g.lb, w = g.w, h = g.h;
@@ -218,6 +242,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
     for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E);
 
     int32_t gbest = 0;
+    StripRegs<R> S;
     for (int32_t i0 = 1; i0 <= la; i0 += R) {
         const int32_t lo0 = i0 + h - w;  // unclipped first column of row i0
         const int32_t J0 = lo0 < 1 ? 1 : lo0;
@@ -226,20 +251,19 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         if (J0 > lb) break;
         if (J1 < J0) continue;
 
-        int32_t hc[R], fT[R], best[R], thr[R];
-        uint32_t arow[R];
         const int32_t gthr = gbest | (KU - 1);
         const int32_t alive = la - i0 + 1 < R ? la - i0 + 1 : R;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            hc[r] = 0;
-            fT[r] = NEG_F;
-            best[r] = 0;
-            thr[r] = gthr;
+            S.hc[r] = 0;
+            S.fT[r] = NEG_F;
+            s_best[r * STRIP_THREADS] = gbest;
             const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : 0u;
-            arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
+            S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
         }
-        int32_t hd0 = (J0 >= 2) ? win[(size_t)((J0 - 1) & wmask) * 32].x : 0;
+        S.hd0 = (J0 >= 2) ? win[(size_t)((J0 - 1) & wmask) * 32].x : 0;
+        S.bnd_n = win[(size_t)(J0 & wmask) * 32];
+        S.bcol_n = (uint32_t)__ldg(B + J0 - 1) * 128u;
 
         // interior columns: every row of the strip is alive and inside its band
         int32_t I0 = lo0 + R - 1;
@@ -248,20 +272,25 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         if (I1 > J1) I1 = J1;
         if (alive == R && I0 <= I1) {
             for (int32_t j = J0; j < I0; ++j)
-                strip_column<R, true>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+                strip_column<R, true>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best);
 #pragma unroll 2
             for (int32_t j = I0; j <= I1; ++j)
-                strip_column<R, false>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+                strip_column<R, false>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
+                                       gthr, s_best);
             for (int32_t j = I1 + 1; j <= J1; ++j)
-                strip_column<R, true>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+                strip_column<R, true>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
+                                      gthr, s_best);
         } else {
             for (int32_t j = J0; j <= J1; ++j)
-                strip_column<R, true>(j, hc, fT, best, thr, arow, hd0, s_inc, win, wmask, B, lo0, w2, alive);
+                strip_column<R, true>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
+                                      gthr, s_best);
         }
         // rows merge in row order: strict '>' keeps the earliest row on ties
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-            if (best[r] > (gbest | (KU - 1))) gbest = best[r];
+        for (int r = 0; r < R; ++r) {
+            const int32_t b = s_best[r * STRIP_THREADS];
+            if (b > (gbest | (KU - 1))) gbest = b;
+        }
         // the columns right of this strip's band read as out-of-band for the next strip
         const int32_t fill_end = J1 + R < lb ? J1 + R : lb;
         for (int32_t j = J1 + 1; j <= fill_end; ++j)
@@ -278,6 +307,11 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
 }
 
 template <int R>
+__host__ __device__ constexpr size_t strip_smem() {
+    return INC_SMEM + (size_t)R * STRIP_THREADS * sizeof(int32_t);
+}
+
+template <int R>
 __global__ void __launch_bounds__(STRIP_THREADS, 2)
 sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
@@ -287,6 +321,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
     extern __shared__ int32_t s_inc[];
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
     __syncthreads();
+    int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
     const int32_t lane = threadIdx.x & 31;
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int2 *win = window + (size_t)gwarp * (size_t)W * 32 + lane;
@@ -300,7 +335,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
         if (grp >= n_groups) break;
         const int32_t q = grp * 32 + lane;
         if (q < n_elig)
-            align_pair_strips<R>(in, out, (int64_t)order[q], (const char *)s_inc, win, W, lane,
+            align_pair_strips<R>(in, out, (int64_t)order[q], (const char *)s_inc, s_best, win, W, lane,
                                  fallback, fallback_count, err);
     }
 }
@@ -312,6 +347,19 @@ static int32_t pow2_at_least(int64_t x) {
     return p;
 }
 
+// Tunables (set by ck_sw_set_config, chosen by the autotuner).
+static int32_t g_rows_per_strip = 16;
+
+int32_t sw_set_rows_per_strip(int32_t r) {
+    if (r != 8 && r != 16 && r != 24) {
+        set_error(CK_ERR_UNSUPPORTED, "rows per strip must be 8, 16 or 24");
+        return CK_ERR_UNSUPPORTED;
+    }
+    g_rows_per_strip = r;
+    return CK_OK;
+}
+int32_t sw_rows_per_strip() { return g_rows_per_strip; }
+
 template <int R>
 static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *order,
                              const int32_t *counters, const int32_t *inc, int32_t wmax,
@@ -319,9 +367,10 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
                              int32_t *err, cudaStream_t st, SwCounters *ctr) {
     int32_t status = CK_OK;
     auto kern = sw_strip_kernel<R>;
-    CK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)INC_SMEM));
+    const size_t smem = strip_smem<R>();
+    CK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, STRIP_THREADS, INC_SMEM));
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, STRIP_THREADS, smem));
     if (per_sm < 1) per_sm = 1;
     const int32_t W = pow2_at_least(2 * (int64_t)wmax + 2 * R + 2);
     // one window of W columns per lane; keep the total under 8 GiB
@@ -334,8 +383,8 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     if (!window) return status;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
-    kern<<<blocks, STRIP_THREADS, INC_SMEM, st>>>(in, out, order, counters, inc, window, W, ticket,
-                                                  fallback, fb_count, err);
+    kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
+                                              fallback, fb_count, err);
     CK_CUDA(cudaGetLastError());
     if (ev1) CK_CUDA(cudaEventRecord(ev1, st));
     if (ctr) ctr->launches += 1;
@@ -391,8 +440,18 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
         CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, dk, dv, (int)M, 0, 26, st));
         int32_t wmax = 0;
         CK_TRY(widest_band(in, st, &wmax));
-        CK_TRY(launch_strips<16>(in, out, dv.Current(), cnt, inc, wmax, cnt + 2, fb, cnt + 1,
-                                 d_err, st, ctr));
+        const uint32_t *order = dv.Current();
+        switch (g_rows_per_strip) {
+            case 8:
+                CK_TRY(launch_strips<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                break;
+            case 24:
+                CK_TRY(launch_strips<24>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                break;
+            default:
+                CK_TRY(launch_strips<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                break;
+        }
         if (ctr) ctr->launches += 1;
     }
     // plain kernel over the fallback list (its length is read on the device)

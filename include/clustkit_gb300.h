@@ -124,6 +124,13 @@ int32_t ck_sw_last_counters(int64_t *out6);
 int32_t ck_sw_profile(int32_t enable);
 int32_t ck_sw_last_kernel_ms(float *out_ms);
 
+/* Tunables of the batched engine, process-wide (the autotuner in
+ * clustkit_gb300/tune.py picks them per workload):
+ *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24 */
+#define CK_CFG_ROWS_PER_STRIP 0
+int32_t ck_sw_set_config(int32_t key, int32_t value);
+int32_t ck_sw_get_config(int32_t key, int32_t *value);
+
 /* ------------------------------------------------------------- sketches
  * Bottom-s MinHash sketches (clustkit/sketch.py:17-183): k-mer value in base
  * `alphabet` (20 protein, 4 nucleotide), hash fmix64(value ^ seed), the s
@@ -150,8 +157,9 @@ int32_t ck_jaccard_device(const int32_t *d_pairs, int64_t M, const uint64_t *d_s
 /* ---------------------------------------------------- measurement probe
  * Sustained lane-operation rate of one integer instruction class on the
  * current device, used as the roofline denominator of the SW kernels.
- * which: 0 = __viaddmax_s32, 1 = __vimax3_s32, 2 = 32-bit add (IADD3),
- * 3 = __viaddmax_s16x2 (2 lane-ops per instruction).  Writes lane-ops/s. */
+ * which: 0 = __viaddmax_s32, 1 = __vimax3_s32, 2 = 3-input 32-bit add,
+ * 3 = __viaddmax_s16x2 (2 lane-ops per instruction), 4 = 3-input logic op,
+ * 5 = 32-bit multiply-add.  Writes lane-ops/s. */
 int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s);
 
 #ifdef __cplusplus

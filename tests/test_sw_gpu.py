@@ -69,6 +69,25 @@ def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist):
     assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
 
 
+@pytest.mark.parametrize("rows", [8, 16, 24])
+@pytest.mark.parametrize("bw", [3, 32, 100, 0])
+def test_rows_per_strip_settings(ck, golden, rows, bw):
+    from clustkit_gb300._lib import CFG_ROWS_PER_STRIP, get_config, set_config
+    keep = get_config(CFG_ROWS_PER_STRIP)
+    try:
+        set_config(CFG_ROWS_PER_STRIP, rows)
+        g = golden("sw_golden.npz")
+        r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
+        assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
+        assert np.array_equal(r["sims"], g[f"bw{bw}_sims"])
+        s = synth.generate_families(25, 8, median=300, lo=30, hi=1500, seed=rows + bw)
+        pairs = synth.mixed_pairs(s, 3000, seed=rows)
+        _same(batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62),
+              oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+    finally:
+        set_config(CFG_ROWS_PER_STRIP, keep)
+
+
 def test_engines_agree_and_counters(ck):
     s = synth.generate_families(40, 10, median=350, lo=30, hi=2000, seed=9)
     pairs = synth.mixed_pairs(s, 20000, seed=2)
@@ -175,6 +194,8 @@ def test_clustkit_compatible_symbol(ck, golden):
     """batch_sw_align_c with clustkit's own ctypes argtypes (clustkit/pairwise.py:50-58)."""
     g = golden("sw_golden.npz")
     lib = ck.load()
+    # keep every array in a local: ctypes holds raw pointers only
+    flat, offsets, lengths = g["flat"], g["offsets"], g["lengths"]
     pairs = np.ascontiguousarray(g["pairs"].reshape(-1), np.int32)
     M = len(pairs) // 2
     sims = np.empty(M, np.float32)
@@ -182,8 +203,8 @@ def test_clustkit_compatible_symbol(ck, golden):
     mask = np.empty(M, np.uint8)
     sub = np.ascontiguousarray(BLOSUM62)
     lib.sw_set_num_threads(8)
-    lib.batch_sw_align_c(pairs.ctypes.data, g["flat"].ctypes.data, g["offsets"].ctypes.data,
-                         g["lengths"].ctypes.data, M, 100, sub.ctypes.data, ctypes.c_float(0.5),
+    lib.batch_sw_align_c(pairs.ctypes.data, flat.ctypes.data, offsets.ctypes.data,
+                         lengths.ctypes.data, M, 100, sub.ctypes.data, ctypes.c_float(0.5),
                          None, sims.ctypes.data, scores.ctypes.data, mask.ctypes.data)
     assert lib.ck_last_status() == 0
     assert np.array_equal(scores, g["bw100_scores"])
