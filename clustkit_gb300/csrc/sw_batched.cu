@@ -54,6 +54,14 @@ constexpr int32_t OPEN_F = GAP_OPEN * KU;
 constexpr int32_t EXT = GAP_EXTEND * KU;
 constexpr int32_t NEG_E = -16 * KU + 1 * PU + TBIT;
 constexpr int32_t NEG_F = -16 * KU + TBIT;
+// Candidates of H's maximum are compared shifted by -3*PU, so that the
+// "zero" candidate is exactly 0 and __vimax3_s32_relu supplies it; the
+// shift keeps the order of every pair of keys (all are shifted alike).
+constexpr int32_t SHIFT = -3 * PU;
+constexpr int32_t OPEN_E_S = OPEN_E + SHIFT;
+constexpr int32_t OPEN_F_S = OPEN_F + SHIFT;
+constexpr int32_t NEG_E_S = NEG_E + SHIFT;
+constexpr int32_t NEG_F_S = NEG_F + SHIFT;
 constexpr int32_t ROWS_MAX = (1 << 13) - 1;
 constexpr int32_t SCORE_LIMIT = 32767 - 24;
 constexpr int32_t MATCH_MASK = (1 << 13) - 1;
@@ -69,7 +77,7 @@ __global__ void build_inc_kernel(const int8_t *sub, int32_t *inc) {
     if (t >= INC_ENTRIES) return;
     int a = t / N_CODES, b = t % N_CODES;
     int s = (a < 20 && b < 20) ? (int)sub[a * 20 + b] : -4;
-    inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0);
+    inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0) + key::SHIFT;
 }
 
 // 1 when every residue code of the sequence is <= 20.
@@ -175,37 +183,32 @@ struct StripRegs {
     uint32_t bcol_n;   // residue offset of the next column's b, prefetched
 };
 
-// One column j of a strip: R cells, top to bottom.  The first-max trackers
-// (one per row, in shared memory) are touched only when some lane's column
-// maximum beats the best score its pair had when the strip began, which is
-// the only way any of its rows can record a new first maximum.
-template <int R, bool MASKED>
-__device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
-                                             const char *s_inc, int2 *win, int32_t wmask,
-                                             const uint8_t *B, int32_t lo0, uint32_t w2,
-                                             int32_t alive, int32_t gthr, int32_t *s_best) {
+// Cells of rows [RB, RE) at column j, top to bottom.  (hu, eu) enter as
+// H and E of row RB - 1 at column j, hdiag as H of row RB - 1 at column
+// j - 1; they leave as the values of row RE - 1.  Stored keys: H clean
+// (score * 2^16 + matches), E and F shifted with the tie bit set.
+//     diag = Hdiag + inc                  (inc holds the shift)
+//     E    = max(E_up - 2^16, H_up + OPEN_E_S) | tie
+//     F    = max(F_left - 2^16, H_left + OPEN_F_S) | tie
+//     H    = (max(diag, E, F, 0) + 3 * 2^14) & CLEAN
+template <int R, int RB, int RE, bool MASKED>
+__device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &hu, int32_t &eu,
+                                            int32_t hdiag, StripRegs<R> &S, const char *s_inc,
+                                            int32_t lo0, uint32_t w2, int32_t alive) {
     using namespace key;
-    const int2 bnd = S.bnd_n;
-    const uint32_t bcol = S.bcol_n;
-    int2 *slot = win + (size_t)(j & wmask) * 32;
-    S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
-    S.bcol_n = (uint32_t)__ldg(B + jb_next - 1) * 128u;
-    int32_t hu = bnd.x, eu = bnd.y;
-    int32_t hdiag = S.hd0;
-    S.hd0 = hu;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
+    for (int r = RB; r < RE; ++r) {
         const int32_t inc = *(const int32_t *)(s_inc + S.arow[r] + bcol);
-        const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
-        const int32_t eT = __viaddmax_s32(eu, EXT, hu + OPEN_E) | TBIT;
-        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, S.hc[r] + OPEN_F) | TBIT;
-        int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
+        const int32_t diag = hdiag + inc;
+        const int32_t eT = __viaddmax_s32(eu, EXT, hu + OPEN_E_S) | TBIT;
+        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, S.hc[r] + OPEN_F_S) | TBIT;
+        int32_t hn = (__vimax3_s32_relu(diag, eT, fTn) - SHIFT) & CLEAN;
         int32_t eo = eT, fo = fTn;
         if (MASKED) {
             const bool in = (r < alive) && ((uint32_t)(j - r - lo0) <= w2);
             hn = in ? hn : 0;
-            eo = in ? eT : NEG_E;
-            fo = in ? fTn : NEG_F;
+            eo = in ? eT : NEG_E_S;
+            fo = in ? fTn : NEG_F_S;
         }
         hdiag = S.hc[r];
         S.hc[r] = hn;
@@ -213,19 +216,112 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
         hu = hn;
         eu = eo;
     }
-    *slot = make_int2(hu, eu);
-    int32_t cm = S.hc[0];
+}
+
+// First-max trackers (one per row, in shared memory) are touched only when
+// some lane's column maximum over rows [RB, RE) beats the best score its
+// pair had when the strip began -- the only way one of its rows can record
+// a new first maximum.
+template <int R, int RB, int RE>
+__device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
+    using namespace key;
+    int32_t cm = S.hc[RB];
 #pragma unroll
-    for (int r = 1; r + 1 < R; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
-    if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
+    for (int r = RB + 1; r + 1 < RE; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
+    if (((RE - RB) & 1) == 0) cm = max(cm, S.hc[RE - 1]);
     if (__any_sync(__activemask(), cm > gthr)) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
+        for (int r = RB; r < RE; ++r) {
             const int32_t b = s_best[r * STRIP_THREADS];
             if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
         }
     }
 }
+
+// A full column: every row computed (masked or not), window read and written.
+template <int R, bool MASKED>
+__device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
+                                             const char *s_inc, int2 *win, int32_t wmask,
+                                             const uint8_t *B, int32_t lo0, uint32_t w2,
+                                             int32_t alive, int32_t gthr, int32_t *s_best) {
+    const int2 bnd = S.bnd_n;
+    const uint32_t bcol = S.bcol_n;
+    int2 *slot = win + (size_t)(j & wmask) * 32;
+    S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
+    S.bcol_n = (uint32_t)__ldg(B + jb_next - 1) * 128u;
+    int32_t hu = bnd.x, eu = bnd.y;
+    const int32_t hdiag = S.hd0;
+    S.hd0 = hu;
+    strip_cells<R, 0, R, MASKED>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive);
+    *slot = make_int2(hu, eu);
+    strip_track<R, 0, R>(S, gthr, s_best);
+}
+
+// Ramp-in column C of an unclipped strip: rows 0..C are inside the band,
+// rows below have not reached it (they keep H = 0, F = -inf).  The bottom
+// row is outside, and no later strip reads this column, so the window entry
+// is not written.
+template <int R, int C>
+__device__ __forceinline__ void ramp_in_column(int32_t j, StripRegs<R> &S, const char *s_inc,
+                                               int2 *win, int32_t wmask, const uint8_t *B,
+                                               int32_t gthr, int32_t *s_best) {
+    const int2 bnd = S.bnd_n;
+    const uint32_t bcol = S.bcol_n;
+    S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
+    S.bcol_n = (uint32_t)__ldg(B + j) * 128u;  // column j + 1 <= lb in an unclipped strip
+    int32_t hu = bnd.x, eu = bnd.y;
+    const int32_t hdiag = S.hd0;
+    S.hd0 = hu;
+    strip_cells<R, 0, C + 1, false>(j, bcol, hu, eu, hdiag, S, s_inc, 0, 0, R);
+    strip_track<R, 0, C + 1>(S, gthr, s_best);
+}
+
+// Ramp-out column C of an unclipped strip: rows 0..C have left the band
+// (row C's last cell was column j - 1), rows C+1.. are inside.  Row C+1
+// starts from the out-of-band boundary above it.
+template <int R, int C>
+__device__ __forceinline__ void ramp_out_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
+                                                const char *s_inc, int2 *win, int32_t wmask,
+                                                const uint8_t *B, int32_t gthr, int32_t *s_best) {
+    using namespace key;
+    const uint32_t bcol = S.bcol_n;
+    S.bcol_n = (uint32_t)__ldg(B + jb_next - 1) * 128u;
+    int32_t hu = 0, eu = NEG_E_S;
+    const int32_t hdiag = S.hc[C];
+    strip_cells<R, C + 1, R, false>(j, bcol, hu, eu, hdiag, S, s_inc, 0, 0, R);
+    win[(size_t)(j & wmask) * 32] = make_int2(hu, eu);
+    strip_track<R, C + 1, R>(S, gthr, s_best);
+}
+
+template <int R, int C>
+struct RampIn {
+    __device__ __forceinline__ static void run(int32_t j0, StripRegs<R> &S, const char *s_inc,
+                                               int2 *win, int32_t wmask, const uint8_t *B,
+                                               int32_t gthr, int32_t *s_best) {
+        RampIn<R, C - 1>::run(j0, S, s_inc, win, wmask, B, gthr, s_best);
+        ramp_in_column<R, C>(j0 + C, S, s_inc, win, wmask, B, gthr, s_best);
+    }
+};
+template <int R>
+struct RampIn<R, -1> {
+    __device__ __forceinline__ static void run(int32_t, StripRegs<R> &, const char *, int2 *, int32_t,
+                                               const uint8_t *, int32_t, int32_t *) {}
+};
+template <int R, int C>
+struct RampOut {
+    __device__ __forceinline__ static void run(int32_t j0, int32_t lb, StripRegs<R> &S,
+                                               const char *s_inc, int2 *win, int32_t wmask,
+                                               const uint8_t *B, int32_t gthr, int32_t *s_best) {
+        RampOut<R, C - 1>::run(j0, lb, S, s_inc, win, wmask, B, gthr, s_best);
+        const int32_t j = j0 + C;
+        ramp_out_column<R, C>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, gthr, s_best);
+    }
+};
+template <int R>
+struct RampOut<R, -1> {
+    __device__ __forceinline__ static void run(int32_t, int32_t, StripRegs<R> &, const char *, int2 *,
+                                               int32_t, const uint8_t *, int32_t, int32_t *) {}
+};
 
 template <int R>
 __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
@@ -239,7 +335,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
     const int32_t wmask = W - 1;
     const uint32_t w2 = 2u * (uint32_t)w;
 
-    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E);
+    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E_S);
 
     int32_t gbest = 0;
     StripRegs<R> S;
@@ -256,7 +352,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             S.hc[r] = 0;
-            S.fT[r] = NEG_F;
+            S.fT[r] = NEG_F_S;
             s_best[r * STRIP_THREADS] = gbest;
             const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : 0u;
             S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
@@ -270,7 +366,15 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         if (I0 < J0) I0 = J0;
         int32_t I1 = i0 + h + w;
         if (I1 > J1) I1 = J1;
-        if (alive == R && I0 <= I1) {
+        if (alive == R && lo0 >= 1 && hi_last <= lb && (int32_t)w2 >= R - 1) {
+            // unclipped strip: triangular ramps of R - 1 columns on each side
+            RampIn<R, R - 2>::run(J0, S, s_inc, win, wmask, B, gthr, s_best);
+#pragma unroll 2
+            for (int32_t j = I0; j <= I1; ++j)
+                strip_column<R, false>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
+                                       gthr, s_best);
+            RampOut<R, R - 2>::run(I1 + 1, lb, S, s_inc, win, wmask, B, gthr, s_best);
+        } else if (alive == R && I0 <= I1) {
             for (int32_t j = J0; j < I0; ++j)
                 strip_column<R, true>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best);
 #pragma unroll 2
@@ -294,7 +398,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         // the columns right of this strip's band read as out-of-band for the next strip
         const int32_t fill_end = J1 + R < lb ? J1 + R : lb;
         for (int32_t j = J1 + 1; j <= fill_end; ++j)
-            win[(size_t)(j & wmask) * 32] = make_int2(0, NEG_E);
+            win[(size_t)(j & wmask) * 32] = make_int2(0, NEG_E_S);
     }
     const int32_t score = gbest >> 16;
     if (score >= SCORE_LIMIT) {
