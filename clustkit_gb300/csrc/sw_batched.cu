@@ -257,72 +257,6 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
     strip_track<R, 0, R>(S, gthr, s_best);
 }
 
-// Ramp-in column C of an unclipped strip: rows 0..C are inside the band,
-// rows below have not reached it (they keep H = 0, F = -inf).  The bottom
-// row is outside, and no later strip reads this column, so the window entry
-// is not written.
-template <int R, int C>
-__device__ __forceinline__ void ramp_in_column(int32_t j, StripRegs<R> &S, const char *s_inc,
-                                               int2 *win, int32_t wmask, const uint8_t *B,
-                                               int32_t gthr, int32_t *s_best) {
-    const int2 bnd = S.bnd_n;
-    const uint32_t bcol = S.bcol_n;
-    S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
-    S.bcol_n = (uint32_t)__ldg(B + j) * 128u;  // column j + 1 <= lb in an unclipped strip
-    int32_t hu = bnd.x, eu = bnd.y;
-    const int32_t hdiag = S.hd0;
-    S.hd0 = hu;
-    strip_cells<R, 0, C + 1, false>(j, bcol, hu, eu, hdiag, S, s_inc, 0, 0, R);
-    strip_track<R, 0, C + 1>(S, gthr, s_best);
-}
-
-// Ramp-out column C of an unclipped strip: rows 0..C have left the band
-// (row C's last cell was column j - 1), rows C+1.. are inside.  Row C+1
-// starts from the out-of-band boundary above it.
-template <int R, int C>
-__device__ __forceinline__ void ramp_out_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
-                                                const char *s_inc, int2 *win, int32_t wmask,
-                                                const uint8_t *B, int32_t gthr, int32_t *s_best) {
-    using namespace key;
-    const uint32_t bcol = S.bcol_n;
-    S.bcol_n = (uint32_t)__ldg(B + jb_next - 1) * 128u;
-    int32_t hu = 0, eu = NEG_E_S;
-    const int32_t hdiag = S.hc[C];
-    strip_cells<R, C + 1, R, false>(j, bcol, hu, eu, hdiag, S, s_inc, 0, 0, R);
-    win[(size_t)(j & wmask) * 32] = make_int2(hu, eu);
-    strip_track<R, C + 1, R>(S, gthr, s_best);
-}
-
-template <int R, int C>
-struct RampIn {
-    __device__ __forceinline__ static void run(int32_t j0, StripRegs<R> &S, const char *s_inc,
-                                               int2 *win, int32_t wmask, const uint8_t *B,
-                                               int32_t gthr, int32_t *s_best) {
-        RampIn<R, C - 1>::run(j0, S, s_inc, win, wmask, B, gthr, s_best);
-        ramp_in_column<R, C>(j0 + C, S, s_inc, win, wmask, B, gthr, s_best);
-    }
-};
-template <int R>
-struct RampIn<R, -1> {
-    __device__ __forceinline__ static void run(int32_t, StripRegs<R> &, const char *, int2 *, int32_t,
-                                               const uint8_t *, int32_t, int32_t *) {}
-};
-template <int R, int C>
-struct RampOut {
-    __device__ __forceinline__ static void run(int32_t j0, int32_t lb, StripRegs<R> &S,
-                                               const char *s_inc, int2 *win, int32_t wmask,
-                                               const uint8_t *B, int32_t gthr, int32_t *s_best) {
-        RampOut<R, C - 1>::run(j0, lb, S, s_inc, win, wmask, B, gthr, s_best);
-        const int32_t j = j0 + C;
-        ramp_out_column<R, C>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, gthr, s_best);
-    }
-};
-template <int R>
-struct RampOut<R, -1> {
-    __device__ __forceinline__ static void run(int32_t, int32_t, StripRegs<R> &, const char *, int2 *,
-                                               int32_t, const uint8_t *, int32_t, int32_t *) {}
-};
-
 template <int R>
 __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
                                   int32_t *s_best, int2 *win, int32_t W, int32_t lane,
@@ -361,33 +295,25 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         S.bnd_n = win[(size_t)(J0 & wmask) * 32];
         S.bcol_n = (uint32_t)__ldg(B + J0 - 1) * 128u;
 
-        // interior columns: every row of the strip is alive and inside its band
+        // Interior columns (every row alive and inside its band) run unmasked,
+        // two at a time; ramp and clipped columns run the masked step.  One
+        // loop keeps a single copy of each body in the instruction cache.
         int32_t I0 = lo0 + R - 1;
         if (I0 < J0) I0 = J0;
         int32_t I1 = i0 + h + w;
         if (I1 > J1) I1 = J1;
-        if (alive == R && lo0 >= 1 && hi_last <= lb && (int32_t)w2 >= R - 1) {
-            // unclipped strip: triangular ramps of R - 1 columns on each side
-            RampIn<R, R - 2>::run(J0, S, s_inc, win, wmask, B, gthr, s_best);
-#pragma unroll 2
-            for (int32_t j = I0; j <= I1; ++j)
-                strip_column<R, false>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
-                                       gthr, s_best);
-            RampOut<R, R - 2>::run(I1 + 1, lb, S, s_inc, win, wmask, B, gthr, s_best);
-        } else if (alive == R && I0 <= I1) {
-            for (int32_t j = J0; j < I0; ++j)
-                strip_column<R, true>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best);
-#pragma unroll 2
-            for (int32_t j = I0; j <= I1; ++j)
-                strip_column<R, false>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
-                                       gthr, s_best);
-            for (int32_t j = I1 + 1; j <= J1; ++j)
+        if (alive < R) { I0 = J1 + 1; I1 = J1; }
+        for (int32_t j = J0; j <= J1;) {
+            if (j >= I0 && j < I1) {
+                strip_column<R, false>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best);
+                strip_column<R, false>(j + 1, j + 1 < lb ? j + 2 : lb, S, s_inc, win, wmask, B, lo0, w2,
+                                       alive, gthr, s_best);
+                j += 2;
+            } else {
                 strip_column<R, true>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
                                       gthr, s_best);
-        } else {
-            for (int32_t j = J0; j <= J1; ++j)
-                strip_column<R, true>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
-                                      gthr, s_best);
+                j += 1;
+            }
         }
         // rows merge in row order: strict '>' keeps the earliest row on ties
 #pragma unroll
