@@ -68,6 +68,15 @@ constexpr int32_t MATCH_MASK = (1 << 13) - 1;
 }  // namespace key
 
 constexpr int STRIP_THREADS = 256;
+
+// a * one + b with `one` a runtime 1: issued as an integer multiply-add on
+// the FMA pipe, which the recurrence leaves mostly idle, instead of an add on
+// the ALU pipe, which the DPX max operations and logic ops already saturate.
+__device__ __forceinline__ int32_t fadd(int32_t a, int32_t b, int32_t one) {
+    int32_t d;
+    asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(one), "r"(b));
+    return d;
+}
 constexpr int INC_ENTRIES = N_CODES * N_CODES;           // 441
 constexpr size_t INC_SMEM = (size_t)INC_ENTRIES * 32 * 4;  // replicated per lane
 
@@ -194,15 +203,15 @@ struct StripRegs {
 template <int R, int RB, int RE, bool MASKED>
 __device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &hu, int32_t &eu,
                                             int32_t hdiag, StripRegs<R> &S, const char *s_inc,
-                                            int32_t lo0, uint32_t w2, int32_t alive) {
+                                            int32_t lo0, uint32_t w2, int32_t alive, int32_t one) {
     using namespace key;
 #pragma unroll
     for (int r = RB; r < RE; ++r) {
-        const int32_t inc = *(const int32_t *)(s_inc + S.arow[r] + bcol);
-        const int32_t diag = hdiag + inc;
-        const int32_t eT = __viaddmax_s32(eu, EXT, hu + OPEN_E_S) | TBIT;
-        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, S.hc[r] + OPEN_F_S) | TBIT;
-        int32_t hn = (__vimax3_s32_relu(diag, eT, fTn) - SHIFT) & CLEAN;
+        const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
+        const int32_t diag = fadd(hdiag, inc, one);
+        const int32_t eT = __viaddmax_s32(eu, EXT, fadd(hu, OPEN_E_S, one)) | TBIT;
+        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F_S, one)) | TBIT;
+        int32_t hn = fadd(__vimax3_s32_relu(diag, eT, fTn), -SHIFT, one) & CLEAN;
         int32_t eo = eT, fo = fTn;
         if (MASKED) {
             const bool in = (r < alive) && ((uint32_t)(j - r - lo0) <= w2);
@@ -243,7 +252,8 @@ template <int R, bool MASKED>
 __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
                                              const char *s_inc, int2 *win, int32_t wmask,
                                              const uint8_t *B, int32_t lo0, uint32_t w2,
-                                             int32_t alive, int32_t gthr, int32_t *s_best) {
+                                             int32_t alive, int32_t gthr, int32_t *s_best,
+                                             int32_t one) {
     const int2 bnd = S.bnd_n;
     const uint32_t bcol = S.bcol_n;
     int2 *slot = win + (size_t)(j & wmask) * 32;
@@ -252,7 +262,7 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
     int32_t hu = bnd.x, eu = bnd.y;
     const int32_t hdiag = S.hd0;
     S.hd0 = hu;
-    strip_cells<R, 0, R, MASKED>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive);
+    strip_cells<R, 0, R, MASKED>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive, one);
     *slot = make_int2(hu, eu);
     strip_track<R, 0, R>(S, gthr, s_best);
 }
@@ -260,7 +270,8 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
 template <int R>
 __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
                                   int32_t *s_best, int2 *win, int32_t W, int32_t lane,
-                                  int32_t *fallback, int32_t *fallback_count, int32_t *err) {
+                                  int32_t *fallback, int32_t *fallback_count, int32_t *err,
+                                  int32_t one) {
     using namespace key;
     PairGeom g = pair_geometry(in, p, err);
     const int32_t la = g.la, lb = g.lb, w = g.w, h = g.h;
@@ -305,13 +316,13 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         if (alive < R) { I0 = J1 + 1; I1 = J1; }
         for (int32_t j = J0; j <= J1;) {
             if (j >= I0 && j < I1) {
-                strip_column<R, false>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best);
+                strip_column<R, false>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best, one);
                 strip_column<R, false>(j + 1, j + 1 < lb ? j + 2 : lb, S, s_inc, win, wmask, B, lo0, w2,
-                                       alive, gthr, s_best);
+                                       alive, gthr, s_best, one);
                 j += 2;
             } else {
                 strip_column<R, true>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
-                                      gthr, s_best);
+                                      gthr, s_best, one);
                 j += 1;
             }
         }
@@ -347,7 +358,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
                 int32_t *__restrict__ fallback, int32_t *__restrict__ fallback_count,
-                int32_t *err) {
+                int32_t *err, int32_t one) {
     extern __shared__ int32_t s_inc[];
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
     __syncthreads();
@@ -366,7 +377,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
         const int32_t q = grp * 32 + lane;
         if (q < n_elig)
             align_pair_strips<R>(in, out, (int64_t)order[q], (const char *)s_inc, s_best, win, W, lane,
-                                 fallback, fallback_count, err);
+                                 fallback, fallback_count, err, one);
     }
 }
 
@@ -414,7 +425,7 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
     kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
-                                              fallback, fb_count, err);
+                                              fallback, fb_count, err, 1);
     CK_CUDA(cudaGetLastError());
     if (ev1) CK_CUDA(cudaEventRecord(ev1, st));
     if (ctr) ctr->launches += 1;
