@@ -54,14 +54,6 @@ constexpr int32_t OPEN_F = GAP_OPEN * KU;
 constexpr int32_t EXT = GAP_EXTEND * KU;
 constexpr int32_t NEG_E = -16 * KU + 1 * PU + TBIT;
 constexpr int32_t NEG_F = -16 * KU + TBIT;
-// Candidates of H's maximum are compared shifted by -3*PU, so that the
-// "zero" candidate is exactly 0 and __vimax3_s32_relu supplies it; the
-// shift keeps the order of every pair of keys (all are shifted alike).
-constexpr int32_t SHIFT = -3 * PU;
-constexpr int32_t OPEN_E_S = OPEN_E + SHIFT;
-constexpr int32_t OPEN_F_S = OPEN_F + SHIFT;
-constexpr int32_t NEG_E_S = NEG_E + SHIFT;
-constexpr int32_t NEG_F_S = NEG_F + SHIFT;
 constexpr int32_t ROWS_MAX = (1 << 13) - 1;
 constexpr int32_t SCORE_LIMIT = 32767 - 24;
 constexpr int32_t MATCH_MASK = (1 << 13) - 1;
@@ -86,7 +78,7 @@ __global__ void build_inc_kernel(const int8_t *sub, int32_t *inc) {
     if (t >= INC_ENTRIES) return;
     int a = t / N_CODES, b = t % N_CODES;
     int s = (a < 20 && b < 20) ? (int)sub[a * 20 + b] : -4;
-    inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0) + key::SHIFT;
+    inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0);
 }
 
 // 1 when every residue code of the sequence is <= 20.
@@ -195,11 +187,11 @@ struct StripRegs {
 // Cells of rows [RB, RE) at column j, top to bottom.  (hu, eu) enter as
 // H and E of row RB - 1 at column j, hdiag as H of row RB - 1 at column
 // j - 1; they leave as the values of row RE - 1.  Stored keys: H clean
-// (score * 2^16 + matches), E and F shifted with the tie bit set.
-//     diag = Hdiag + inc                  (inc holds the shift)
-//     E    = max(E_up - 2^16, H_up + OPEN_E_S) | tie
-//     F    = max(F_left - 2^16, H_left + OPEN_F_S) | tie
-//     H    = (max(diag, E, F, 0) + 3 * 2^14) & CLEAN
+// (score * 2^16 + matches), E and F with the tie bit set.
+//     diag = max(Hdiag + inc, ZERO)
+//     E    = max(E_up - 2^16, H_up + OPEN_E) | tie
+//     F    = max(F_left - 2^16, H_left + OPEN_F) | tie
+//     H    = max(diag, E, F) & CLEAN
 template <int R, int RB, int RE, bool MASKED>
 __device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &hu, int32_t &eu,
                                             int32_t hdiag, StripRegs<R> &S, const char *s_inc,
@@ -208,16 +200,16 @@ __device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &h
 #pragma unroll
     for (int r = RB; r < RE; ++r) {
         const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
-        const int32_t diag = fadd(hdiag, inc, one);
-        const int32_t eT = __viaddmax_s32(eu, EXT, fadd(hu, OPEN_E_S, one)) | TBIT;
-        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F_S, one)) | TBIT;
-        int32_t hn = fadd(__vimax3_s32_relu(diag, eT, fTn), -SHIFT, one) & CLEAN;
+        const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
+        const int32_t eT = __viaddmax_s32(eu, EXT, fadd(hu, OPEN_E, one)) | TBIT;
+        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
+        int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
         int32_t eo = eT, fo = fTn;
         if (MASKED) {
             const bool in = (r < alive) && ((uint32_t)(j - r - lo0) <= w2);
             hn = in ? hn : 0;
-            eo = in ? eT : NEG_E_S;
-            fo = in ? fTn : NEG_F_S;
+            eo = in ? eT : NEG_E;
+            fo = in ? fTn : NEG_F;
         }
         hdiag = S.hc[r];
         S.hc[r] = hn;
@@ -228,23 +220,32 @@ __device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &h
 }
 
 // First-max trackers (one per row, in shared memory) are touched only when
-// some lane's column maximum over rows [RB, RE) beats the best score its
-// pair had when the strip began -- the only way one of its rows can record
-// a new first maximum.
-template <int R, int RB, int RE>
-__device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
+// some lane's maximum over a group of 4 rows of this column beats the best
+// score its pair had when the strip began -- the only way one of those rows
+// can record a new first maximum -- and then only for that group.
+template <int R, int G>
+__device__ __forceinline__ void strip_track_group(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
     using namespace key;
-    int32_t cm = S.hc[RB];
-#pragma unroll
-    for (int r = RB + 1; r + 1 < RE; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
-    if (((RE - RB) & 1) == 0) cm = max(cm, S.hc[RE - 1]);
+    constexpr int RB = 4 * G;
+    const int32_t cm = max(__vimax3_s32(S.hc[RB], S.hc[RB + 1], S.hc[RB + 2]), S.hc[RB + 3]);
     if (__any_sync(__activemask(), cm > gthr)) {
 #pragma unroll
-        for (int r = RB; r < RE; ++r) {
+        for (int r = RB; r < RB + 4; ++r) {
             const int32_t b = s_best[r * STRIP_THREADS];
             if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
         }
     }
+}
+
+template <int R>
+__device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
+    static_assert(R % 4 == 0, "rows per strip must be a multiple of 4");
+    strip_track_group<R, 0>(S, gthr, s_best);
+    strip_track_group<R, 1>(S, gthr, s_best);
+    if (R > 8) strip_track_group<R, (R > 8 ? 2 : 0)>(S, gthr, s_best);
+    if (R > 12) strip_track_group<R, (R > 12 ? 3 : 0)>(S, gthr, s_best);
+    if (R > 16) strip_track_group<R, (R > 16 ? 4 : 0)>(S, gthr, s_best);
+    if (R > 20) strip_track_group<R, (R > 20 ? 5 : 0)>(S, gthr, s_best);
 }
 
 // A full column: every row computed (masked or not), window read and written.
@@ -264,7 +265,7 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
     S.hd0 = hu;
     strip_cells<R, 0, R, MASKED>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive, one);
     *slot = make_int2(hu, eu);
-    strip_track<R, 0, R>(S, gthr, s_best);
+    strip_track<R>(S, gthr, s_best);
 }
 
 template <int R>
@@ -280,7 +281,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
     const int32_t wmask = W - 1;
     const uint32_t w2 = 2u * (uint32_t)w;
 
-    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E_S);
+    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E);
 
     int32_t gbest = 0;
     StripRegs<R> S;
@@ -297,7 +298,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             S.hc[r] = 0;
-            S.fT[r] = NEG_F_S;
+            S.fT[r] = NEG_F;
             s_best[r * STRIP_THREADS] = gbest;
             const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : 0u;
             S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
@@ -335,7 +336,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         // the columns right of this strip's band read as out-of-band for the next strip
         const int32_t fill_end = J1 + R < lb ? J1 + R : lb;
         for (int32_t j = J1 + 1; j <= fill_end; ++j)
-            win[(size_t)(j & wmask) * 32] = make_int2(0, NEG_E_S);
+            win[(size_t)(j & wmask) * 32] = make_int2(0, NEG_E);
     }
     const int32_t score = gbest >> 16;
     if (score >= SCORE_LIMIT) {
