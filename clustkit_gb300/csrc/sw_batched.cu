@@ -199,53 +199,48 @@ __device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &h
     using namespace key;
 #pragma unroll
     for (int r = RB; r < RE; ++r) {
-        const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
-        const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
-        const int32_t eT = __viaddmax_s32(eu, EXT, fadd(hu, OPEN_E, one)) | TBIT;
-        const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
-        int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
-        int32_t eo = eT, fo = fTn;
-        if (MASKED) {
-            const bool in = (r < alive) && ((uint32_t)(j - r - lo0) <= w2);
-            hn = in ? hn : 0;
-            eo = in ? eT : NEG_E;
-            fo = in ? fTn : NEG_F;
+        // Ramp and clipped columns skip rows outside their band: a row that
+        // has not reached its band keeps H = 0, F = -inf; a row that has left
+        // it hands the out-of-band boundary (H = 0, E = -inf) to the row
+        // below and its last H as that row's diagonal input.
+        if (!MASKED || ((r < alive) && ((uint32_t)(j - r - lo0) <= w2))) {
+            const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
+            const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
+            const int32_t eT = __viaddmax_s32(eu, EXT, fadd(hu, OPEN_E, one)) | TBIT;
+            const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
+            const int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
+            hdiag = S.hc[r];
+            S.hc[r] = hn;
+            S.fT[r] = fTn;
+            hu = hn;
+            eu = eT;
+        } else {
+            hdiag = S.hc[r];
+            S.hc[r] = 0;
+            hu = 0;
+            eu = NEG_E;
         }
-        hdiag = S.hc[r];
-        S.hc[r] = hn;
-        S.fT[r] = fo;
-        hu = hn;
-        eu = eo;
     }
 }
 
 // First-max trackers (one per row, in shared memory) are touched only when
-// some lane's maximum over a group of 4 rows of this column beats the best
-// score its pair had when the strip began -- the only way one of those rows
-// can record a new first maximum -- and then only for that group.
-template <int R, int G>
-__device__ __forceinline__ void strip_track_group(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
+// some lane's column maximum beats the best score its pair had when the
+// strip began -- the only way one of its rows can record a new first
+// maximum.
+template <int R>
+__device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
     using namespace key;
-    constexpr int RB = 4 * G;
-    const int32_t cm = max(__vimax3_s32(S.hc[RB], S.hc[RB + 1], S.hc[RB + 2]), S.hc[RB + 3]);
+    int32_t cm = S.hc[0];
+#pragma unroll
+    for (int r = 1; r + 1 < R; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
+    if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
     if (__any_sync(__activemask(), cm > gthr)) {
 #pragma unroll
-        for (int r = RB; r < RB + 4; ++r) {
+        for (int r = 0; r < R; ++r) {
             const int32_t b = s_best[r * STRIP_THREADS];
             if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
         }
     }
-}
-
-template <int R>
-__device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
-    static_assert(R % 4 == 0, "rows per strip must be a multiple of 4");
-    strip_track_group<R, 0>(S, gthr, s_best);
-    strip_track_group<R, 1>(S, gthr, s_best);
-    if (R > 8) strip_track_group<R, (R > 8 ? 2 : 0)>(S, gthr, s_best);
-    if (R > 12) strip_track_group<R, (R > 12 ? 3 : 0)>(S, gthr, s_best);
-    if (R > 16) strip_track_group<R, (R > 16 ? 4 : 0)>(S, gthr, s_best);
-    if (R > 20) strip_track_group<R, (R > 20 ? 5 : 0)>(S, gthr, s_best);
 }
 
 // A full column: every row computed (masked or not), window read and written.
