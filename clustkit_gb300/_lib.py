@@ -41,6 +41,8 @@ SIGNATURES = {
                            _P, _P, _P, _P, _P]),
     "ck_sw_batch_device": (_I32, [_P, _I64, _P, _I64, _P, _P, _I64, _I32, _P, ctypes.c_float, _P, _I32,
                                   _I32, _P, _P, _P, _P, _P, _P]),
+    "ck_sw_batch_device_noalloc": (_I32, [_P, _I64, _P, _I64, _P, _P, _I64, _I32, _P, ctypes.c_float,
+                                          _P, _I32, _P, _P, _P, _P, _P, _P]),
     "ck_sw_status_device": (_I32, [_P]),
     "ck_sw_last_counters": (_I32, [_P]),
     "ck_sketch": (_I32, [_P, _I64, _P, _P, _I64, _I32, _I32, _I32, ctypes.c_uint64, _P]),

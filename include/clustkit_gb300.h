@@ -104,6 +104,33 @@ int32_t ck_sw_batch_device(const int32_t *d_pairs, int64_t M, const uint8_t *d_f
                            const int32_t *d_diag_hints, int32_t pass_rule, int32_t engine,
                            float *d_sims, int32_t *d_scores, int32_t *d_matches,
                            int32_t *d_shorter, uint8_t *d_mask, void *stream);
+/* Allocation-free form of ck_sw_batch_device.  No counterpart in clustkit:
+ * it is for callers that cannot let a library allocate GPU memory -- a host
+ * system that owns the device's memory through its own pre-sized pool, or a
+ * latency-bound serving loop where an allocation could stall or fail
+ * mid-request.  It calls no cudaMalloc/cudaFree and no allocating library
+ * routine: the caller passes device buffers for inputs and outputs, and the
+ * kernel's workspace is a 32 MiB static device array inside this library,
+ * held on every GPU that loads it until the process exits.
+ *   - Runs the plain kernel (one thread per pair); results equal
+ *     ck_sw_batch_device's.
+ *   - band_width must be 1..8191 (the workspace per thread grows with the
+ *     band); larger, or <= 0 (full matrix), returns CK_ERR_UNSUPPORTED.
+ *   - Blocking: enqueues on `stream`, waits for it, and returns
+ *     CK_ERR_OUT_OF_RANGE if a pair index or sequence extent was bad.
+ *   - The first call on a device looks up the static arrays' device
+ *     addresses; make that first call before any stream capture.
+ *   - Every call shares the static arrays (which keep the last call's
+ *     contents); calls that overlap on the GPU, e.g. from two streams or
+ *     threads, race on them. */
+int32_t ck_sw_batch_device_noalloc(const int32_t *d_pairs, int64_t M, const uint8_t *d_flat,
+                                   int64_t flat_len, const int64_t *d_offsets,
+                                   const int32_t *d_lengths, int64_t n_seqs, int32_t band_width,
+                                   const int8_t *sub_matrix_host, float threshold,
+                                   const int32_t *d_diag_hints, int32_t pass_rule, float *d_sims,
+                                   int32_t *d_scores, int32_t *d_matches, int32_t *d_shorter,
+                                   uint8_t *d_mask, void *stream);
+
 /* Synchronises `stream`, returns CK_OK or CK_ERR_OUT_OF_RANGE for the GPU
  * checks of the ck_*_device calls since the previous ck_sw_status_device on
  * this device, and clears the flag. */
