@@ -262,6 +262,8 @@ def run_ours(args, world, rank, local):
     _lib.require_gpu()
     if args.rows:
         _lib.set_config(_lib.CFG_ROWS_PER_STRIP, args.rows)
+    if args.variant >= 0:
+        _lib.set_config(_lib.CFG_STRIP_VARIANT, args.variant)
     s, pairs, n_cand = build_workload(use_gpu=True, quick=args.quick)
     pairs = shard(pairs, world, rank)
     M = len(pairs)
@@ -321,12 +323,15 @@ def run_ours(args, world, rank, local):
     res_b = {k: v.cpu().numpy() for k, v in out.items()}
     sweep = {}
     if args.sweep:
-        keep_rows = _lib.get_config(_lib.CFG_ROWS_PER_STRIP)
+        keep = (_lib.get_config(_lib.CFG_ROWS_PER_STRIP), _lib.get_config(_lib.CFG_STRIP_VARIANT))
         for rows in (8, 16, 24):
-            _lib.set_config(_lib.CFG_ROWS_PER_STRIP, rows)
-            t_r, _ = timed(ENGINE_BATCHED, 3, 1)
-            sweep[rows] = cells / (t_r / 3) / 1e9
-        _lib.set_config(_lib.CFG_ROWS_PER_STRIP, keep_rows)
+            for var in range(4):
+                _lib.set_config(_lib.CFG_ROWS_PER_STRIP, rows)
+                _lib.set_config(_lib.CFG_STRIP_VARIANT, var)
+                t_r, _ = timed(ENGINE_BATCHED, 3, 1)
+                sweep[f"R{rows}_V{var}"] = round(cells / (t_r / 3) / 1e9, 1)
+        _lib.set_config(_lib.CFG_ROWS_PER_STRIP, keep[0])
+        _lib.set_config(_lib.CFG_STRIP_VARIANT, keep[1])
     # ---- plain engine (the plain GPU form), same pairs
     plain_steps = max(1, min(args.steps, 3))
     lib.ck_sw_profile(1)
@@ -417,7 +422,8 @@ def run_ours(args, world, rank, local):
                      "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL)},
         "cpu_baseline": cpu,
         "rows_per_strip": _lib.get_config(_lib.CFG_ROWS_PER_STRIP),
-        "sweep_gcups_by_rows": sweep or None,
+        "strip_variant": _lib.get_config(_lib.CFG_STRIP_VARIANT),
+        "sweep_gcups": sweep or None,
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -437,7 +443,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="10x smaller workload (smoke-testing the bench)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24); 0 = library default")
-    ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip setting")
+    ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default")
+    ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -24,6 +24,7 @@ CK_ERR_NO_DEVICE = 6
 PASS_CPU, PASS_NUMBA, PASS_CUPY, PASS_SCORE = 0, 1, 2, 3
 ENGINE_BATCHED, ENGINE_PLAIN = 0, 1
 CFG_ROWS_PER_STRIP = 0
+CFG_STRIP_VARIANT = 1
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32

@@ -360,6 +360,7 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     std::lock_guard<std::mutex> lock(g_mutex);
     t_status = CK_OK;
     if (key == CK_CFG_ROWS_PER_STRIP) return sw_set_rows_per_strip(value);
+    if (key == CK_CFG_STRIP_VARIANT) return sw_set_variant(value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -368,6 +369,7 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     std::lock_guard<std::mutex> lock(g_mutex);
     if (!value) return CK_ERR_INVALID_ARGUMENT;
     if (key == CK_CFG_ROWS_PER_STRIP) { *value = sw_rows_per_strip(); return CK_OK; }
+    if (key == CK_CFG_STRIP_VARIANT) { *value = sw_variant(); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

@@ -160,6 +160,8 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
                           int32_t *d_err, cudaStream_t st, SwCounters *ctr, bool read_counters);
 int32_t sw_set_rows_per_strip(int32_t r);
 int32_t sw_rows_per_strip();
+int32_t sw_set_variant(int32_t v);
+int32_t sw_variant();
 int32_t sw_run_device(const SwIn &in, const SwOut &out, int64_t M, int32_t engine,
                       const int8_t *sub_host, cudaStream_t st, SwCounters *ctr,
                       bool read_counters);

@@ -182,6 +182,16 @@ struct StripRegs {
     int32_t hd0;       // H(i0 - 1, j - 1): diagonal input of the strip's first row
     int2 bnd_n;        // window entry (row i0 - 1) prefetched for the next column
     uint32_t bcol_n;   // residue offset of the next column's b, prefetched
+    int2 bnd_n2;       // the same, two columns ahead (prefetch distance 2)
+    uint32_t bcol_n2;
+};
+
+// Structural variants of the strip kernel (picked by the autotuner):
+// bit 0 -- prefetch the window entry and residue 2 columns ahead instead of 1;
+// bit 1 -- run interior columns 4 at a time instead of 2.
+template <int V> struct StripVariant {
+    static constexpr int PREFETCH = (V & 1) ? 2 : 1;
+    static constexpr int UNROLL = (V & 2) ? 4 : 2;
 };
 
 // Cells of rows [RB, RE) at column j, top to bottom.  (hu, eu) enter as
@@ -243,9 +253,10 @@ __device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr,
     }
 }
 
-// A full column: every row computed (masked or not), window read and written.
-template <int R, bool MASKED>
-__device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRegs<R> &S,
+// A full column: every row computed (or skipped when outside its band),
+// window read and written, next columns' inputs prefetched.
+template <int R, bool MASKED, int PF>
+__device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R> &S,
                                              const char *s_inc, int2 *win, int32_t wmask,
                                              const uint8_t *B, int32_t lo0, uint32_t w2,
                                              int32_t alive, int32_t gthr, int32_t *s_best,
@@ -253,8 +264,16 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
     const int2 bnd = S.bnd_n;
     const uint32_t bcol = S.bcol_n;
     int2 *slot = win + (size_t)(j & wmask) * 32;
-    S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
-    S.bcol_n = (uint32_t)__ldg(B + jb_next - 1) * 128u;
+    const int32_t jn = j + PF < lb ? j + PF : lb;  // column whose residue is prefetched
+    if (PF == 2) {
+        S.bnd_n = S.bnd_n2;
+        S.bcol_n = S.bcol_n2;
+        S.bnd_n2 = win[(size_t)((j + 2) & wmask) * 32];
+        S.bcol_n2 = (uint32_t)__ldg(B + jn - 1) * 128u;
+    } else {
+        S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
+        S.bcol_n = (uint32_t)__ldg(B + jn - 1) * 128u;
+    }
     int32_t hu = bnd.x, eu = bnd.y;
     const int32_t hdiag = S.hd0;
     S.hd0 = hu;
@@ -263,7 +282,7 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t jb_next, StripRe
     strip_track<R>(S, gthr, s_best);
 }
 
-template <int R>
+template <int R, int V>
 __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
                                   int32_t *s_best, int2 *win, int32_t W, int32_t lane,
                                   int32_t *fallback, int32_t *fallback_count, int32_t *err,
@@ -301,6 +320,10 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         S.hd0 = (J0 >= 2) ? win[(size_t)((J0 - 1) & wmask) * 32].x : 0;
         S.bnd_n = win[(size_t)(J0 & wmask) * 32];
         S.bcol_n = (uint32_t)__ldg(B + J0 - 1) * 128u;
+        if (StripVariant<V>::PREFETCH == 2) {
+            S.bnd_n2 = win[(size_t)((J0 + 1) & wmask) * 32];
+            S.bcol_n2 = (uint32_t)__ldg(B + (J0 + 1 < lb ? J0 + 1 : lb) - 1) * 128u;
+        }
 
         // Interior columns (every row alive and inside its band) run unmasked,
         // two at a time; ramp and clipped columns run the masked step.  One
@@ -310,15 +333,17 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         int32_t I1 = i0 + h + w;
         if (I1 > J1) I1 = J1;
         if (alive < R) { I0 = J1 + 1; I1 = J1; }
+        constexpr int U = StripVariant<V>::UNROLL, PF = StripVariant<V>::PREFETCH;
         for (int32_t j = J0; j <= J1;) {
-            if (j >= I0 && j < I1) {
-                strip_column<R, false>(j, j + 1, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best, one);
-                strip_column<R, false>(j + 1, j + 1 < lb ? j + 2 : lb, S, s_inc, win, wmask, B, lo0, w2,
-                                       alive, gthr, s_best, one);
-                j += 2;
+            if (j >= I0 && j + U - 1 <= I1) {
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    strip_column<R, false, PF>(j + u, lb, S, s_inc, win, wmask, B, lo0, w2, alive, gthr,
+                                               s_best, one);
+                j += U;
             } else {
-                strip_column<R, true>(j, j < lb ? j + 1 : lb, S, s_inc, win, wmask, B, lo0, w2, alive,
-                                      gthr, s_best, one);
+                strip_column<R, true, PF>(j, lb, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best,
+                                          one);
                 j += 1;
             }
         }
@@ -348,7 +373,7 @@ __host__ __device__ constexpr size_t strip_smem() {
     return INC_SMEM + (size_t)R * STRIP_THREADS * sizeof(int32_t);
 }
 
-template <int R>
+template <int R, int V>
 __global__ void __launch_bounds__(STRIP_THREADS, 2)
 sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
@@ -372,7 +397,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
         if (grp >= n_groups) break;
         const int32_t q = grp * 32 + lane;
         if (q < n_elig)
-            align_pair_strips<R>(in, out, (int64_t)order[q], (const char *)s_inc, s_best, win, W, lane,
+            align_pair_strips<R, V>(in, out, (int64_t)order[q], (const char *)s_inc, s_best, win, W, lane,
                                  fallback, fallback_count, err, one);
     }
 }
@@ -386,6 +411,23 @@ static int32_t pow2_at_least(int64_t x) {
 
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
 static int32_t g_rows_per_strip = 16;
+static int32_t g_variant = 0;
+
+int32_t sw_set_variant(int32_t v) {
+    if (v < 0 || v > 3) {
+        set_error(CK_ERR_UNSUPPORTED, "strip kernel variant must be 0..3");
+        return CK_ERR_UNSUPPORTED;
+    }
+    g_variant = v;
+    return CK_OK;
+}
+int32_t sw_variant() { return g_variant; }
+
+template <int R>
+static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
+                               const int32_t *counters, const int32_t *inc, int32_t wmax,
+                               int32_t *ticket, int32_t *fallback, int32_t *fb_count,
+                               int32_t *err, cudaStream_t st, SwCounters *ctr);
 
 int32_t sw_set_rows_per_strip(int32_t r) {
     if (r != 8 && r != 16 && r != 24) {
@@ -397,13 +439,13 @@ int32_t sw_set_rows_per_strip(int32_t r) {
 }
 int32_t sw_rows_per_strip() { return g_rows_per_strip; }
 
-template <int R>
+template <int R, int V>
 static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *order,
                              const int32_t *counters, const int32_t *inc, int32_t wmax,
                              int32_t *ticket, int32_t *fallback, int32_t *fb_count,
                              int32_t *err, cudaStream_t st, SwCounters *ctr) {
     int32_t status = CK_OK;
-    auto kern = sw_strip_kernel<R>;
+    auto kern = sw_strip_kernel<R, V>;
     const size_t smem = strip_smem<R>();
     CK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -426,6 +468,19 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     if (ev1) CK_CUDA(cudaEventRecord(ev1, st));
     if (ctr) ctr->launches += 1;
     return CK_OK;
+}
+
+template <int R>
+static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
+                               const int32_t *counters, const int32_t *inc, int32_t wmax,
+                               int32_t *ticket, int32_t *fallback, int32_t *fb_count,
+                               int32_t *err, cudaStream_t st, SwCounters *ctr) {
+    switch (g_variant) {
+        case 1: return launch_strips<R, 1>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 2: return launch_strips<R, 2>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 3: return launch_strips<R, 3>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        default: return launch_strips<R, 0>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+    }
 }
 
 int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int8_t *d_sub,
@@ -480,13 +535,13 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
         const uint32_t *order = dv.Current();
         switch (g_rows_per_strip) {
             case 8:
-                CK_TRY(launch_strips<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;
             case 24:
-                CK_TRY(launch_strips<24>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<24>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;
             default:
-                CK_TRY(launch_strips<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;
         }
         if (ctr) ctr->launches += 1;

@@ -153,8 +153,12 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 
 /* Tunables of the batched engine, process-wide (the autotuner in
  * clustkit_gb300/tune.py picks them per workload):
- *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24 */
+ *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24
+ *   CK_CFG_STRIP_VARIANT   0..3: bit 0 prefetches the next columns' inputs two
+ *                          columns ahead (else one), bit 1 runs interior
+ *                          columns four at a time (else two) */
 #define CK_CFG_ROWS_PER_STRIP 0
+#define CK_CFG_STRIP_VARIANT 1
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

@@ -69,13 +69,15 @@ def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist):
     assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
 
 
-@pytest.mark.parametrize("rows", [8, 16, 24])
+@pytest.mark.parametrize("rows,variant", [(8, 0), (16, 0), (24, 0), (16, 1), (16, 2), (16, 3), (8, 3),
+                                          (24, 3)])
 @pytest.mark.parametrize("bw", [3, 32, 100, 0])
-def test_rows_per_strip_settings(ck, golden, rows, bw):
-    from clustkit_gb300._lib import CFG_ROWS_PER_STRIP, get_config, set_config
-    keep = get_config(CFG_ROWS_PER_STRIP)
+def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
+    from clustkit_gb300._lib import CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, get_config, set_config
+    keep = (get_config(CFG_ROWS_PER_STRIP), get_config(CFG_STRIP_VARIANT))
     try:
         set_config(CFG_ROWS_PER_STRIP, rows)
+        set_config(CFG_STRIP_VARIANT, variant)
         g = golden("sw_golden.npz")
         r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
         assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
@@ -85,7 +87,8 @@ def test_rows_per_strip_settings(ck, golden, rows, bw):
         _same(batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62),
               oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
     finally:
-        set_config(CFG_ROWS_PER_STRIP, keep)
+        set_config(CFG_ROWS_PER_STRIP, keep[0])
+        set_config(CFG_STRIP_VARIANT, keep[1])
 
 
 def test_engines_agree_and_counters(ck):
