@@ -411,7 +411,7 @@ static int32_t pow2_at_least(int64_t x) {
 
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
 static int32_t g_rows_per_strip = 16;
-static int32_t g_variant = 0;
+static int32_t g_variant = 1;
 
 int32_t sw_set_variant(int32_t v) {
     if (v < 0 || v > 3) {
