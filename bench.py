@@ -430,11 +430,100 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if rank == 0 and (args.search == "on" or (args.search == "auto" and not args.quick)):
+        try:
+            line["search"] = run_search(args)
+        except Exception as e:  # the SW line stands; the failure is reported in it
+            line["search"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- search / serving
+def make_queries(s, n, seed=11):
+    """Half mutated database members (30-90% identity), half background;
+    lengths lognormal, median 300, clipped 50..2000."""
+    from clustkit_gb300 import synth
+    rng = np.random.default_rng(seed)
+    L = np.clip(np.rint(np.exp(np.log(300) + 0.5 * rng.standard_normal(n))), 50, 2000).astype(int)
+    bg = synth.random_sequences(n, median=300, lo=50, hi=2000, seed=seed + 1)
+    qs = []
+    for i in range(n):
+        if i % 2 == 0:
+            m = s.seq(int(rng.integers(s.n))).copy()
+            ln = min(int(L[i]), len(m))
+            st = int(rng.integers(0, len(m) - ln + 1))
+            q = m[st:st + ln]
+            mut = rng.random(ln) < rng.uniform(0.1, 0.7)
+            q[mut] = rng.integers(0, 20, int(mut.sum()))
+            qs.append(q.astype(np.uint8))
+        else:
+            qs.append(bg.seq(i).copy())
+    return qs
+
+
+def run_search(args, n_db_fam=50000):
+    """Resident 500k-sequence database; continuous-batching server under
+    Poisson arrivals swept over rates, against a one-query-at-a-time loop."""
+    import torch
+    from clustkit_gb300 import synth
+    from clustkit_gb300.search import DeviceDatabase, SearchServer, _Slot, search_batch
+    t0 = time.time()
+    s = synth.generate_families(n_db_fam, 10, median=350, lo=30, hi=2000, seed=7)
+    t1 = time.time()
+    db = DeviceDatabase(s.flat, s.offsets, s.lengths, arena_slots=4, arena_queries=64,
+                        arena_residues=64 * 2000)
+    t2 = time.time()
+    log(f"search db: {s.n} seqs gen {t1 - t0:.1f}s, index+sketch {t2 - t1:.1f}s, "
+        f"{db.n_entries} index entries, band {db.band_width}, freq cap {db.freq_thresh}")
+    qs = make_queries(s, 6000)
+    # one query at a time
+    slot = _Slot(db, 0, 500)
+    for q in qs[:20]:
+        search_batch(db, [q], top_k=10, slot=slot)
+    lat = []
+    tp0 = time.perf_counter()
+    n_plain = 300
+    for q in qs[:n_plain]:
+        a = time.perf_counter()
+        search_batch(db, [q], top_k=10, slot=slot)
+        lat.append(time.perf_counter() - a)
+    plain_qps = n_plain / (time.perf_counter() - tp0)
+    slot.close()
+    plain = {"qps": plain_qps, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+             "p99_ms": float(np.percentile(lat, 99) * 1e3), "queries": n_plain}
+    server = SearchServer(db, top_k=10, max_cands=500).start()
+    sweep = []
+    rng = np.random.default_rng(3)
+    qi = 0
+    try:
+        for rate in (100, 1000, 3000, 10000, 20000):
+            n = int(min(2000, max(200, rate * 2)))
+            arr = np.cumsum(rng.exponential(1.0 / rate, n))
+            server.latencies.clear()
+            futs = []
+            t_start = time.perf_counter()
+            for i in range(n):
+                target = t_start + arr[i]
+                while time.perf_counter() < target:
+                    pass
+                futs.append(server.submit(qs[qi % len(qs)], t_arrival=target))
+                qi += 1
+            for f in futs:
+                f.result(timeout=300)
+            t_end = time.perf_counter()
+            p = server.latency_percentiles()
+            sweep.append({"offered_qps": rate, "achieved_qps": n / (t_end - t_start), "queries": n,
+                          "p50_ms": p["p50_ms"], "p99_ms": p["p99_ms"]})
+            log(f"search rate {rate}/s: {sweep[-1]}")
+    finally:
+        server.stop()
+    return {"db_sequences": int(s.n), "db_residues": int(s.flat.size), "index_entries": db.n_entries,
+            "band_width": db.band_width, "max_cands": 500, "top_k": 10, "slots": len(server.slots),
+            "plain_loop": plain, "continuous_batching": sweep}
 
 
 def main():
@@ -448,10 +537,20 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24); 0 = library default")
     ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default")
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
+    ap.add_argument("--search", choices=["auto", "on", "off", "only"], default="auto",
+                    help="search/serving leg (auto: on for the full workload, off with --quick)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.search == "only":
+        import torch
+        from clustkit_gb300 import _lib
+        torch.cuda.set_device(local)
+        _lib.load()
+        _lib.require_gpu()
+        print(json.dumps({"metric": "search queries/s and p50/p99 latency (500k-sequence resident DB)",
+                          "search": run_search(args, 5000 if args.quick else 50000)}), flush=True)
     else:
         run_ours(args, world, rank, local)
 

@@ -45,6 +45,15 @@ SIGNATURES = {
     "ck_sw_batch_device_noalloc": (_I32, [_P, _I64, _P, _I64, _P, _P, _I64, _I32, _P, ctypes.c_float,
                                           _P, _I32, _P, _P, _P, _P, _P, _P]),
     "ck_sw_status_device": (_I32, [_P]),
+    "ck_ctx_create": (_I32, [_P]),
+    "ck_ctx_destroy": (_I32, [_I32]),
+    "ck_ctx_status": (_I32, [_I32, _P]),
+    "ck_sw_batch_device_ctx": (_I32, [_I32, _P, _I64, _P, _I64, _P, _P, _I64, _I32, _P, ctypes.c_float, _P,
+                                      _I32, _I32, _P, _P, _P, _P, _P, _P]),
+    "ck_kmer_index_build_device": (_I32, [_I32, _P, _I64, _P, _P, _I64, _I32, _I32, _P, _P, _I64, _P, _P,
+                                          _P]),
+    "ck_search_phase_a_device": (_I32, [_I32, _P, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _I32, _I32,
+                                        _I32, _I32, _P, _P, _P, _P]),
     "ck_sw_last_counters": (_I32, [_P]),
     "ck_sketch": (_I32, [_P, _I64, _P, _P, _I64, _I32, _I32, _I32, ctypes.c_uint64, _P]),
     "ck_sketch_device": (_I32, [_P, _I64, _P, _P, _I64, _I32, _I32, _I32, ctypes.c_uint64, _P, _P]),

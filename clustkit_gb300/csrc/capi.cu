@@ -21,13 +21,21 @@ namespace {
 
 constexpr int MAX_DEVICES = 16;
 
+// One set of grow-only scratch buffers plus an error word.  Each device has
+// a default set; contexts (ck_ctx_create) own further sets so that work
+// enqueued on different streams never shares scratch.
+struct ScratchSet {
+    int device = -1;
+    void *buf[SLOT_COUNT] = {};
+    size_t cap[SLOT_COUNT] = {};
+    int32_t *err = nullptr;
+};
+
 struct DeviceState {
     bool init = false;
     int sms = 0;
     cudaStream_t stream = nullptr;
-    void *buf[SLOT_COUNT] = {};
-    size_t cap[SLOT_COUNT] = {};
-    int32_t *err = nullptr;
+    ScratchSet def;
     int8_t *sub = nullptr;
     int8_t sub_host[400] = {};
     bool sub_valid = false;
@@ -35,9 +43,11 @@ struct DeviceState {
 
 std::mutex g_mutex;
 DeviceState g_dev[MAX_DEVICES];
+std::vector<ScratchSet *> g_ctx;  // handle h -> g_ctx[h - 1]
 thread_local std::string t_error;
 thread_local int32_t t_status = CK_OK;
 thread_local SwCounters t_counters = {};
+thread_local ScratchSet *t_set = nullptr;  // context of the entry point running on this thread
 
 DeviceState *state(int32_t *status) {
     int d = 0;
@@ -59,9 +69,10 @@ DeviceState *state(int32_t *status) {
         s.sms = prop.multiProcessorCount;
         e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) { *status = cuda_status(e, "cudaStreamCreate"); return nullptr; }
-        e = cudaMalloc(&s.err, 64);
+        s.def.device = d;
+        e = cudaMalloc(&s.def.err, 64);
         if (e != cudaSuccess) { *status = cuda_status(e, "cudaMalloc(error word)"); return nullptr; }
-        e = cudaMemset(s.err, 0, 64);
+        e = cudaMemset(s.def.err, 0, 64);
         if (e != cudaSuccess) { *status = cuda_status(e, "cudaMemset(error word)"); return nullptr; }
         e = cudaMalloc(&s.sub, 512);
         if (e != cudaSuccess) { *status = cuda_status(e, "cudaMalloc(sub)"); return nullptr; }
@@ -97,8 +108,15 @@ int sm_count() {
     return s ? s->sms : 1;
 }
 
+static ScratchSet *current_set(int32_t *status) {
+    DeviceState *d = state(status);
+    if (!d) return nullptr;
+    if (t_set && t_set->device == current_device()) return t_set;
+    return &d->def;
+}
+
 void *scratch(int slot, size_t bytes, int32_t *status) {
-    DeviceState *s = state(status);
+    ScratchSet *s = current_set(status);
     if (!s) return nullptr;
     if (bytes == 0) bytes = 1;
     if (s->cap[slot] < bytes) {
@@ -122,8 +140,26 @@ void *scratch(int slot, size_t bytes, int32_t *status) {
 }
 
 int32_t *device_error_word(int32_t *status) {
-    DeviceState *s = state(status);
+    ScratchSet *s = current_set(status);
     return s ? s->err : nullptr;
+}
+
+// Runs `fn` with the scratch set of context `handle` (0 = the device default).
+template <class F>
+static int32_t with_context(int32_t handle, F fn) {
+    if (handle < 0 || handle > (int32_t)g_ctx.size() || (handle > 0 && !g_ctx[handle - 1])) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "unknown context handle");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    ScratchSet *set = handle > 0 ? g_ctx[handle - 1] : nullptr;
+    if (set && set->device != current_device()) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "context belongs to another device");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    t_set = set;
+    const int32_t st = fn();
+    t_set = nullptr;
+    return st;
 }
 
 const int8_t *device_sub_matrix(const int8_t *host, int32_t *status) {
@@ -141,6 +177,12 @@ const int8_t *device_sub_matrix(const int8_t *host, int32_t *status) {
         return nullptr;
     }
     return s->sub;
+}
+
+std::mutex &library_mutex() { return g_mutex; }
+void reset_thread_status() { t_status = CK_OK; }
+int32_t run_in_context(int32_t handle, int32_t (*fn)(void *), void *arg) {
+    return with_context(handle, [&] { return fn(arg); });
 }
 
 static cudaStream_t lib_stream(int32_t *status) {
@@ -337,6 +379,73 @@ int32_t ck_sw_batch_device(const int32_t *d_pairs, int64_t M, const uint8_t *d_f
     SwOut out{d_sims, d_scores, d_matches, d_shorter, d_mask};
     return sw_run_device(in, out, M, engine, sub_matrix_host, (cudaStream_t)stream, &t_counters,
                          false);
+}
+
+int32_t ck_ctx_create(int32_t *out_handle) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    if (!out_handle) return CK_ERR_INVALID_ARGUMENT;
+    int32_t status = CK_OK;
+    if (!state(&status)) return status;
+    ScratchSet *set = new ScratchSet();
+    set->device = current_device();
+    cudaError_t e = cudaMalloc(&set->err, 64);
+    if (e != cudaSuccess) { delete set; return cuda_status(e, "cudaMalloc(context error word)"); }
+    e = cudaMemset(set->err, 0, 64);
+    if (e != cudaSuccess) { cudaFree(set->err); delete set; return cuda_status(e, "cudaMemset"); }
+    for (size_t i = 0; i < g_ctx.size(); ++i)
+        if (!g_ctx[i]) { g_ctx[i] = set; *out_handle = (int32_t)i + 1; return CK_OK; }
+    g_ctx.push_back(set);
+    *out_handle = (int32_t)g_ctx.size();
+    return CK_OK;
+}
+
+int32_t ck_ctx_destroy(int32_t handle) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    if (handle < 1 || handle > (int32_t)g_ctx.size() || !g_ctx[handle - 1]) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "unknown context handle");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    ScratchSet *set = g_ctx[handle - 1];
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(set->device);
+    cudaDeviceSynchronize();
+    for (int i = 0; i < SLOT_COUNT; ++i)
+        if (set->buf[i]) cudaFree(set->buf[i]);
+    if (set->err) cudaFree(set->err);
+    cudaSetDevice(prev);
+    delete set;
+    g_ctx[handle - 1] = nullptr;
+    return CK_OK;
+}
+
+int32_t ck_ctx_status(int32_t handle, void *stream) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    return with_context(handle, [&] { return read_and_clear_error((cudaStream_t)stream); });
+}
+
+int32_t ck_sw_batch_device_ctx(int32_t ctx, const int32_t *d_pairs, int64_t M, const uint8_t *d_flat,
+                               int64_t flat_len, const int64_t *d_offsets, const int32_t *d_lengths,
+                               int64_t n_seqs, int32_t band_width, const int8_t *sub_matrix_host,
+                               float threshold, const int32_t *d_diag_hints, int32_t pass_rule,
+                               int32_t engine, float *d_sims, int32_t *d_scores, int32_t *d_matches,
+                               int32_t *d_shorter, uint8_t *d_mask, void *stream) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    t_counters = SwCounters{};
+    CK_TRY(check_sw_args(d_pairs, M, d_flat, flat_len, d_offsets, d_lengths, n_seqs, sub_matrix_host,
+                         pass_rule, engine));
+    if (M == 0) return CK_OK;
+    SwIn in{d_pairs, d_flat, d_offsets, d_lengths, d_diag_hints, n_seqs, flat_len, band_width,
+            threshold, pass_rule};
+    SwOut out{d_sims, d_scores, d_matches, d_shorter, d_mask};
+    return with_context(ctx, [&] {
+        return sw_run_device(in, out, M, engine, sub_matrix_host, (cudaStream_t)stream, &t_counters,
+                             false);
+    });
 }
 
 int32_t ck_sw_profile(int32_t enable) {

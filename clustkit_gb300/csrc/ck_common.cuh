@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 
 #include "clustkit_gb300.h"
@@ -176,6 +177,11 @@ int32_t jaccard_launch(const int32_t *pairs, int64_t M, const uint64_t *sk, int6
 // to record around the dominant kernel's launch on its own stream.
 bool profile_events(cudaEvent_t *start, cudaEvent_t *stop);
 
+// Lock and context plumbing for entry points defined outside capi.cu.
+std::mutex &library_mutex();
+int32_t run_in_context(int32_t handle, int32_t (*fn)(void *), void *arg);
+void reset_thread_status();
+
 // Per-device scratch: grow-only buffers owned by the library.
 void *scratch(int slot, size_t bytes, int32_t *status);
 int32_t *device_error_word(int32_t *status);
@@ -196,6 +202,12 @@ enum ScratchSlot {
     SLOT_INC,
     SLOT_SEQ_OK,
     SLOT_MAXLEN,
+    SLOT_SEARCH_COUNTS,
+    SLOT_SEARCH_TMP0,
+    SLOT_SEARCH_TMP1,
+    SLOT_SEARCH_TMP2,
+    SLOT_SEARCH_TMP3,
+    SLOT_SEARCH_TMP4,
     SLOT_HOST_IO0,
     SLOT_HOST_IO1,
     SLOT_HOST_IO2,

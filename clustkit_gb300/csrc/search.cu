@@ -1,0 +1,351 @@
+// search.cu -- k-mer inverted index and Phase-A k-mer scoring for search.
+//
+// Index (clustkit/kmer_index.py:77-166): CSR over all alpha^k k-mer values;
+// kmer_freqs[v] = occurrences of v, kmer_offsets = exclusive prefix sum,
+// kmer_entries = (sequence << 32 | position) grouped by k-mer and, inside a
+// k-mer, in (sequence, position) order.  k-mers holding a code >= alpha are
+// not indexed.  Built on the GPU: every position emits (k-mer, entry), a
+// stable radix sort by k-mer keeps the (sequence, position) order.
+//
+// Phase A (clustkit/kmer_index.py:470-534, :858-902): for each query k-mer
+// (valid, frequency <= freq_thresh) every posting adds one hit to its target;
+// counts saturate at 32767 as clustkit's int16 counters do; targets with
+// count >= min_total_hits survive; at most top_k survive per query, chosen by
+// count (ties: lower target id first), returned in target-id order.
+#include <cub/block/block_scan.cuh>
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "ck_common.cuh"
+
+namespace ck {
+
+// ----------------------------------------------------------------- index build
+__global__ void kmer_pos_count_kernel(const int32_t *lengths, int64_t n, int32_t k, int64_t *cnt) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t L = lengths[i];
+        cnt[i] = L >= k ? (int64_t)(L - k + 1) : 0;
+    }
+}
+
+__global__ void kmer_emit_kernel(const uint8_t *__restrict__ flat, int64_t flat_len,
+                                 const int64_t *__restrict__ offsets,
+                                 const int32_t *__restrict__ lengths, int64_t n, int32_t k,
+                                 int32_t alpha, const int64_t *__restrict__ pos_base,
+                                 uint32_t *__restrict__ keys, int64_t *__restrict__ vals,
+                                 int32_t *__restrict__ freqs, uint32_t sentinel, int32_t *err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n; q += warps) {
+        const int32_t L = lengths[q];
+        const int64_t o = offsets[q];
+        if (L < k) continue;
+        if (o < 0 || o + L > flat_len) {
+            if (lane == 0) atomicOr(err, ERRBIT_SEQ_EXTENT);
+            continue;
+        }
+        const int64_t base = pos_base[q];
+        for (int32_t p = lane; p <= L - k; p += 32) {
+            uint32_t v = 0;
+            bool ok = true;
+            for (int32_t m = 0; m < k; ++m) {
+                const uint32_t c = flat[o + p + m];
+                ok &= c < (uint32_t)alpha;
+                v = v * (uint32_t)alpha + c;
+            }
+            keys[base + p] = ok ? v : sentinel;
+            vals[base + p] = ((int64_t)q << 32) | (int64_t)p;
+            if (ok) atomicAdd(&freqs[v], 1);
+        }
+    }
+}
+
+__global__ void widen_kernel(const int32_t *in, int64_t n, int64_t *out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = i < n ? (int64_t)in[i] : 0;
+}
+
+static int grid_for(int64_t n, int threads, int cap_per_sm = 16) {
+    int64_t b = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)sm_count() * cap_per_sm;
+    if (b > cap) b = cap;
+    return (int)(b < 1 ? 1 : b);
+}
+
+struct IndexBuildArgs {
+    const uint8_t *flat; int64_t flat_len; const int64_t *offsets; const int32_t *lengths; int64_t n;
+    int32_t k, alpha; int64_t *kmer_offsets; int64_t *kmer_entries; int64_t capacity;
+    int32_t *kmer_freqs; int64_t *out_total; cudaStream_t st;
+};
+
+static int32_t index_build_impl(void *pv) {
+    IndexBuildArgs &a = *(IndexBuildArgs *)pv;
+    int32_t status = CK_OK;
+    int64_t nk = 1;
+    for (int32_t i = 0; i < a.k; ++i) nk *= a.alpha;
+    int32_t *err = device_error_word(&status);
+    if (!err) return status;
+    const size_t n1 = (size_t)(a.n > 0 ? a.n : 1);
+    int64_t *cnt = (int64_t *)scratch(SLOT_SEARCH_TMP0, (n1 + 1) * 8, &status);
+    if (!cnt) return status;
+    kmer_pos_count_kernel<<<grid_for(a.n, 256), 256, 0, a.st>>>(a.lengths, a.n, a.k, cnt);
+    CK_CUDA(cudaGetLastError());
+    CK_CUDA(cudaMemsetAsync(cnt + a.n, 0, 8, a.st));
+    size_t tb = 0;
+    CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, cnt, a.n + 1, a.st));
+    void *tmp = scratch(SLOT_SEARCH_TMP4, tb, &status);
+    if (!tmp) return status;
+    CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, cnt, a.n + 1, a.st));
+    int64_t P = 0;
+    CK_CUDA(cudaMemcpyAsync(&P, cnt + a.n, 8, cudaMemcpyDeviceToHost, a.st));
+    CK_CUDA(cudaStreamSynchronize(a.st));
+    if (P > a.capacity) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "kmer index: entries capacity below the number of k-mer positions");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    CK_CUDA(cudaMemsetAsync(a.kmer_freqs, 0, (size_t)nk * 4, a.st));
+    const size_t P1 = (size_t)(P > 0 ? P : 1);
+    uint32_t *k0 = (uint32_t *)scratch(SLOT_SEARCH_TMP1, P1 * 4, &status);
+    uint32_t *k1 = (uint32_t *)scratch(SLOT_SEARCH_TMP2, P1 * 4, &status);
+    int64_t *v0 = (int64_t *)scratch(SLOT_SEARCH_TMP3, P1 * 8, &status);
+    if (!k0 || !k1 || !v0) return status;
+    const uint32_t sentinel = (uint32_t)nk;
+    if (a.n > 0)
+        kmer_emit_kernel<<<grid_for(a.n * 32, 256), 256, 0, a.st>>>(
+            a.flat, a.flat_len, a.offsets, a.lengths, a.n, a.k, a.alpha, cnt, k0, v0, a.kmer_freqs,
+            sentinel, err);
+    CK_CUDA(cudaGetLastError());
+    int bits = 1;
+    while (((int64_t)1 << bits) <= (int64_t)sentinel) ++bits;
+    if (P > 0) {
+        // the caller's entries buffer is the sort's second value buffer
+        cub::DoubleBuffer<uint32_t> dk(k0, k1);
+        cub::DoubleBuffer<int64_t> dv(v0, a.kmer_entries);
+        size_t sb = 0;
+        CK_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sb, dk, dv, (int)P, 0, bits, a.st));
+        void *stmp = scratch(SLOT_SEARCH_TMP4, sb, &status);
+        if (!stmp) return status;
+        CK_CUDA(cub::DeviceRadixSort::SortPairs(stmp, sb, dk, dv, (int)P, 0, bits, a.st));
+        if (dv.Current() != a.kmer_entries)
+            CK_CUDA(cudaMemcpyAsync(a.kmer_entries, dv.Current(), (size_t)P * 8, cudaMemcpyDeviceToDevice, a.st));
+    }
+    widen_kernel<<<grid_for(nk + 1, 256), 256, 0, a.st>>>(a.kmer_freqs, nk, a.kmer_offsets);
+    CK_CUDA(cudaGetLastError());
+    size_t tb2 = 0;
+    CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb2, a.kmer_offsets, a.kmer_offsets, nk + 1, a.st));
+    void *tmp2 = scratch(SLOT_SEARCH_TMP4, tb2, &status);
+    if (!tmp2) return status;
+    CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp2, tb2, a.kmer_offsets, a.kmer_offsets, nk + 1, a.st));
+    int64_t total = 0;
+    CK_CUDA(cudaMemcpyAsync(&total, a.kmer_offsets + nk, 8, cudaMemcpyDeviceToHost, a.st));
+    int32_t h = 0;
+    CK_CUDA(cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, a.st));
+    CK_CUDA(cudaMemsetAsync(err, 0, 4, a.st));
+    CK_CUDA(cudaStreamSynchronize(a.st));
+    if (h) {
+        set_error(CK_ERR_OUT_OF_RANGE, "kmer index: sequence extent outside the flat buffer");
+        return CK_ERR_OUT_OF_RANGE;
+    }
+    *a.out_total = total;
+    return CK_OK;
+}
+
+// ----------------------------------------------------------------- phase A
+// Grid (blocks, nq): the warps of a query's blocks take its k-mer positions
+// in turn; a warp walks one posting list, lanes adding hits in parallel.
+__global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat,
+                                     const int64_t *__restrict__ qoff,
+                                     const int32_t *__restrict__ qlen, int32_t k, int32_t alpha,
+                                     const int64_t *__restrict__ kmer_offsets,
+                                     const int64_t *__restrict__ kmer_entries,
+                                     const int32_t *__restrict__ kmer_freqs, int32_t freq_thresh,
+                                     int32_t num_db, int32_t *__restrict__ counts, int32_t *err) {
+    const int32_t q = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int32_t L = qlen[q];
+    const uint8_t *s = qflat + qoff[q];
+    int32_t *c = counts + (int64_t)q * num_db;
+    const int32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p <= L - k; p += warps) {
+        uint32_t v = 0;
+        bool ok = true;
+        for (int32_t m = 0; m < k; ++m) {
+            const uint32_t r = s[p + m];
+            ok &= r < (uint32_t)alpha;
+            v = v * (uint32_t)alpha + r;
+        }
+        if (!ok || kmer_freqs[v] > freq_thresh) continue;
+        const int64_t b = kmer_offsets[v], e = kmer_offsets[v + 1];
+        for (int64_t h = b + lane; h < e; h += 32) {
+            const int32_t t = (int32_t)(kmer_entries[h] >> 32);
+            if (t >= 0 && t < num_db) atomicAdd(&c[t], 1);
+            else atomicOr(err, ERRBIT_PAIR_INDEX);
+        }
+    }
+}
+
+constexpr int SELECT_THREADS = 1024;
+
+// One block per query: the top_k surviving targets by (count desc, id asc),
+// written in id order.  Counts are clamped to 32767 first.
+__global__ void __launch_bounds__(SELECT_THREADS)
+phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits,
+                      int32_t top_k, int32_t *__restrict__ out_targets,
+                      int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
+    using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
+    __shared__ typename BlockScan::TempStorage scan_tmp;
+    __shared__ int32_t hist[256];
+    __shared__ int32_t sh_thr, sh_take_eq, sh_total, sh_run_eq, sh_run_sel;
+    const int32_t q = blockIdx.x;
+    const int32_t *c = counts + (int64_t)q * num_db;
+    const int tid = threadIdx.x;
+    auto val = [&](int32_t t) { const int32_t v = c[t]; return v > 32767 ? 32767 : v; };
+
+    for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (int32_t t = tid; t < num_db; t += blockDim.x) {
+        const int32_t v = val(t);
+        if (v >= min_hits) atomicAdd(&hist[v >> 7], 1);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int32_t total = 0;
+        for (int i = 0; i < 256; ++i) total += hist[i];
+        sh_total = total;
+        sh_thr = -1;  // -1: every survivor is taken
+        sh_take_eq = 0;
+        if (total > top_k) {
+            int32_t above = 0, b = 255;
+            for (; b >= 0; --b) {
+                if (above + hist[b] >= top_k) break;
+                above += hist[b];
+            }
+            sh_thr = b;        // coarse bin holding the threshold
+            sh_take_eq = above; // survivors in higher bins
+        }
+    }
+    __syncthreads();
+    if (sh_thr >= 0) {
+        const int32_t coarse = sh_thr, above_coarse = sh_take_eq;
+        for (int i = tid; i < 128; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        for (int32_t t = tid; t < num_db; t += blockDim.x) {
+            const int32_t v = val(t);
+            if (v >= min_hits && (v >> 7) == coarse) atomicAdd(&hist[v & 127], 1);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int32_t above = above_coarse, lo = 127;
+            for (; lo >= 0; --lo) {
+                if (above + hist[lo] >= top_k) break;
+                above += hist[lo];
+            }
+            sh_thr = (coarse << 7) | lo;     // exact threshold count
+            sh_take_eq = top_k - above;      // how many of the ties at the threshold
+        }
+        __syncthreads();
+    }
+    const int32_t thr = sh_thr, take_eq = sh_take_eq;
+    if (tid == 0) { sh_run_eq = 0; sh_run_sel = 0; }
+    __syncthreads();
+    for (int32_t base = 0; base < num_db; base += blockDim.x) {
+        const int32_t t = base + tid;
+        const int32_t v = t < num_db ? val(t) : -1;
+        const bool surv = t < num_db && v >= min_hits;
+        const int32_t is_eq = (surv && thr >= 0 && v == thr) ? 1 : 0;
+        int32_t eq_rank, eq_tot;
+        BlockScan(scan_tmp).ExclusiveSum(is_eq, eq_rank, eq_tot);
+        __syncthreads();
+        const bool sel = surv && (thr < 0 || v > thr || (is_eq && sh_run_eq + eq_rank < take_eq));
+        int32_t pos, sel_tot;
+        BlockScan(scan_tmp).ExclusiveSum(sel ? 1 : 0, pos, sel_tot);
+        if (sel) {
+            const int64_t o = (int64_t)q * top_k + sh_run_sel + pos;
+            out_targets[o] = t;
+            if (out_scores) out_scores[o] = v;
+        }
+        __syncthreads();
+        if (tid == 0) { sh_run_eq += eq_tot; sh_run_sel += sel_tot; }
+        __syncthreads();
+    }
+    if (tid == 0) out_n[q] = sh_total < top_k ? sh_total : top_k;
+}
+
+struct PhaseAArgs {
+    const uint8_t *qflat; const int64_t *qoff; const int32_t *qlen; int32_t nq; int32_t max_qlen;
+    int32_t k, alpha; const int64_t *kmer_offsets; const int64_t *kmer_entries;
+    const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
+    int32_t *out_targets; int32_t *out_scores; int32_t *out_n; cudaStream_t st;
+};
+
+static int32_t phase_a_impl(void *pv) {
+    PhaseAArgs &a = *(PhaseAArgs *)pv;
+    int32_t status = CK_OK;
+    int32_t *err = device_error_word(&status);
+    if (!err) return status;
+    if (a.nq == 0) return CK_OK;
+    const size_t nc = (size_t)a.nq * (size_t)a.num_db;
+    int32_t *counts = (int32_t *)scratch(SLOT_SEARCH_COUNTS, nc * 4 + 4, &status);
+    if (!counts) return status;
+    CK_CUDA(cudaMemsetAsync(counts, 0, nc * 4, a.st));
+    const int32_t npos = a.max_qlen - a.k + 1;
+    if (npos > 0) {
+        int bx = (npos + 7) / 8;  // 8 warps per block
+        if (bx > 16) bx = 16;
+        dim3 grid((unsigned)bx, (unsigned)a.nq);
+        phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qoff, a.qlen, a.k, a.alpha,
+                                                      a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
+                                                      a.freq_thresh, a.num_db, counts, err);
+        CK_CUDA(cudaGetLastError());
+    }
+    phase_a_select_kernel<<<a.nq, SELECT_THREADS, 0, a.st>>>(counts, a.num_db, a.min_hits, a.top_k,
+                                                             a.out_targets, a.out_scores, a.out_n);
+    CK_CUDA(cudaGetLastError());
+    return CK_OK;
+}
+
+}  // namespace ck
+
+using namespace ck;
+
+extern "C" int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat, int64_t flat_len,
+                                              const int64_t *d_offsets, const int32_t *d_lengths,
+                                              int64_t n_seqs, int32_t k, int32_t alpha,
+                                              int64_t *d_kmer_offsets, int64_t *d_kmer_entries,
+                                              int64_t entries_capacity, int32_t *d_kmer_freqs,
+                                              int64_t *out_total, void *stream) {
+    std::lock_guard<std::mutex> lock(library_mutex());
+    reset_thread_status();
+    int64_t nk = 1;
+    for (int32_t i = 0; i < k && nk < ((int64_t)1 << 31); ++i) nk *= (alpha > 0 ? alpha : 1);
+    if (k < 1 || alpha < 1 || nk >= ((int64_t)1 << 31) || n_seqs < 0 || flat_len < 0 || !out_total ||
+        !d_kmer_offsets || !d_kmer_freqs || (n_seqs > 0 && (!d_offsets || !d_lengths))) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "kmer index: bad arguments (need alpha^k < 2^31)");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    IndexBuildArgs a{d_flat, flat_len, d_offsets, d_lengths, n_seqs, k, alpha, d_kmer_offsets,
+                     d_kmer_entries, entries_capacity, d_kmer_freqs, out_total, (cudaStream_t)stream};
+    return run_in_context(ctx, index_build_impl, &a);
+}
+
+extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, const int64_t *d_qoffsets,
+                                            const int32_t *d_qlengths, int32_t nq, int32_t max_qlen,
+                                            int32_t k, int32_t alpha, const int64_t *d_kmer_offsets,
+                                            const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
+                                            int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
+                                            int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
+                                            int32_t *d_out_n, void *stream) {
+    std::lock_guard<std::mutex> lock(library_mutex());
+    reset_thread_status();
+    if (nq < 0 || top_k < 1 || k < 1 || alpha < 1 || num_db < 0 || !d_out_targets || !d_out_n ||
+        (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets || !d_kmer_freqs) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "phase A: bad arguments");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    PhaseAArgs a{d_qflat, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha, d_kmer_offsets, d_kmer_entries,
+                 d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k, d_out_targets, d_out_scores,
+                 d_out_n, (cudaStream_t)stream};
+    return run_in_context(ctx, phase_a_impl, &a);
+}

@@ -81,22 +81,18 @@ __global__ void build_inc_kernel(const int8_t *sub, int32_t *inc) {
     inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0);
 }
 
-// 1 when every residue code of the sequence is <= 20.
-__global__ void seq_codes_kernel(const uint8_t *flat, const int64_t *offsets,
-                                 const int32_t *lengths, int64_t n, int64_t flat_len,
-                                 uint8_t *ok) {
-    const int lane = threadIdx.x & 31;
-    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n;
-         q += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-        int64_t o = offsets[q];
-        int32_t L = lengths[q];
-        bool good = true;
-        if (o < 0 || L < 0 || o + L > flat_len) good = false;
-        else
-            for (int32_t t = lane; t < L; t += 32) good &= flat[o + t] <= 20;
-        good = __all_sync(0xffffffffu, good);
-        if (lane == 0) ok[q] = good;
-    }
+// Whether every residue code of sequence i is <= 20, memoised per call in
+// ok[i] (0 unknown, 1 yes, 2 no): only sequences that some pair references
+// are read, once or a few times (concurrent first readers agree).
+__device__ __forceinline__ bool seq_codes_ok(const SwIn &in, int32_t i, uint8_t *ok) {
+    const uint8_t m = ok[i];
+    if (m) return m == 1;
+    const uint8_t *s = in.flat + in.offsets[i];
+    const int32_t L = in.lengths[i];
+    bool good = true;
+    for (int32_t t = 0; t < L && good; ++t) good = __ldg(s + t) <= 20;
+    ok[i] = good ? 1 : 2;
+    return good;
 }
 
 // Closed-form count of the band cells of a pair (the cells clustkit's loop
@@ -133,7 +129,7 @@ __host__ __device__ inline int64_t band_cells_closed(int32_t la, int32_t lb, int
 }
 
 // ----------------------------------------------------------------- prep
-__global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, const uint8_t *__restrict__ seq_ok,
+__global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restrict__ seq_ok,
                                uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
                                int32_t *__restrict__ fallback, int32_t *__restrict__ counters,
                                unsigned long long *__restrict__ cells, int32_t *err) {
@@ -150,7 +146,8 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, const uint8_t *__r
             write_result(out, in, p, 0, 0, g.la, g.la, g.lb);
         } else {
             local_cells += band_cells_closed(g.la, g.lb, g.w, g.h);
-            if (g.la <= key::ROWS_MAX && seq_ok[g.a_idx] && seq_ok[g.b_idx]) {
+            if (g.la <= key::ROWS_MAX && seq_codes_ok(in, g.a_idx, seq_ok) &&
+                seq_codes_ok(in, g.b_idx, seq_ok)) {
                 int32_t cb = g.lb < key::ROWS_MAX ? g.lb : key::ROWS_MAX;
                 k = ((uint32_t)g.la << 13) | (uint32_t)cb;
                 elig++;
@@ -499,13 +496,7 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
 
     uint8_t *ok = (uint8_t *)scratch(SLOT_SEQ_OK, (size_t)(in.n_seqs > 0 ? in.n_seqs : 1), &status);
     if (!ok) return status;
-    if (in.n_seqs > 0) {
-        int64_t want = (in.n_seqs * 32 + 255) / 256;
-        int blocks = (int)(want < 8 * (int64_t)sm_count() ? want : 8 * (int64_t)sm_count());
-        seq_codes_kernel<<<blocks, 256, 0, st>>>(in.flat, in.offsets, in.lengths, in.n_seqs,
-                                                in.flat_len, ok);
-        CK_CUDA(cudaGetLastError());
-    }
+    CK_CUDA(cudaMemsetAsync(ok, 0, (size_t)(in.n_seqs > 0 ? in.n_seqs : 1), st));
     int32_t *inc = (int32_t *)scratch(SLOT_INC, INC_ENTRIES * sizeof(int32_t), &status);
     if (!inc) return status;
     build_inc_kernel<<<(INC_ENTRIES + 127) / 128, 128, 0, st>>>(d_sub, inc);

@@ -1,0 +1,417 @@
+"""Query-vs-database search on the GPU, batch and continuous-batching serving.
+
+Mirrors the k-mer search of clustkit (clustkit/kmer_index.py:1475-2349) in
+the configuration it takes with ``min_diag_hits <= 1`` and no similar-k-mer
+scoring: k-mer inverted index (k = 5, clustkit's CSR layout,
+kmer_index.py:117-166), Phase-A hit counting with the frequency cap
+(:451-534), at most ``max_cands`` candidates per query (:893-902), banded
+Smith-Waterman with a positive score as pass (:2271-2280, pairwise.py:636-681),
+rank ``0.267 * score - ln(qlen * tlen)`` (:2318-2323) and the top-k hits per
+query (clustkit/search.py:727-800).
+
+Differences, by design:
+* candidates above the cap are chosen by hit count with ties to the lower
+  target id (clustkit orders them with numpy's unstable quicksort);
+* the band width is fixed when the database is loaded
+  (``max(20, 0.3 * p95(database lengths))``) instead of being recomputed per
+  query batch, so a query's result does not depend on which other queries
+  share its batch.
+
+Everything heavy runs in libckgpu.so: the index is built on the GPU and stays
+resident with the sequences; a batch's queries are copied into a per-slot
+arena behind the database sequences so that query/target pairs address one
+sequence space.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .blosum import BLOSUM62
+from .pairwise import ENGINE_BATCHED, PASS_SCORE
+
+LAMBDA = np.float32(0.267)
+
+
+def compute_freq_threshold(kmer_freqs, num_sequences: int, percentile: float = 99.5) -> int:
+    """clustkit/kmer_index.py:451-463."""
+    nonzero = kmer_freqs[kmer_freqs > 0]
+    if len(nonzero) == 0:
+        return int(num_sequences)
+    pctl = int(np.percentile(nonzero, percentile))
+    return int(max(pctl, max(100, num_sequences // 200)))
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@dataclass
+class SearchHit:
+    query: int
+    target: int
+    identity: float
+    score: int
+    rank: float
+
+
+class DeviceDatabase:
+    """Sequences, k-mer index and sketches resident on one GPU.
+
+    ``arena_slots`` x ``arena_queries`` query entries and ``arena_slots`` x
+    ``arena_residues`` residues are reserved behind the database sequences
+    for query batches (one region per serving slot)."""
+
+    def __init__(self, flat, offsets, lengths, k: int = 5, freq_percentile: float = 95.0,
+                 band_width: int | None = None, arena_slots: int = 1, arena_queries: int = 64,
+                 arena_residues: int = 64 * 2000, sketch_size: int = 128, sketch_k: int = 5,
+                 device: str = "cuda:0"):
+        torch = _torch()
+        self.lib = _lib.load()
+        _lib.require_gpu()
+        self.dev = torch.device(device)
+        flat = np.ascontiguousarray(flat, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.int64)
+        lengths = np.ascontiguousarray(lengths, np.int32)
+        if flat.size and flat.max() > 20:
+            raise ValueError("database residue codes must be 0..20")
+        self.n = int(lengths.shape[0])
+        self.k = int(k)
+        self.alpha = 20
+        self.lengths_host = lengths
+        self.slots = int(arena_slots)
+        self.arena_queries = int(arena_queries)
+        self.arena_residues = int(arena_residues)
+        # merged sequence space: database, one empty sequence, then the arenas
+        self.empty_idx = self.n
+        self.arena_seq0 = self.n + 1
+        n_all = self.n + 1 + self.slots * self.arena_queries
+        self.flat_len = int(flat.size) + self.slots * self.arena_residues
+        self.arena_res0 = int(flat.size)
+        self.d_flat = torch.zeros(max(self.flat_len, 1), dtype=torch.uint8, device=self.dev)
+        self.d_flat[: flat.size].copy_(torch.from_numpy(flat))
+        off_all = np.zeros(n_all, np.int64)
+        len_all = np.zeros(n_all, np.int32)
+        off_all[: self.n] = offsets
+        len_all[: self.n] = lengths
+        self.d_offsets = torch.from_numpy(off_all).to(self.dev)
+        self.d_lengths = torch.from_numpy(len_all).to(self.dev)
+        self.n_all = n_all
+        # k-mer index
+        nk = self.alpha ** self.k
+        positions = int(np.maximum(lengths.astype(np.int64) - self.k + 1, 0).sum())
+        self.d_kmer_offsets = torch.empty(nk + 1, dtype=torch.int64, device=self.dev)
+        self.d_kmer_freqs = torch.empty(nk, dtype=torch.int32, device=self.dev)
+        self.d_kmer_entries = torch.empty(max(positions, 1), dtype=torch.int64, device=self.dev)
+        total = np.zeros(1, np.int64)
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
+        _lib.check(self.lib.ck_kmer_index_build_device(
+            0, self.d_flat.data_ptr(), self.flat_len, self.d_offsets.data_ptr(),
+            self.d_lengths.data_ptr(), self.n, self.k, self.alpha, self.d_kmer_offsets.data_ptr(),
+            self.d_kmer_entries.data_ptr(), positions, self.d_kmer_freqs.data_ptr(),
+            total.ctypes.data, stream))
+        self.n_entries = int(total[0])
+        freqs = self.d_kmer_freqs.cpu().numpy()
+        self.freq_thresh = compute_freq_threshold(freqs, self.n, freq_percentile)
+        if band_width is None:
+            band_width = max(20, int(int(np.percentile(lengths, 95)) * 0.3)) if self.n else 20
+        self.band_width = int(band_width)
+        # MinHash sketches of the database, resident beside the index
+        self.d_sketches = torch.empty((self.n, sketch_size), dtype=torch.int64, device=self.dev)
+        if self.n:
+            _lib.check(self.lib.ck_sketch_device(
+                self.d_flat.data_ptr(), self.flat_len, self.d_offsets.data_ptr(),
+                self.d_lengths.data_ptr(), self.n, sketch_k, sketch_size, 20, 42,
+                self.d_sketches.data_ptr(), stream))
+        torch.cuda.synchronize(self.dev)
+
+    def index_arrays(self):
+        """(kmer_offsets, kmer_entries, kmer_freqs) as numpy, clustkit's layout."""
+        return (self.d_kmer_offsets.cpu().numpy(),
+                self.d_kmer_entries[: self.n_entries].cpu().numpy(),
+                self.d_kmer_freqs.cpu().numpy())
+
+
+class _Slot:
+    """Buffers, stream and library context for one batch in flight."""
+
+    def __init__(self, db: DeviceDatabase, index: int, max_cands: int):
+        torch = _torch()
+        self.db = db
+        self.index = index
+        self.max_cands = max_cands
+        self.stream = torch.cuda.Stream(db.dev)
+        h = np.zeros(1, np.int32)
+        _lib.check(db.lib.ck_ctx_create(h.ctypes.data))
+        self.ctx = int(h[0])
+        Q, K = db.arena_queries, max_cands
+        self.seq0 = db.arena_seq0 + index * Q
+        self.res0 = db.arena_res0 + index * db.arena_residues
+        dev = db.dev
+        self.d_targets = torch.empty(Q * K, dtype=torch.int32, device=dev)
+        self.d_counts = torch.empty(Q * K, dtype=torch.int32, device=dev)
+        self.d_n = torch.empty(Q, dtype=torch.int32, device=dev)
+        self.d_pairs = torch.empty((Q * K, 2), dtype=torch.int32, device=dev)
+        self.d_sims = torch.empty(Q * K, dtype=torch.float32, device=dev)
+        self.d_scores = torch.empty(Q * K, dtype=torch.int32, device=dev)
+        self.d_mask = torch.empty(Q * K, dtype=torch.uint8, device=dev)
+        self.d_slotq = torch.arange(Q, dtype=torch.int32, device=dev).repeat_interleave(K)
+        self.d_col = torch.arange(K, dtype=torch.int32, device=dev).repeat(Q)
+        pin = lambda n, dt: torch.empty(n, dtype=dt).pin_memory()
+        self.h_res = pin(db.arena_residues, torch.uint8)
+        self.h_off = pin(Q, torch.int64)
+        self.h_len = pin(Q, torch.int32)
+        self.h_n = pin(Q, torch.int32)
+        self.h_targets = pin(Q * K, torch.int32)
+        self.h_sims = pin(Q * K, torch.float32)
+        self.h_scores = pin(Q * K, torch.int32)
+        self.h_mask = pin(Q * K, torch.uint8)
+        self.event = torch.cuda.Event()
+        self.batch = None
+
+    def close(self):
+        if self.ctx:
+            self.db.lib.ck_ctx_destroy(self.ctx)
+            self.ctx = 0
+
+    def launch(self, queries: list[np.ndarray], min_total_hits: int):
+        """Enqueue the whole pipeline for a batch on this slot's stream."""
+        torch = _torch()
+        db = self.db
+        nq = len(queries)
+        lens = np.array([len(q) for q in queries], np.int32)
+        offs = np.zeros(nq, np.int64)
+        if nq > 1:
+            offs[1:] = np.cumsum(lens[:-1])
+        tot = int(lens.sum())
+        if nq > db.arena_queries or tot > db.arena_residues:
+            raise ValueError("batch exceeds the slot arena")
+        hres = self.h_res.numpy()
+        if tot:
+            hres[:tot] = np.concatenate(queries)
+        self.h_off.numpy()[:nq] = offs + self.res0
+        self.h_len.numpy()[:nq] = lens
+        K = self.max_cands
+        M = nq * K
+        lib = db.lib
+        with torch.cuda.stream(self.stream):
+            st = self.stream.cuda_stream
+            db.d_flat[self.res0:self.res0 + tot].copy_(self.h_res[:tot], non_blocking=True)
+            db.d_offsets[self.seq0:self.seq0 + nq].copy_(self.h_off[:nq], non_blocking=True)
+            db.d_lengths[self.seq0:self.seq0 + nq].copy_(self.h_len[:nq], non_blocking=True)
+            qoff_ptr = db.d_offsets.data_ptr() + self.seq0 * 8
+            qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
+            _lib.check(lib.ck_search_phase_a_device(
+                self.ctx, db.d_flat.data_ptr(), qoff_ptr, qlen_ptr, nq, int(lens.max() if nq else 0),
+                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
+                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+            # dense pair list: (query, target) or (empty, empty) past a query's candidates
+            q = self.d_slotq[:M]
+            valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
+            self.d_pairs[:M, 0] = torch.where(valid, q + self.seq0,
+                                              torch.full_like(q, db.empty_idx))
+            self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M],
+                                              torch.full_like(q, db.empty_idx))
+            _lib.check(lib.ck_sw_batch_device_ctx(
+                self.ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
+                db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, db.band_width,
+                np.ascontiguousarray(BLOSUM62).ctypes.data, 0.0, None, PASS_SCORE, ENGINE_BATCHED,
+                self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(),
+                st))
+            self.h_n[:nq].copy_(self.d_n[:nq], non_blocking=True)
+            self.h_targets[:M].copy_(self.d_targets[:M], non_blocking=True)
+            self.h_sims[:M].copy_(self.d_sims[:M], non_blocking=True)
+            self.h_scores[:M].copy_(self.d_scores[:M], non_blocking=True)
+            self.h_mask[:M].copy_(self.d_mask[:M], non_blocking=True)
+            self.event.record(self.stream)
+        self.batch = (nq, lens)
+
+    def results(self, top_k: int) -> list[list[SearchHit]]:
+        """Hits of the batch (after the slot's event): top_k per query."""
+        db = self.db
+        _lib.check(db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream))
+        nq, lens = self.batch
+        K = self.max_cands
+        n = self.h_n.numpy()[:nq]
+        tg = self.h_targets.numpy()[: nq * K].reshape(nq, K)
+        sims = self.h_sims.numpy()[: nq * K].reshape(nq, K)
+        scores = self.h_scores.numpy()[: nq * K].reshape(nq, K)
+        mask = self.h_mask.numpy()[: nq * K].reshape(nq, K)
+        out = []
+        for qi in range(nq):
+            c = int(n[qi])
+            keep = mask[qi, :c].astype(bool)
+            t = tg[qi, :c][keep]
+            sc = scores[qi, :c][keep]
+            si = sims[qi, :c][keep]
+            rank = LAMBDA * sc.astype(np.float32) - np.log(
+                np.float32(lens[qi]) * db.lengths_host[t].astype(np.float32))
+            order = np.argsort(-rank, kind="stable")[:top_k]
+            out.append([SearchHit(qi, int(t[o]), float(si[o]), int(sc[o]), float(rank[o])) for o in order])
+        self.batch = None
+        return out
+
+
+def search_batch(db: DeviceDatabase, queries: list[np.ndarray], top_k: int = 10,
+                 max_cands: int = 500, min_total_hits: int = 2, slot: _Slot | None = None):
+    """Synchronous search of a list of encoded queries; list of hit lists."""
+    own = slot is None
+    if own:
+        slot = _Slot(db, 0, max_cands)
+    try:
+        res = []
+        for s in range(0, len(queries), db.arena_queries):
+            chunk = queries[s:s + db.arena_queries]
+            slot.launch(chunk, min_total_hits)
+            slot.event.synchronize()
+            for qi, hits in enumerate(slot.results(top_k)):
+                for h in hits:
+                    h.query = s + qi
+                res.append(hits)
+        return res
+    finally:
+        if own:
+            slot.close()
+
+
+@dataclass
+class _Request:
+    query: np.ndarray
+    future: Future
+    t_arrival: float
+
+
+class SearchServer:
+    """Continuous-batching search server on one GPU.
+
+    Requests (encoded protein queries) are queued on arrival.  A scheduler
+    thread admits queued requests into a batch whenever a slot -- a stream, a
+    library context and a pre-sized region of device memory -- is free, up to
+    the slot's query and residue capacity; batches in different slots overlap
+    on the device.  The number of slots is bounded by free device memory at
+    start-up.  Each request's future resolves to its list of SearchHit (query
+    index 0) when its batch completes; latency is recorded per request.
+    """
+
+    def __init__(self, db: DeviceDatabase, top_k: int = 10, max_cands: int = 500,
+                 min_total_hits: int = 2, max_batch: int | None = None):
+        torch = _torch()
+        self.db = db
+        self.top_k = top_k
+        self.max_cands = max_cands
+        self.min_total_hits = min_total_hits
+        self.max_batch = min(max_batch or db.arena_queries, db.arena_queries)
+        free, _ = torch.cuda.mem_get_info(db.dev)
+        # per slot: counts scratch + pair/SW buffers + the SW kernel's window scratch
+        per_slot = (db.arena_queries * db.n * 4 + db.arena_queries * max_cands * 64 + (256 << 20))
+        n_slots = int(max(1, min(db.slots, (free // 2) // max(per_slot, 1))))
+        self.slots = [_Slot(db, i, max_cands) for i in range(n_slots)]
+        self.free = list(self.slots)
+        self.busy: list[tuple[_Slot, list[_Request]]] = []
+        self.queue: collections.deque[_Request] = collections.deque()
+        self.cv = threading.Condition()
+        self.running = False
+        self.latencies: list[float] = []
+        self.thread = None
+        # warm every slot so its scratch is allocated before serving
+        warm = [np.arange(40, dtype=np.uint8) % 20]
+        for s in self.slots:
+            s.launch(warm, min_total_hits)
+            s.event.synchronize()
+            s.results(1)
+
+    def start(self):
+        self.running = True
+        self.thread = threading.Thread(target=self._loop, name="ck-search-scheduler", daemon=True)
+        self.thread.start()
+        return self
+
+    def stop(self):
+        with self.cv:
+            self.running = False
+            self.cv.notify_all()
+        if self.thread:
+            self.thread.join()
+        for s in self.slots:
+            s.close()
+
+    def submit(self, query, t_arrival: float | None = None) -> Future:
+        """Queue a query; ``t_arrival`` (perf_counter time) defaults to now and
+        is where its latency is measured from."""
+        q = np.ascontiguousarray(query, np.uint8)
+        if q.size and q.max() > 20:
+            raise ValueError("query residue codes must be 0..20")
+        if q.size > self.db.arena_residues:
+            raise ValueError("query longer than a slot arena")
+        fut: Future = Future()
+        with self.cv:
+            self.queue.append(_Request(q, fut, time.perf_counter() if t_arrival is None else t_arrival))
+            self.cv.notify()
+        return fut
+
+    def _finish(self, slot: _Slot, reqs: list[_Request]):
+        try:
+            res = slot.results(self.top_k)
+            now = time.perf_counter()
+            for r, hits in zip(reqs, res):
+                for h in hits:
+                    h.query = 0
+                self.latencies.append(now - r.t_arrival)
+                r.future.set_result(hits)
+        except Exception as e:  # surface device errors to every waiting request
+            for r in reqs:
+                r.future.set_exception(e)
+
+    def _loop(self):
+        while True:
+            with self.cv:
+                if not self.running and not self.queue and not self.busy:
+                    return
+            progressed = False
+            still = []
+            for slot, reqs in self.busy:
+                if slot.event.query():
+                    self._finish(slot, reqs)
+                    self.free.append(slot)
+                    progressed = True
+                else:
+                    still.append((slot, reqs))
+            self.busy = still
+            batch: list[_Request] = []
+            with self.cv:
+                if self.free and self.queue:
+                    res = 0
+                    while (self.queue and len(batch) < self.max_batch and
+                           res + self.queue[0].query.size <= self.db.arena_residues):
+                        r = self.queue.popleft()
+                        res += r.query.size
+                        batch.append(r)
+            if batch:
+                slot = self.free.pop()
+                try:
+                    slot.launch([r.query for r in batch], self.min_total_hits)
+                    self.busy.append((slot, batch))
+                except Exception as e:
+                    for r in batch:
+                        r.future.set_exception(e)
+                    self.free.append(slot)
+                progressed = True
+            if not progressed:
+                with self.cv:
+                    if not self.queue or not self.free:
+                        self.cv.wait(timeout=0.0002)
+
+    def latency_percentiles(self):
+        a = np.array(self.latencies)
+        if not a.size:
+            return {}
+        return {"p50_ms": float(np.percentile(a, 50) * 1e3), "p99_ms": float(np.percentile(a, 99) * 1e3),
+                "mean_ms": float(a.mean() * 1e3), "n": int(a.size)}

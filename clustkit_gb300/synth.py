@@ -81,15 +81,6 @@ def _draw(cdf: np.ndarray, u: np.ndarray) -> np.ndarray:
     return np.minimum(np.searchsorted(cdf, u, side="right"), cdf.shape[-1] - 1).astype(np.uint8)
 
 
-def _draw_conditional(cond_cdf: np.ndarray, a: np.ndarray, u: np.ndarray) -> np.ndarray:
-    out = np.empty(a.shape[0], dtype=np.uint8)
-    for code in range(cond_cdf.shape[0]):
-        sel = a == code
-        if sel.any():
-            out[sel] = _draw(cond_cdf[code], u[sel])
-    return out
-
-
 def _lengths(rng, n, median, lo, hi, dist, sigma, pareto_alpha):
     if dist == "pareto":
         x = lo * (1.0 + rng.pareto(pareto_alpha, size=n))
@@ -98,60 +89,83 @@ def _lengths(rng, n, median, lo, hi, dist, sigma, pareto_alpha):
     return np.clip(np.rint(x), lo, hi).astype(np.int64)
 
 
-def _indels(rng, seq: np.ndarray, rate: float, mean_len: float, bg_cdf: np.ndarray) -> np.ndarray:
-    L = seq.shape[0]
-    if L == 0 or rate <= 0:
-        return seq
-    ev = np.nonzero(rng.random(L) < rate)[0]
-    if ev.size == 0:
-        return seq
-    pieces = []
-    pos = 0
-    geo_p = 1.0 / mean_len
-    for e in ev:
-        if e < pos:
-            continue
-        ln = int(rng.geometric(geo_p))
-        pieces.append(seq[pos:e])
-        if rng.random() < 0.5:  # insertion before e
-            pieces.append(_draw(bg_cdf, rng.random(ln)))
-            pos = e
-        else:                   # deletion of seq[e:e+ln]
-            pos = min(L, e + ln)
-    pieces.append(seq[pos:])
-    return np.concatenate(pieces)
+def _gen_chunk(rng, n_fam, per_family, anc_len, div, bg_cdf, cond_cdf, indel_rate, indel_mean,
+               lo, hi):
+    """Descendants of ``n_fam`` families, vectorised over the whole chunk."""
+    # ancestors, then per_family copies of each
+    anc = _draw(bg_cdf, rng.random(int(anc_len.sum())))
+    anc_off = np.concatenate([[0], np.cumsum(anc_len)])
+    seq_anc = np.repeat(np.arange(n_fam), per_family)
+    L = anc_len[seq_anc]
+    starts = np.concatenate([[0], np.cumsum(L)[:-1]])
+    idx = np.repeat(anc_off[seq_anc] - starts, L) + np.arange(int(L.sum()))
+    res = anc[idx].copy()
+    seq_of = np.repeat(np.arange(seq_anc.size), L)
+    # substitutions: each residue mutates with its family's divergence
+    mut = rng.random(res.size) < div[seq_anc][seq_of]
+    if mut.any():
+        a = res[mut]
+        u = rng.random(a.size)
+        res[mut] = np.minimum((cond_cdf[a] < u[:, None]).sum(1), 19).astype(np.uint8)
+    # indels: events at rate indel_rate, geometric lengths; half delete the
+    # residues from the event on, half insert background residues before it
+    ev = np.nonzero(rng.random(res.size) < indel_rate)[0]
+    ln = rng.geometric(1.0 / indel_mean, size=ev.size)
+    is_del = rng.random(ev.size) < 0.5
+    keep = np.ones(res.size, bool)
+    if is_del.any():
+        d0 = ev[is_del]
+        d1 = np.minimum(d0 + ln[is_del], (starts + L)[seq_of[d0]])
+        diff = np.zeros(res.size + 1, np.int64)
+        np.add.at(diff, d0, 1)
+        np.add.at(diff, d1, -1)
+        keep = np.cumsum(diff[:-1]) == 0
+    ins_at = np.repeat(ev[~is_del], ln[~is_del])
+    ins_val = _draw(bg_cdf, rng.random(ins_at.size))
+    seq_keep = seq_of[keep]
+    out = np.insert(res[keep], np.searchsorted(np.nonzero(keep)[0], ins_at), ins_val)
+    out_seq = np.insert(seq_keep, np.searchsorted(np.nonzero(keep)[0], ins_at), seq_of[ins_at])
+    newL = np.bincount(out_seq, minlength=seq_anc.size)
+    # clip to [lo, hi]: truncate long ones, pad short ones with background
+    o_starts = np.concatenate([[0], np.cumsum(newL)[:-1]])
+    pos_in = np.arange(out.size) - np.repeat(o_starts, newL)
+    trunc = pos_in < hi
+    out = out[trunc]
+    newL = np.minimum(newL, hi)
+    seqs_short = np.nonzero(newL < lo)[0]
+    if seqs_short.size:
+        pieces = np.split(out, np.cumsum(newL)[:-1])
+        for i in seqs_short:
+            pieces[i] = np.concatenate([pieces[i], _draw(bg_cdf, rng.random(lo - newL[i]))])
+        newL = np.array([p.size for p in pieces])
+        out = np.concatenate(pieces)
+    return out.astype(np.uint8), newL.astype(np.int32)
 
 
 def generate_families(n_families: int, per_family: int = 10, median: int = 300,
                       lo: int = 50, hi: int = 800, seed: int = 0, *,
                       length_dist: str = "lognormal", sigma: float = 0.5,
                       pareto_alpha: float = 1.5, divergence=(0.10, 0.70),
-                      indel_rate: float = 0.05, indel_mean: float = 3.0) -> SequenceSet:
+                      indel_rate: float = 0.05, indel_mean: float = 3.0,
+                      chunk: int = 5000) -> SequenceSet:
     """``n_families`` ancestors, each replaced by ``per_family`` descendants."""
     rng = np.random.default_rng(seed)
     bg_cdf, cond_cdf = substitution_cdf()
     anc_len = _lengths(rng, n_families, median, lo, hi, length_dist, sigma, pareto_alpha)
-    seqs = []
-    fam = np.repeat(np.arange(n_families, dtype=np.int32), per_family)
-    for f in range(n_families):
-        anc = _draw(bg_cdf, rng.random(int(anc_len[f])))
-        d = rng.uniform(*divergence)
-        for _ in range(per_family):
-            child = anc.copy()
-            mut = rng.random(child.shape[0]) < d
-            if mut.any():
-                child[mut] = _draw_conditional(cond_cdf, child[mut], rng.random(int(mut.sum())))
-            child = _indels(rng, child, indel_rate, indel_mean, bg_cdf)
-            if child.shape[0] > hi:
-                child = child[:hi]
-            if child.shape[0] < lo:
-                child = np.concatenate([child, _draw(bg_cdf, rng.random(lo - child.shape[0]))])
-            seqs.append(child)
-    lengths = np.array([s.shape[0] for s in seqs], dtype=np.int32)
-    offsets = np.zeros(len(seqs), dtype=np.int64)
-    if len(seqs) > 1:
+    div = rng.uniform(*divergence, size=n_families)
+    flats, lens = [], []
+    for f0 in range(0, n_families, chunk):
+        f1 = min(n_families, f0 + chunk)
+        fl, ln = _gen_chunk(rng, f1 - f0, per_family, anc_len[f0:f1], div[f0:f1], bg_cdf, cond_cdf,
+                            indel_rate, indel_mean, lo, hi)
+        flats.append(fl)
+        lens.append(ln)
+    lengths = np.concatenate(lens) if lens else np.zeros(0, np.int32)
+    flat = np.concatenate(flats) if flats else np.zeros(0, np.uint8)
+    offsets = np.zeros(lengths.size, dtype=np.int64)
+    if lengths.size > 1:
         offsets[1:] = np.cumsum(lengths[:-1], dtype=np.int64)
-    flat = np.concatenate(seqs).astype(np.uint8) if seqs else np.empty(0, np.uint8)
+    fam = np.repeat(np.arange(n_families, dtype=np.int32), per_family)
     return SequenceSet(flat=flat, offsets=offsets, lengths=lengths, family=fam)
 
 

@@ -185,6 +185,56 @@ int32_t ck_jaccard_device(const int32_t *d_pairs, int64_t M, const uint64_t *d_s
                           int64_t N, int32_t s, float floor, float *d_sims,
                           uint8_t *d_mask, void *stream);
 
+/* ------------------------------------------------------------ contexts
+ * A context owns its own scratch buffers and error word, so that calls
+ * enqueued on different streams (e.g. overlapping search batches) never share
+ * scratch.  Handles are small positive integers; 0 names the device's default
+ * scratch used by the entry points without a context argument.  A context is
+ * bound to the device current at creation. */
+int32_t ck_ctx_create(int32_t *out_handle);
+int32_t ck_ctx_destroy(int32_t handle);
+/* Synchronises `stream` and returns CK_OK or CK_ERR_OUT_OF_RANGE for GPU-side
+ * input checks of the context's calls since its last status read. */
+int32_t ck_ctx_status(int32_t handle, void *stream);
+/* ck_sw_batch_device with the scratch of context `ctx`. */
+int32_t ck_sw_batch_device_ctx(int32_t ctx, const int32_t *d_pairs, int64_t M, const uint8_t *d_flat,
+                               int64_t flat_len, const int64_t *d_offsets,
+                               const int32_t *d_lengths, int64_t n_seqs, int32_t band_width,
+                               const int8_t *sub_matrix_host, float threshold,
+                               const int32_t *d_diag_hints, int32_t pass_rule, int32_t engine,
+                               float *d_sims, int32_t *d_scores, int32_t *d_matches,
+                               int32_t *d_shorter, uint8_t *d_mask, void *stream);
+
+/* ------------------------------------------------------ search: k-mer index
+ * CSR inverted index in clustkit's layout (clustkit/kmer_index.py:117-166),
+ * built on the GPU: kmer_offsets int64[alpha^k + 1], kmer_freqs
+ * int32[alpha^k], kmer_entries int64 (sequence << 32 | position), grouped by
+ * k-mer value and in (sequence, position) order within a k-mer.  k-mers with a
+ * code >= alpha are skipped.  entries_capacity must be at least
+ * sum(max(0, length - k + 1)) (the buffer also serves as sort space); the
+ * number of entries written is returned in *out_total.  Synchronous. */
+int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat, int64_t flat_len,
+                                   const int64_t *d_offsets, const int32_t *d_lengths,
+                                   int64_t n_seqs, int32_t k, int32_t alpha, int64_t *d_kmer_offsets,
+                                   int64_t *d_kmer_entries, int64_t entries_capacity,
+                                   int32_t *d_kmer_freqs, int64_t *out_total, void *stream);
+
+/* Phase-A k-mer scoring of a query batch (clustkit/kmer_index.py:470-534 with
+ * the per-query cap of :858-902): hits per database sequence from the query's
+ * valid k-mers with frequency <= freq_thresh, saturating at 32767; targets with
+ * at least min_total_hits hits survive; at most top_k per query, chosen by hit
+ * count with ties to the lower target id, are written in target-id order to
+ * d_out_targets[q * top_k ...] (hit counts to d_out_scores, may be NULL) and
+ * their number to d_out_n[q].  max_qlen bounds the query lengths.  Uses
+ * nq * num_db * 4 bytes of context scratch. */
+int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, const int64_t *d_qoffsets,
+                                 const int32_t *d_qlengths, int32_t nq, int32_t max_qlen, int32_t k,
+                                 int32_t alpha, const int64_t *d_kmer_offsets,
+                                 const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
+                                 int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
+                                 int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
+                                 int32_t *d_out_n, void *stream);
+
 /* ---------------------------------------------------- measurement probe
  * Sustained lane-operation rate of one integer instruction class on the
  * current device, used as the roofline denominator of the SW kernels.

@@ -1,0 +1,103 @@
+"""CPU restatement of clustkit's k-mer search path (numpy).
+
+TEST INFRASTRUCTURE ONLY -- the checker for clustkit_gb300.search, never the
+thing measured or shipped.  Reference paths are relative to the clustkit
+project root.
+
+* ``build_kmer_index``      -- clustkit/kmer_index.py:77-166
+* ``compute_freq_threshold`` -- clustkit/kmer_index.py:451-463
+* ``phase_a``               -- clustkit/kmer_index.py:470-534 (Phase A only,
+  the path taken when min_diag_hits <= 1, :832-850) with the per-query cap of
+  :893-902; ties at the cap go to the lower target id (clustkit's
+  ``np.argsort(-scores)`` leaves tie order to numpy's unstable quicksort)
+* ``rank_hits``             -- the E-value-style rank of
+  clustkit/kmer_index.py:2318-2323 and the top-k collection of
+  clustkit/search.py:727-800
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def kmer_values(seq: np.ndarray, k: int, alpha: int):
+    """(values, valid) for every k-mer start of one sequence."""
+    L = len(seq)
+    if L < k:
+        return np.empty(0, np.int64), np.empty(0, bool)
+    s = seq.astype(np.int64)
+    n = L - k + 1
+    v = np.zeros(n, np.int64)
+    ok = np.ones(n, bool)
+    for m in range(k):
+        c = s[m:m + n]
+        ok &= c < alpha
+        v = v * alpha + c
+    return v, ok
+
+
+def build_kmer_index(flat, offsets, lengths, k: int, alpha: int = 20):
+    """(kmer_offsets int64[alpha^k+1], kmer_entries int64[total], kmer_freqs int32[alpha^k])."""
+    nk = alpha ** k
+    keys, vals = [], []
+    for i in range(len(lengths)):
+        L = int(lengths[i])
+        o = int(offsets[i])
+        v, ok = kmer_values(flat[o:o + L], k, alpha)
+        pos = np.nonzero(ok)[0]
+        keys.append(v[ok])
+        vals.append((np.int64(i) << 32) | pos.astype(np.int64))
+    keys = np.concatenate(keys) if keys else np.empty(0, np.int64)
+    vals = np.concatenate(vals) if vals else np.empty(0, np.int64)
+    order = np.argsort(keys, kind="stable")  # (sequence, position) order kept inside a k-mer
+    freqs = np.bincount(keys, minlength=nk).astype(np.int32)
+    offs = np.zeros(nk + 1, np.int64)
+    np.cumsum(freqs, out=offs[1:])
+    return offs, vals[order], freqs
+
+
+def compute_freq_threshold(kmer_freqs, num_sequences: int, percentile: float = 99.5) -> int:
+    nonzero = kmer_freqs[kmer_freqs > 0]
+    if len(nonzero) == 0:
+        return int(num_sequences)
+    pctl = int(np.percentile(nonzero, percentile))
+    return int(max(pctl, max(100, num_sequences // 200)))
+
+
+def phase_a(query, k, alpha, kmer_offsets, kmer_entries, kmer_freqs, freq_thresh, num_db,
+            min_total_hits, top_k):
+    """Surviving target ids (ascending) and their hit counts, at most top_k."""
+    v, ok = kmer_values(np.asarray(query), k, alpha)
+    counts = np.zeros(num_db, np.int64)
+    for val in v[ok]:
+        if kmer_freqs[val] > freq_thresh:
+            continue
+        t = (kmer_entries[kmer_offsets[val]:kmer_offsets[val + 1]] >> 32).astype(np.int64)
+        np.add.at(counts, t, 1)
+    counts = np.minimum(counts, 32767)
+    ids = np.nonzero(counts >= min_total_hits)[0]
+    sc = counts[ids]
+    if len(ids) > top_k:
+        order = np.lexsort((ids, -sc))[:top_k]
+        keep = np.sort(ids[order])
+        return keep.astype(np.int32), counts[keep].astype(np.int32)
+    return ids.astype(np.int32), sc.astype(np.int32)
+
+
+def rank_hits(pairs, sims, scores, q_lengths, t_lengths, nq, top_k):
+    """Top-k hits per query: list of lists of (target, identity, rank score).
+
+    rank = float32(0.267) * score - log(qlen * tlen) in float32; ordering is
+    numpy's stable lexsort on (-rank, query), as clustkit does."""
+    hits = [[] for _ in range(nq)]
+    if len(pairs) == 0:
+        return hits
+    lam = np.float32(0.267)
+    ql = q_lengths[pairs[:, 0]].astype(np.float32)
+    tl = t_lengths[pairs[:, 1]].astype(np.float32)
+    rank = lam * scores.astype(np.float32) - np.log(ql * tl)
+    order = np.lexsort((-rank, pairs[:, 0]))
+    for idx in order:
+        q = int(pairs[idx, 0])
+        if len(hits[q]) < top_k:
+            hits[q].append((int(pairs[idx, 1]), float(sims[idx]), float(rank[idx])))
+    return hits

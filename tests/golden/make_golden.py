@@ -23,6 +23,10 @@ Outputs (all small, compressed):
   lsh_golden.npz        reference lsh_candidates on the sketches
   pipeline_golden.npz   config-1 sized run: sketches -> LSH -> the reference's
                         compute_pairwise_alignment(use_sw=True, use_c_sw=True)
+  search_golden.npz     a 240-sequence database and 20 queries: the reference's
+                        build_kmer_index (k = 5), compute_freq_threshold,
+                        _score_query_phase_a and search_kmer_index (Phase A,
+                        every survivor aligned with SW, E-value rank, top 5)
 """
 from __future__ import annotations
 
@@ -76,9 +80,15 @@ def install_numba_shim():
     sys.modules["numba"] = mod
 
 
+def logging_quiet():
+    import logging
+    logging.getLogger("clustkit").setLevel(logging.WARNING)
+
+
 def import_reference():
     install_numba_shim()
     sys.path.insert(0, str(REF_ROOT))
+    logging_quiet()
     import clustkit.lsh as rlsh
     import clustkit.pairwise as rpw
     import clustkit.sketch as rsk
@@ -236,7 +246,83 @@ def main():
                         lengths=c1.lengths, family=c1.family, sketches=c1_sk,
                         candidates=c1_pairs, num_tables=lp["num_tables"],
                         num_bands=lp["num_bands"], **results)
+    make_search_golden(rpw)
     print("done")
+
+
+def _dataset(flat, offsets, lengths, prefix):
+    from clustkit.io import SequenceDataset, SequenceRecord
+    from clustkit_gb300.blosum import PROTEIN_ALPHABET
+    letters = np.array(list(PROTEIN_ALPHABET + "X"))
+    recs = []
+    for i in range(len(lengths)):
+        o, L = int(offsets[i]), int(lengths[i])
+        recs.append(SequenceRecord(id=f"{prefix}{i}", description="",
+                                   sequence="".join(letters[flat[o:o + L]])))
+    return SequenceDataset(records=recs, mode="protein", lengths=lengths.astype(np.int32),
+                           ids=[r.id for r in recs], flat_sequences=flat, offsets=offsets)
+
+
+def make_search_golden(rpw):
+    """clustkit's k-mer search in the configuration the serving path mirrors:
+    k = 5 index, Phase A only (min_diag_hits = 1, no similar-k-mer scoring),
+    every survivor aligned (cap above the survivor count), SW + E-value rank."""
+    import clustkit.kmer_index as rki
+    from clustkit.database import DatabaseIndex
+    sys.path.insert(0, str(REPO))
+    from clustkit_gb300 import synth
+    db = synth.generate_families(40, 6, median=90, lo=30, hi=180, seed=404)
+    rng = np.random.default_rng(405)
+    qs = []
+    for i in rng.choice(db.n, 10, replace=False):  # mutated members
+        q = db.seq(int(i)).copy()
+        m = rng.random(len(q)) < rng.uniform(0.1, 0.5)
+        q[m] = rng.integers(0, 20, int(m.sum()))
+        qs.append(q.astype(np.uint8))
+    bg = synth.random_sequences(8, median=90, lo=30, hi=180, seed=406)
+    qs += [bg.seq(i).copy() for i in range(bg.n)]
+    qs.append(np.array([1, 2, 20, 3, 4, 5, 6, 7, 8, 9, 20, 20, 1, 2, 3], np.uint8))  # X codes
+    qs.append(np.array([5, 6, 7], np.uint8))                                        # shorter than k
+    qflat, qoff, qlen = pack(qs)
+    k = 5
+    t0 = time.time()
+    koff, kent, kfreq = rki.build_kmer_index(db.flat, db.offsets, db.lengths, k, "protein")
+    thr = int(rki.compute_freq_threshold(kfreq, db.n, 95.0))
+    phase = {}
+    for qi in range(len(qs)):
+        ids, sc = rki._score_query_phase_a(qs[qi], np.int32(len(qs[qi])), np.int32(k), np.int32(20),
+                                           koff, kent, kfreq, np.int32(thr), np.int32(db.n), np.int32(2))
+        phase[f"q{qi}_ids"] = np.asarray(ids, np.int32)
+        phase[f"q{qi}_counts"] = np.asarray(sc, np.int32)
+    print(f"search index + phase A {time.time()-t0:.1f}s")
+    db_ds = _dataset(db.flat, db.offsets, db.lengths, "d")
+    q_ds = _dataset(qflat, qoff, qlen, "q")
+    idx = DatabaseIndex(dataset=db_ds, sketches=None, lsh_bucket_ids=None, lsh_band_indices=None,
+                        lsh_seeds=None, params={"mode": "protein", "kmer_size": k},
+                        kmer_offsets=koff, kmer_entries=kent, kmer_freqs=kfreq)
+    t0 = time.time()
+    res = rki.search_kmer_index(idx, q_ds, threshold=0.0, top_k=5, band_width=None,
+                                min_total_hits=2, min_diag_hits=1, max_cands_per_query=100000,
+                                freq_percentile=95.0, kmer_score_thresh=0, local_alignment=True,
+                                evalue_normalize=True)
+    print(f"search_kmer_index {time.time()-t0:.1f}s, {sum(len(h) for h in res.hits)} hits")
+    hq, ht, hid, hsc = [], [], [], []
+    for qi, hl in enumerate(res.hits):
+        for h in hl:
+            hq.append(qi)
+            ht.append(int(h.target_id[1:]))
+            hid.append(h.identity)
+            hsc.append(h.score)
+    nz = np.nonzero(kfreq)[0]
+    all_len = np.concatenate([qlen, db.lengths])
+    np.savez_compressed(HERE / "search_golden.npz", db_flat=db.flat, db_offsets=db.offsets,
+                        db_lengths=db.lengths, q_flat=qflat, q_offsets=qoff, q_lengths=qlen,
+                        k=np.int32(k), kmer_entries=kent, freq_nonzero_idx=nz.astype(np.int64),
+                        freq_nonzero_val=kfreq[nz], offsets_total=np.int64(koff[-1]), freq_thresh=np.int32(thr),
+                        band_width=np.int32(max(20, int(int(np.percentile(all_len, 95)) * 0.3))),
+                        hit_query=np.array(hq, np.int32), hit_target=np.array(ht, np.int32),
+                        hit_identity=np.array(hid, np.float64), hit_score=np.array(hsc, np.float64),
+                        top_k=np.int32(5), **phase)
 
 
 if __name__ == "__main__":

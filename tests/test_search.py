@@ -1,0 +1,165 @@
+"""Search path: k-mer index, Phase-A scoring, SW + rank, continuous batching.
+
+CPU tests pin the numpy restatement (oracle/search_oracle.py) against the
+reference's own outputs (tests/golden/search_golden.npz); GPU tests compare
+the device index, Phase A and the full search with both, and check that a
+query's result is the same alone and inside a concurrent mix.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import search_oracle as so
+from clustkit_gb300 import synth
+from clustkit_gb300.blosum import BLOSUM62
+
+
+def _queries(g):
+    return [g["q_flat"][o:o + L] for o, L in zip(g["q_offsets"], g["q_lengths"])]
+
+
+def test_oracle_index_and_phase_a_match_reference(golden):
+    g = golden("search_golden.npz")
+    k = int(g["k"])
+    off, ent, fr = so.build_kmer_index(g["db_flat"], g["db_offsets"], g["db_lengths"], k)
+    assert np.array_equal(ent, g["kmer_entries"])
+    nz = np.nonzero(fr)[0]
+    assert np.array_equal(nz, g["freq_nonzero_idx"]) and np.array_equal(fr[nz], g["freq_nonzero_val"])
+    assert off[-1] == g["offsets_total"]
+    thr = so.compute_freq_threshold(fr, len(g["db_lengths"]), 95.0)
+    assert thr == int(g["freq_thresh"])
+    for qi, q in enumerate(_queries(g)):
+        ids, c = so.phase_a(q, k, 20, off, ent, fr, thr, len(g["db_lengths"]), 2, 10**9)
+        assert np.array_equal(ids, g[f"q{qi}_ids"]) and np.array_equal(c, g[f"q{qi}_counts"])
+
+
+def _oracle_search(g, top_k):
+    k = int(g["k"])
+    off, ent, fr = so.build_kmer_index(g["db_flat"], g["db_offsets"], g["db_lengths"], k)
+    thr = so.compute_freq_threshold(fr, len(g["db_lengths"]), 95.0)
+    qs = _queries(g)
+    nq, nd = len(qs), len(g["db_lengths"])
+    pairs = []
+    for qi, q in enumerate(qs):
+        ids, _ = so.phase_a(q, k, 20, off, ent, fr, thr, nd, 2, 10**9)
+        pairs += [(qi, t) for t in ids]
+    pairs = np.array(pairs, np.int32).reshape(-1, 2)
+    flat = np.concatenate([g["q_flat"], g["db_flat"]])
+    offs = np.concatenate([g["q_offsets"], g["db_offsets"] + len(g["q_flat"])])
+    lens = np.concatenate([g["q_lengths"], g["db_lengths"]])
+    merged = pairs.copy()
+    merged[:, 1] += nq
+    r = oracle.sw_batch(merged, flat, offs, lens, int(g["band_width"]), BLOSUM62)
+    keep = r["scores"] > 0
+    return so.rank_hits(pairs[keep], r["sims"][keep], r["scores"][keep], g["q_lengths"],
+                        g["db_lengths"], nq, top_k)
+
+
+def _golden_hits(g):
+    hits = [[] for _ in range(len(g["q_lengths"]))]
+    for q, t, i, s in zip(g["hit_query"], g["hit_target"], g["hit_identity"], g["hit_score"]):
+        hits[int(q)].append((int(t), float(i), float(s)))
+    return hits
+
+
+def test_oracle_search_matches_reference(golden):
+    g = golden("search_golden.npz")
+    got = _oracle_search(g, int(g["top_k"]))
+    want = _golden_hits(g)
+    for a, b in zip(got, want):
+        assert [x[0] for x in a] == [x[0] for x in b]
+        assert np.allclose([x[1] for x in a], [x[1] for x in b], rtol=0, atol=0)
+        assert np.allclose([x[2] for x in a], [x[2] for x in b], rtol=0, atol=0)
+
+
+@pytest.mark.gpu
+def test_device_index_and_phase_a(ck, golden):
+    torch = pytest.importorskip("torch")
+    from clustkit_gb300.search import DeviceDatabase, _Slot
+    g = golden("search_golden.npz")
+    db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["band_width"]),
+                        arena_queries=32, arena_residues=32 * 400)
+    off, ent, fr = db.index_arrays()
+    assert np.array_equal(ent, g["kmer_entries"])
+    nz = np.nonzero(fr)[0]
+    assert np.array_equal(nz, g["freq_nonzero_idx"]) and np.array_equal(fr[nz], g["freq_nonzero_val"])
+    assert off[-1] == g["offsets_total"] and db.freq_thresh == int(g["freq_thresh"])
+    slot = _Slot(db, 0, 1000)
+    try:
+        qs = _queries(g)
+        slot.launch(qs, 2)
+        slot.event.synchronize()
+        n = slot.h_n.numpy()[:len(qs)]
+        tg = slot.h_targets.numpy().reshape(-1, 1000)
+        for qi in range(len(qs)):
+            assert np.array_equal(tg[qi, :n[qi]], g[f"q{qi}_ids"]), qi
+        slot.results(5)
+    finally:
+        slot.close()
+
+
+@pytest.mark.gpu
+def test_search_batch_matches_reference(ck, golden):
+    from clustkit_gb300.search import DeviceDatabase, search_batch
+    g = golden("search_golden.npz")
+    db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["band_width"]),
+                        arena_queries=8, arena_residues=8 * 400)
+    res = search_batch(db, _queries(g), top_k=int(g["top_k"]), max_cands=1000)
+    want = _golden_hits(g)
+    for hits, w in zip(res, want):
+        assert [h.target for h in hits] == [x[0] for x in w]
+        assert [h.identity for h in hits] == [x[1] for x in w]
+        assert [np.float32(h.rank) for h in hits] == [np.float32(x[2]) for x in w]
+
+
+@pytest.mark.gpu
+def test_phase_a_cap_and_ties_vs_oracle(ck):
+    from clustkit_gb300.search import DeviceDatabase, _Slot
+    db_set = synth.generate_families(300, 8, median=150, lo=40, hi=400, seed=91)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=16,
+                        arena_residues=16 * 500)
+    off, ent, fr = db.index_arrays()
+    rng = np.random.default_rng(3)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 12, replace=False)]
+    qs += [np.tile(np.array([1, 2, 3, 4, 5, 6], np.uint8), 30), np.arange(60, dtype=np.uint8) % 20]
+    for cap in (3, 17, 500):
+        slot = _Slot(db, 0, cap)
+        try:
+            slot.launch(qs, 1)
+            slot.event.synchronize()
+            n = slot.h_n.numpy()[:len(qs)]
+            tg = slot.h_targets.numpy().reshape(-1, cap)
+            for qi, q in enumerate(qs):
+                ids, _ = so.phase_a(q, 5, 20, off, ent, fr, db.freq_thresh, db_set.n, 1, cap)
+                assert np.array_equal(tg[qi, :n[qi]], ids), (cap, qi)
+            slot.results(3)
+        finally:
+            slot.close()
+
+
+@pytest.mark.gpu
+def test_server_results_same_alone_and_in_mix(ck):
+    """Each query's hits are identical whether it is searched alone or lands
+    in concurrent batches of the continuous-batching server."""
+    from clustkit_gb300.search import DeviceDatabase, SearchServer, search_batch
+    db_set = synth.generate_families(400, 10, median=200, lo=40, hi=600, seed=92)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_slots=3, arena_queries=16,
+                        arena_residues=16 * 600)
+    rng = np.random.default_rng(5)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 40, replace=False)]
+    bg = synth.random_sequences(20, median=200, lo=40, hi=600, seed=93)
+    qs += [bg.seq(i).copy() for i in range(bg.n)]
+    alone = [search_batch(db, [q], top_k=10)[0] for q in qs]
+    server = SearchServer(db, top_k=10, max_batch=7).start()
+    try:
+        futs = [server.submit(q) for q in qs]
+        mixed = [f.result(timeout=120) for f in futs]
+    finally:
+        server.stop()
+    assert len(server.slots) >= 2
+    for a, b in zip(alone, mixed):
+        assert [(h.target, h.identity, h.score, h.rank) for h in a] == \
+            [(h.target, h.identity, h.score, h.rank) for h in b]
+    assert any(len(h) for h in mixed)
+    lat = server.latency_percentiles()
+    assert lat["n"] == len(qs)
