@@ -101,6 +101,10 @@ static int32_t index_build_impl(void *pv) {
     int64_t P = 0;
     CK_CUDA(cudaMemcpyAsync(&P, cnt + a.n, 8, cudaMemcpyDeviceToHost, a.st));
     CK_CUDA(cudaStreamSynchronize(a.st));
+    if (P >= ((int64_t)1 << 31)) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "kmer index: more than 2^31-1 k-mer positions in one build");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
     if (P > a.capacity) {
         set_error(CK_ERR_INVALID_ARGUMENT, "kmer index: entries capacity below the number of k-mer positions");
         return CK_ERR_INVALID_ARGUMENT;
@@ -339,7 +343,7 @@ extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat,
                                             int32_t *d_out_n, void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
-    if (nq < 0 || top_k < 1 || k < 1 || alpha < 1 || num_db < 0 || !d_out_targets || !d_out_n ||
+    if (nq < 0 || nq > 65535 || top_k < 1 || k < 1 || alpha < 1 || num_db < 0 || !d_out_targets || !d_out_n ||
         (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets || !d_kmer_freqs) {
         set_error(CK_ERR_INVALID_ARGUMENT, "phase A: bad arguments");
         return CK_ERR_INVALID_ARGUMENT;
