@@ -492,9 +492,25 @@ def run_search(args, n_db_fam=50000):
         search_batch(db, [q], top_k=10, slot=slot)
         lat.append(time.perf_counter() - a)
     plain_qps = n_plain / (time.perf_counter() - tp0)
+    # device time per stage of a one-query batch (separate pass: events add syncs)
+    slot.enable_stage_timing()
+    stages = []
+    for q in qs[:50]:
+        search_batch(db, [q], top_k=10, slot=slot)
+        stages.append(slot.stage_ms())
+    full = []
+    for r in range(5):
+        search_batch(db, qs[64 * r:64 * (r + 1)], top_k=10, slot=slot)
+        full.append(slot.stage_ms())
     slot.close()
+    full_med = np.median(np.array(full), axis=0)
+    st_med = np.median(np.array(stages), axis=0)
     plain = {"qps": plain_qps, "p50_ms": float(np.percentile(lat, 50) * 1e3),
-             "p99_ms": float(np.percentile(lat, 99) * 1e3), "queries": n_plain}
+             "p99_ms": float(np.percentile(lat, 99) * 1e3), "queries": n_plain,
+             "device_stage_ms_median": {"h2d": float(st_med[0]), "phase_a": float(st_med[1]),
+                                        "sw": float(st_med[2]), "d2h": float(st_med[3])},
+             "device_stage_ms_median_batch64": {"h2d": float(full_med[0]), "phase_a": float(full_med[1]),
+                                                "sw": float(full_med[2]), "d2h": float(full_med[3])}}
     server = SearchServer(db, top_k=10, max_cands=500).start()
     sweep = []
     rng = np.random.default_rng(3)
@@ -508,8 +524,9 @@ def run_search(args, n_db_fam=50000):
             t_start = time.perf_counter()
             for i in range(n):
                 target = t_start + arr[i]
-                while time.perf_counter() < target:
-                    pass
+                lag = target - time.perf_counter()
+                if lag > 0:
+                    time.sleep(lag)  # sleeping releases the GIL to the scheduler thread
                 futs.append(server.submit(qs[qi % len(qs)], t_arrival=target))
                 qi += 1
             for f in futs:

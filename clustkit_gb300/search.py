@@ -175,11 +175,26 @@ class _Slot:
         self.h_mask = pin(Q * K, torch.uint8)
         self.event = torch.cuda.Event()
         self.batch = None
+        # optional stage events: start, after the H2D copy, after Phase A, after SW, end
+        self.stage_events = None
 
     def close(self):
         if self.ctx:
             self.db.lib.ck_ctx_destroy(self.ctx)
             self.ctx = 0
+
+    def enable_stage_timing(self):
+        torch = _torch()
+        self.stage_events = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+
+    def stage_ms(self):
+        """(h2d, phase_a, sw, d2h) milliseconds of the last batch (after its event)."""
+        ev = self.stage_events
+        return tuple(ev[i].elapsed_time(ev[i + 1]) for i in range(4))
+
+    def _mark(self, i):
+        if self.stage_events is not None:
+            self.stage_events[i].record(self.stream)
 
     def launch(self, queries: list[np.ndarray], min_total_hits: int):
         """Enqueue the whole pipeline for a batch on this slot's stream."""
@@ -203,16 +218,19 @@ class _Slot:
         lib = db.lib
         with torch.cuda.stream(self.stream):
             st = self.stream.cuda_stream
+            self._mark(0)
             db.d_flat[self.res0:self.res0 + tot].copy_(self.h_res[:tot], non_blocking=True)
             db.d_offsets[self.seq0:self.seq0 + nq].copy_(self.h_off[:nq], non_blocking=True)
             db.d_lengths[self.seq0:self.seq0 + nq].copy_(self.h_len[:nq], non_blocking=True)
             qoff_ptr = db.d_offsets.data_ptr() + self.seq0 * 8
             qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
+            self._mark(1)
             _lib.check(lib.ck_search_phase_a_device(
                 self.ctx, db.d_flat.data_ptr(), qoff_ptr, qlen_ptr, nq, int(lens.max() if nq else 0),
                 db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+            self._mark(2)
             # dense pair list: (query, target) or (empty, empty) past a query's candidates
             q = self.d_slotq[:M]
             valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
@@ -226,11 +244,13 @@ class _Slot:
                 np.ascontiguousarray(BLOSUM62).ctypes.data, 0.0, None, PASS_SCORE, ENGINE_BATCHED,
                 self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(),
                 st))
+            self._mark(3)
             self.h_n[:nq].copy_(self.d_n[:nq], non_blocking=True)
             self.h_targets[:M].copy_(self.d_targets[:M], non_blocking=True)
             self.h_sims[:M].copy_(self.d_sims[:M], non_blocking=True)
             self.h_scores[:M].copy_(self.d_scores[:M], non_blocking=True)
             self.h_mask[:M].copy_(self.d_mask[:M], non_blocking=True)
+            self._mark(4)
             self.event.record(self.stream)
         self.batch = (nq, lens)
 
@@ -245,17 +265,24 @@ class _Slot:
         sims = self.h_sims.numpy()[: nq * K].reshape(nq, K)
         scores = self.h_scores.numpy()[: nq * K].reshape(nq, K)
         mask = self.h_mask.numpy()[: nq * K].reshape(nq, K)
+        # one vectorised pass over the batch: candidates that passed, their
+        # rank, then a stable sort by (query, -rank) -- per query this is the
+        # stable descending-rank order
+        col = np.arange(K)[None, :]
+        keep = (col < n[:, None]) & mask.astype(bool)
+        qi, ci = np.nonzero(keep)
+        t = tg[qi, ci]
+        sc = scores[qi, ci]
+        si = sims[qi, ci]
+        rank = LAMBDA * sc.astype(np.float32) - np.log(
+            lens[qi].astype(np.float32) * db.lengths_host[t].astype(np.float32))
+        order = np.lexsort((-rank, qi))
+        qs = qi[order]
+        first = np.searchsorted(qs, np.arange(nq + 1))
         out = []
-        for qi in range(nq):
-            c = int(n[qi])
-            keep = mask[qi, :c].astype(bool)
-            t = tg[qi, :c][keep]
-            sc = scores[qi, :c][keep]
-            si = sims[qi, :c][keep]
-            rank = LAMBDA * sc.astype(np.float32) - np.log(
-                np.float32(lens[qi]) * db.lengths_host[t].astype(np.float32))
-            order = np.argsort(-rank, kind="stable")[:top_k]
-            out.append([SearchHit(qi, int(t[o]), float(si[o]), int(sc[o]), float(rank[o])) for o in order])
+        for q in range(nq):
+            sel = order[first[q]:min(first[q + 1], first[q] + top_k)]
+            out.append([SearchHit(q, int(t[o]), float(si[o]), int(sc[o]), float(rank[o])) for o in sel])
         self.batch = None
         return out
 
