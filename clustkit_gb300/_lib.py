@@ -25,6 +25,8 @@ PASS_CPU, PASS_NUMBA, PASS_CUPY, PASS_SCORE = 0, 1, 2, 3
 ENGINE_BATCHED, ENGINE_PLAIN = 0, 1
 CFG_ROWS_PER_STRIP = 0
 CFG_STRIP_VARIANT = 1
+CFG_WAVE_MIN_ROWS = 2
+CFG_WAVE_ALL_BELOW = 3
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -55,6 +57,7 @@ SIGNATURES = {
     "ck_search_phase_a_device": (_I32, [_I32, _P, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _I32, _I32,
                                         _I32, _I32, _P, _P, _P, _P]),
     "ck_sw_last_counters": (_I32, [_P]),
+    "ck_sw_last_wave_pairs": (_I32, [_P]),
     "ck_sketch": (_I32, [_P, _I64, _P, _P, _I64, _I32, _I32, _I32, ctypes.c_uint64, _P]),
     "ck_sketch_device": (_I32, [_P, _I64, _P, _P, _I64, _I32, _I32, _I32, ctypes.c_uint64, _P, _P]),
     "ck_jaccard": (_I32, [_P, _I64, _P, _I64, _I32, ctypes.c_float, _P, _P]),
@@ -119,7 +122,11 @@ def sw_counters() -> dict:
     out = np.zeros(6, np.int64)
     check(load().ck_sw_last_counters(out.ctypes.data))
     keys = ("pairs", "cells", "batched", "plain", "rerun", "launches")
-    return {k: int(v) for k, v in zip(keys, out)}
+    d = {k: int(v) for k, v in zip(keys, out)}
+    wave = np.zeros(1, np.int64)
+    check(load().ck_sw_last_wave_pairs(wave.ctypes.data))
+    d["wave"] = int(wave[0])
+    return d
 
 
 def set_config(key: int, value: int) -> None:

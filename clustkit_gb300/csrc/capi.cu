@@ -291,6 +291,12 @@ int32_t ck_sw_last_counters(int64_t *out6) {
     return CK_OK;
 }
 
+int32_t ck_sw_last_wave_pairs(int64_t *out) {
+    if (!out) return CK_ERR_INVALID_ARGUMENT;
+    *out = t_counters.wave;
+    return CK_OK;
+}
+
 static int32_t check_sw_args(const void *pairs, int64_t M, const void *flat, int64_t flat_len,
                              const void *offsets, const void *lengths, int64_t n_seqs,
                              const int8_t *sub, int32_t pass_rule, int32_t engine) {
@@ -470,6 +476,8 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     t_status = CK_OK;
     if (key == CK_CFG_ROWS_PER_STRIP) return sw_set_rows_per_strip(value);
     if (key == CK_CFG_STRIP_VARIANT) return sw_set_variant(value);
+    if (key == CK_CFG_WAVE_MIN_ROWS) return sw_set_wave(0, value);
+    if (key == CK_CFG_WAVE_ALL_BELOW) return sw_set_wave(1, value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -479,6 +487,8 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (!value) return CK_ERR_INVALID_ARGUMENT;
     if (key == CK_CFG_ROWS_PER_STRIP) { *value = sw_rows_per_strip(); return CK_OK; }
     if (key == CK_CFG_STRIP_VARIANT) { *value = sw_variant(); return CK_OK; }
+    if (key == CK_CFG_WAVE_MIN_ROWS) { *value = sw_wave(0); return CK_OK; }
+    if (key == CK_CFG_WAVE_ALL_BELOW) { *value = sw_wave(1); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

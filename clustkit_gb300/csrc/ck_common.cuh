@@ -150,7 +150,7 @@ __device__ __forceinline__ bool cupy_ratio_skip(const SwIn &in, int32_t la, int3
 
 // ---------------------------------------------------------------- launchers
 struct SwCounters {
-    int64_t pairs, cells, batched, plain, rerun, launches;
+    int64_t pairs, cells, batched, plain, rerun, launches, wave;
 };
 
 int32_t sw_plain_launch(const SwIn &in, const SwOut &out, int64_t M, const int32_t *d_index,
@@ -163,6 +163,8 @@ int32_t sw_set_rows_per_strip(int32_t r);
 int32_t sw_rows_per_strip();
 int32_t sw_set_variant(int32_t v);
 int32_t sw_variant();
+int32_t sw_set_wave(int32_t key, int32_t v);  // key 0: min rows, 1: all-pairs batch limit
+int32_t sw_wave(int32_t key);
 int32_t sw_run_device(const SwIn &in, const SwOut &out, int64_t M, int32_t engine,
                       const int8_t *sub_host, cudaStream_t st, SwCounters *ctr,
                       bool read_counters);

@@ -128,14 +128,28 @@ __host__ __device__ inline int64_t band_cells_closed(int32_t la, int32_t lb, int
     return sum_min(ilo, ihi, c2, lb) - sum_max(ilo, ihi, c1, 1) + (ihi - ilo + 1);
 }
 
+// Rows per lane strip for the warp-per-pair kernel, 0 when it cannot take
+// the pair.  Lane l runs strips l, l + 32, ... one column behind lane l - 1;
+// a lane may only start its next strip once its previous one (R + 2w - 1
+// steps) is done and its upstream lane has moved past the band, which holds
+// when 2w < 31 R + 32, or trivially when the pair has at most 32 strips.
+// The smallest such R keeps the most lanes busy.
+__host__ __device__ inline int32_t wave_rows_per_strip(int32_t la, int32_t w) {
+    if (la <= 128 || 2 * w < 31 * 4 + 32) return 4;
+    if (la <= 256 || 2 * w < 31 * 8 + 32) return 8;
+    if (la <= 512 || 2 * w < 31 * 16 + 32) return 16;
+    return 0;
+}
+
 // ----------------------------------------------------------------- prep
 __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restrict__ seq_ok,
                                uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
                                int32_t *__restrict__ fallback, int32_t *__restrict__ counters,
-                               unsigned long long *__restrict__ cells, int32_t *err) {
-    // counters[0] = eligible, counters[1] = fallback count
+                               unsigned long long *__restrict__ cells, int32_t wave_min_rows,
+                               int32_t *err) {
+    // counters[0] = eligible, counters[1] = fallback count, counters[6] = wave pairs
     int64_t local_cells = 0;
-    int32_t elig = 0;
+    int32_t elig = 0, wave = 0;
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < M;
          p += (int64_t)gridDim.x * blockDim.x) {
         PairGeom g = pair_geometry(in, p, err);
@@ -150,6 +164,10 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
                 seq_codes_ok(in, g.b_idx, seq_ok)) {
                 int32_t cb = g.lb < key::ROWS_MAX ? g.lb : key::ROWS_MAX;
                 k = ((uint32_t)g.la << 13) | (uint32_t)cb;
+                if (g.la >= wave_min_rows && wave_rows_per_strip(g.la, g.w) > 0) {
+                    k |= 1u << 26;  // warp-per-pair kernel; sorts ahead of the strip pairs
+                    wave++;
+                }
                 elig++;
             } else {
                 int32_t pos = atomicAdd(&counters[1], 1);
@@ -162,10 +180,12 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
     for (int o = 16; o; o >>= 1) {
         local_cells += __shfl_xor_sync(0xffffffffu, local_cells, o);
         elig += __shfl_xor_sync(0xffffffffu, elig, o);
+        wave += __shfl_xor_sync(0xffffffffu, wave, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (local_cells) atomicAdd(cells, (unsigned long long)local_cells);
         if (elig) atomicAdd(&counters[0], elig);
+        if (wave) atomicAdd(&counters[6], wave);
     }
 }
 
@@ -378,14 +398,18 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 int32_t *__restrict__ fallback, int32_t *__restrict__ fallback_count,
                 int32_t *err, int32_t one) {
     extern __shared__ int32_t s_inc[];
+    if (counters[0] <= counters[6]) return;  // every pair went to the warp-per-pair kernel
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
     __syncthreads();
     int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
     const int32_t lane = threadIdx.x & 31;
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int2 *win = window + (size_t)gwarp * (size_t)W * 32 + lane;
-    const int32_t n_elig = counters[0];
+    // the first counters[6] sorted pairs belong to the warp-per-pair kernel
+    const int32_t n_skip = counters[6];
+    const int32_t n_elig = counters[0] - n_skip;
     const int32_t n_groups = (n_elig + 31) >> 5;
+    order += n_skip;
     for (;;) {
         __syncwarp();
         int32_t grp = 0;
@@ -399,6 +423,176 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
     }
 }
 
+// ----------------------------------------------------------------- wave kernel
+// One warp per pair, for pairs too few to fill the GPU one per lane and for
+// long pairs whose serial time would set the strip kernel's tail.  Rows are
+// cut into strips of R; lane l computes strips l, l + 32, l + 64, ..., and
+// at step T strip s works on column j = T - s + 1 + h - w, one column behind
+// strip s - 1.  Each step a lane receives by shuffle the (H, E) of the row
+// above its strip at column j, which the upstream lane produced the step
+// before, and the H it received the step before is its diagonal input.  A
+// lane outside its strip's columns sends the out-of-band boundary
+// (H = 0, E = -inf), and a lane whose upstream row has left its band
+// replaces what it receives by that boundary, so a lane that has moved on to
+// its next strip is never read.  Cells use the strip kernel's masked step.
+//
+// First maximum: a warp-wide running best score gs; when some lane's column
+// holds a score >= gs, every lane updates its per-row trackers (strict '>'
+// along a row) and gs rises.  A cell below gs cannot be the pair's maximum;
+// one equal to it may be, in an earlier row, so '>=' triggers.  At the end
+// of a strip its rows merge into the lane's best in row order (strict '>');
+// at the end of the pair the lanes agree on the best score, then on the
+// lowest row holding it -- clustkit's first cell in row-major order.
+template <int R>
+__device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, const PairGeom &g,
+                                const char *s_inc, int32_t *s_best, int32_t lane, int32_t *fallback,
+                                int32_t *fallback_count, int32_t one) {
+    using namespace key;
+    constexpr int32_t D = R + 1;
+    const int32_t la = g.la, lb = g.lb, w = g.w, h = g.h;
+    const uint8_t *A = in.flat + in.offsets[g.a_idx];
+    const uint8_t *B = in.flat + in.offsets[g.b_idx];
+    const uint32_t w2 = 2u * (uint32_t)w;
+    const int32_t c0 = 1 + h - w;  // j = T - s + c0
+
+    // strips that reach column <= lb (later ones lie right of the matrix)
+    int32_t n_strips = (la + R - 1) / R;
+    {
+        const int64_t lim = (int64_t)lb - 1 - h + w;  // s * R <= lim
+        const int64_t s_lim = lim < 0 ? 0 : lim / R + 1;
+        if (s_lim < n_strips) n_strips = (int32_t)s_lim;
+    }
+    int32_t lbest = 0, lrow = INT32_MAX;
+    if (n_strips > 0) {
+        const int32_t J0_0 = c0 > 1 ? c0 : 1;
+        const int32_t T_first = J0_0 - c0;
+        const int32_t sl = n_strips - 1;
+        const int32_t J1_l = sl * R + R + h + w < lb ? sl * R + R + h + w : lb;
+        const int32_t T_last = J1_l + sl - c0;
+
+        // this lane's strip at T_first; with at most 32 strips each lane has
+        // one and keeps it (its band may then be wider than the rotation allows)
+        const bool rotate = n_strips > 32;
+        int32_t s = lane;
+        if (rotate && T_first >= lane * D) s = lane + 32 * ((T_first - lane * D) / (32 * D));
+        int32_t next_switch = rotate ? (s + 32) * D : INT32_MAX;
+        int32_t i0 = 0, lo0 = 0, J0 = 0, J1 = -1, alive = 0;
+        StripRegs<R> S;
+        auto setup = [&]() {
+            i0 = s * R + 1;
+            lo0 = i0 + h - w;
+            J0 = lo0 > 1 ? lo0 : 1;
+            J1 = i0 + R - 1 + h + w < lb ? i0 + R - 1 + h + w : lb;
+            if (s >= n_strips) { J0 = 1; J1 = 0; }
+            alive = la - i0 + 1 < R ? la - i0 + 1 : R;
+            if (alive < 0) alive = 0;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                S.hc[r] = 0;
+                S.fT[r] = NEG_F;
+                s_best[r * STRIP_THREADS] = 0;
+                const uint32_t code = (r < alive && s < n_strips) ? (uint32_t)A[i0 + r - 1] : 0u;
+                S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
+            }
+        };
+        auto merge = [&]() {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int32_t b = s_best[r * STRIP_THREADS];
+                if (r < alive && b > (lbest | (KU - 1))) { lbest = b; lrow = i0 + r; }
+            }
+        };
+        setup();
+        int32_t hout = 0, eout = NEG_E, hprev = 0, gs = 1;
+        for (int32_t T = T_first; T <= T_last; ++T) {
+            if (T == next_switch) {
+                merge();
+                s += 32;
+                next_switch += 32 * D;
+                setup();
+            }
+            const int32_t j = T - s + c0;
+            int32_t hin = __shfl_sync(0xffffffffu, hout, (lane + 31) & 31);
+            int32_t ein = __shfl_sync(0xffffffffu, eout, (lane + 31) & 31);
+            if (s == 0 || j > s * R + h + w) { hin = 0; ein = NEG_E; }
+            const int32_t hdiag = hprev;
+            hprev = hin;
+            int32_t cm = 0;
+            if (j >= J0 && j <= J1) {
+                const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
+                int32_t hu = hin, eu = ein;
+                strip_cells<R, 0, R, true>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive, one);
+                hout = hu;
+                eout = eu;
+                cm = S.hc[0];
+#pragma unroll
+                for (int r = 1; r + 1 < R; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
+                if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
+            } else {
+                hout = 0;
+                eout = NEG_E;
+            }
+            if (__any_sync(0xffffffffu, (cm >> 16) >= gs)) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int32_t b = s_best[r * STRIP_THREADS];
+                    if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
+                }
+                const int32_t m = __reduce_max_sync(0xffffffffu, cm >> 16);
+                if (m > gs) gs = m;
+            }
+        }
+        merge();
+    }
+    // lanes agree on the best score, then on the lowest row holding it
+    const int32_t best = __reduce_max_sync(0xffffffffu, lbest >> 16);
+    const int32_t row = __reduce_min_sync(0xffffffffu, (best > 0 && (lbest >> 16) == best) ? lrow : INT32_MAX);
+    const bool writer = best > 0 ? ((lbest >> 16) == best && lrow == row) : lane == 0;
+    const uint32_t wmask = __ballot_sync(0xffffffffu, writer);
+    if (lane != __ffs(wmask) - 1) return;
+    if (best >= SCORE_LIMIT) {
+        const int32_t pos = atomicAdd(fallback_count, 1);
+        fallback[pos] = (int32_t)p;
+        atomicAdd(fallback_count + 2, 1);  // re-run counter
+        return;
+    }
+    write_result(out, in, p, best, best > 0 ? (lbest & MATCH_MASK) : 0, la, la, lb);
+}
+
+__global__ void __launch_bounds__(STRIP_THREADS, 2)
+sw_wave_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
+               const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
+               int32_t *__restrict__ ticket, int32_t *__restrict__ fallback,
+               int32_t *__restrict__ fallback_count, int32_t *err, int32_t one) {
+    extern __shared__ int32_t s_inc[];
+    const int32_t n_wave = counters[6];
+    if (n_wave <= 0) return;
+    for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
+    __syncthreads();
+    int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
+    const int32_t lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        int32_t q = 0;
+        if (lane == 0) q = atomicAdd(ticket, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n_wave) break;
+        const int64_t p = (int64_t)order[q];
+        const PairGeom g = pair_geometry(in, p, err);
+        switch (wave_rows_per_strip(g.la, g.w)) {
+            case 4:
+                align_pair_wave<4>(in, out, p, g, (const char *)s_inc, s_best, lane, fallback, fallback_count, one);
+                break;
+            case 8:
+                align_pair_wave<8>(in, out, p, g, (const char *)s_inc, s_best, lane, fallback, fallback_count, one);
+                break;
+            default:
+                align_pair_wave<16>(in, out, p, g, (const char *)s_inc, s_best, lane, fallback, fallback_count, one);
+                break;
+        }
+    }
+}
+
 // ----------------------------------------------------------------- driver
 static int32_t pow2_at_least(int64_t x) {
     int32_t p = 1;
@@ -409,6 +603,20 @@ static int32_t pow2_at_least(int64_t x) {
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
 static int32_t g_rows_per_strip = 16;
 static int32_t g_variant = 1;
+// pairs with at least this many rows go to the warp-per-pair kernel ...
+static int32_t g_wave_min_rows = 1024;
+// ... and every pair does when a call has at most this many pairs
+static int32_t g_wave_all_below = 24576;
+
+int32_t sw_set_wave(int32_t key, int32_t v) {
+    if (v < 0) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "warp-per-pair thresholds must be >= 0");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    if (key == 0) g_wave_min_rows = v; else g_wave_all_below = v;
+    return CK_OK;
+}
+int32_t sw_wave(int32_t key) { return key == 0 ? g_wave_min_rows : g_wave_all_below; }
 
 int32_t sw_set_variant(int32_t v) {
     if (v < 0 || v > 3) {
@@ -419,6 +627,22 @@ int32_t sw_set_variant(int32_t v) {
     return CK_OK;
 }
 int32_t sw_variant() { return g_variant; }
+
+static int32_t launch_wave(const SwIn &in, const SwOut &out, const uint32_t *order,
+                           const int32_t *counters, const int32_t *inc, int32_t *ticket,
+                           int32_t *fallback, int32_t *fb_count, int32_t *err, cudaStream_t st,
+                           SwCounters *ctr) {
+    const size_t smem = strip_smem<16>();
+    CK_CUDA(cudaFuncSetAttribute(sw_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw_wave_kernel, STRIP_THREADS, smem));
+    if (per_sm < 1) per_sm = 1;
+    sw_wave_kernel<<<sm_count() * per_sm, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, ticket,
+                                                                     fallback, fb_count, err, 1);
+    CK_CUDA(cudaGetLastError());
+    if (ctr) ctr->launches += 1;
+    return CK_OK;
+}
 
 template <int R>
 static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
@@ -457,12 +681,9 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     if (blocks < 1) blocks = 1;
     int2 *window = (int2 *)scratch(SLOT_WINDOW, (size_t)blocks * per_block, &status);
     if (!window) return status;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
     kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
                                               fallback, fb_count, err, 1);
     CK_CUDA(cudaGetLastError());
-    if (ev1) CK_CUDA(cudaEventRecord(ev1, st));
     if (ctr) ctr->launches += 1;
     return CK_OK;
 }
@@ -513,17 +734,22 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
     if (M > 0) {
         int64_t want = (M + 255) / 256;
         int blocks = (int)(want < 16 * (int64_t)sm_count() ? want : 16 * (int64_t)sm_count());
-        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, d_err);
+        const int32_t wave_rows = M <= (int64_t)g_wave_all_below ? 0 : g_wave_min_rows;
+        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, wave_rows, d_err);
         CK_CUDA(cudaGetLastError());
         cub::DoubleBuffer<uint32_t> dk(k0, k1), dv(v0, v1);
         size_t temp = 0;
-        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, temp, dk, dv, (int)M, 0, 26, st));
+        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, temp, dk, dv, (int)M, 0, 27, st));
         void *tmp = scratch(SLOT_SORT_TEMP, temp > 0 ? temp : 1, &status);
         if (!tmp) return status;
-        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, dk, dv, (int)M, 0, 26, st));
+        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, dk, dv, (int)M, 0, 27, st));
         int32_t wmax = 0;
         CK_TRY(widest_band(in, st, &wmax));
         const uint32_t *order = dv.Current();
+        // profiling events bracket the two alignment kernels (wave, then strip)
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
+        CK_TRY(launch_wave(in, out, order, cnt, inc, cnt + 7, fb, cnt + 1, d_err, st, ctr));
         switch (g_rows_per_strip) {
             case 8:
                 CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
@@ -535,6 +761,7 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
                 CK_TRY(launch_strips_v<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;
         }
+        if (ev1) CK_CUDA(cudaEventRecord(ev1, st));
         if (ctr) ctr->launches += 1;
     }
     // plain kernel over the fallback list (its length is read on the device)
@@ -542,12 +769,14 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
     if (read_counters && ctr) {
         int32_t hcnt[8];
         CK_CUDA(cudaMemcpyAsync(hcnt, cnt, 32, cudaMemcpyDeviceToHost, st));
+        // hcnt[6]: pairs the warp-per-pair kernel took (part of hcnt[0])
         CK_CUDA(cudaStreamSynchronize(st));
         unsigned long long c = 0;
         memcpy(&c, hcnt + 4, sizeof(c));
         ctr->batched += hcnt[0];
         ctr->plain += hcnt[1];
         ctr->rerun += hcnt[3];
+        ctr->wave += hcnt[6];
         ctr->cells += (int64_t)c;
     }
     return CK_OK;

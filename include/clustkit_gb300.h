@@ -142,6 +142,9 @@ int32_t ck_sw_status_device(void *stream);
  * kernel, out[4] pairs re-run after a score overflowed the packed lane,
  * out[5] kernel launches issued. */
 int32_t ck_sw_last_counters(int64_t *out6);
+/* Of the batched pairs of the same call, how many ran one warp per pair
+ * (long pairs, or every pair of a small call; see CK_CFG_WAVE_*). */
+int32_t ck_sw_last_wave_pairs(int64_t *out);
 
 /* Kernel timing for measurement: after ck_sw_profile(1), every SW call
  * records CUDA events on its stream around its dominant kernel (the strip
@@ -156,9 +159,16 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24
  *   CK_CFG_STRIP_VARIANT   0..3: bit 0 prefetches the next columns' inputs two
  *                          columns ahead (else one), bit 1 runs interior
- *                          columns four at a time (else two) */
+ *                          columns four at a time (else two)
+ *   CK_CFG_WAVE_MIN_ROWS   pairs with at least this many rows (shorter side)
+ *                          run one warp per pair instead of one lane per pair
+ *                          (default 1024)
+ *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs run every pair
+ *                          one warp per pair (default 24576) */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
+#define CK_CFG_WAVE_MIN_ROWS 2
+#define CK_CFG_WAVE_ALL_BELOW 3
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

@@ -3,6 +3,7 @@
 Bit-exact integer parity: scores, identity numerator and denominator, the
 float32 identity (matches/shorter, correctly rounded) and pass/fail.
 """
+import contextlib
 import ctypes
 
 import numpy as np
@@ -59,12 +60,14 @@ def test_golden_numba_twin(ck, golden, engine):
 @pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("bw,median,hi,dist", [(100, 300, 800, "lognormal"), (32, 350, 2000, "lognormal"),
                                                (16, 200, 3000, "pareto"), (64, 120, 400, "lognormal")])
-def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist):
+@pytest.mark.parametrize("route", ["default", "strip"])
+def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist, route):
     s = synth.generate_families(30, 8, median=median, lo=30, hi=hi, seed=bw + median,
                                 length_dist=dist)
     pairs = synth.mixed_pairs(s, 4000, seed=bw, min_ratio=0.0)
     ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
-    r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, 0.3, engine=engine)
+    with wave_config(*((0, 1 << 30) if route == "strip" else (24576, 1024))):
+        r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, 0.3, engine=engine)
     _same(r, ref)
     assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
 
@@ -73,22 +76,87 @@ def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist):
                                           (24, 3)])
 @pytest.mark.parametrize("bw", [3, 32, 100, 0])
 def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
-    from clustkit_gb300._lib import CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, get_config, set_config
+    from clustkit_gb300._lib import (CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, CFG_WAVE_ALL_BELOW,
+                                     CFG_WAVE_MIN_ROWS, get_config, set_config)
     keep = (get_config(CFG_ROWS_PER_STRIP), get_config(CFG_STRIP_VARIANT))
     try:
         set_config(CFG_ROWS_PER_STRIP, rows)
         set_config(CFG_STRIP_VARIANT, variant)
-        g = golden("sw_golden.npz")
-        r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
-        assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
-        assert np.array_equal(r["sims"], g[f"bw{bw}_sims"])
-        s = synth.generate_families(25, 8, median=300, lo=30, hi=1500, seed=rows + bw)
-        pairs = synth.mixed_pairs(s, 3000, seed=rows)
-        _same(batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62),
-              oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+        with wave_config(all_below=0, min_rows=1 << 30):  # strip kernel only
+            g = golden("sw_golden.npz")
+            r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
+            assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
+            assert np.array_equal(r["sims"], g[f"bw{bw}_sims"])
+            s = synth.generate_families(25, 8, median=300, lo=30, hi=1500, seed=rows + bw)
+            pairs = synth.mixed_pairs(s, 3000, seed=rows)
+            _same(batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62),
+                  oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+            assert ck.sw_counters()["batched"] > 0
     finally:
         set_config(CFG_ROWS_PER_STRIP, keep[0])
         set_config(CFG_STRIP_VARIANT, keep[1])
+
+
+@contextlib.contextmanager
+def wave_config(all_below, min_rows):
+    """Route pairs between the warp-per-pair and the lane-per-pair kernels."""
+    from clustkit_gb300._lib import CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, get_config, set_config
+    keep = (get_config(CFG_WAVE_ALL_BELOW), get_config(CFG_WAVE_MIN_ROWS))
+    set_config(CFG_WAVE_ALL_BELOW, all_below)
+    set_config(CFG_WAVE_MIN_ROWS, min_rows)
+    try:
+        yield
+    finally:
+        set_config(CFG_WAVE_ALL_BELOW, keep[0])
+        set_config(CFG_WAVE_MIN_ROWS, keep[1])
+
+
+# every pair on the warp-per-pair kernel; a split at 64 rows; only long pairs
+WAVE_ROUTES = [(1 << 30, 0), (0, 64), (0, 1024)]
+
+
+@pytest.mark.parametrize("all_below,min_rows", WAVE_ROUTES)
+@pytest.mark.parametrize("bw", [0, 3, 16, 32, 50, 100, 128, 238, 300])
+def test_wave_kernel_golden_and_random(ck, golden, all_below, min_rows, bw):
+    with wave_config(all_below, min_rows):
+        g = golden("sw_golden.npz")
+        if f"bw{bw}_scores" in g.files:
+            r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
+            assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
+            assert np.array_equal(r["sims"], g[f"bw{bw}_sims"])
+        s = synth.generate_families(30, 8, median=400, lo=20, hi=2500, seed=bw + 3)
+        pairs = synth.mixed_pairs(s, 2500, seed=bw)
+        rng = np.random.default_rng(bw)
+        L = s.lengths
+        sh = np.minimum(L[pairs[:, 0]], L[pairs[:, 1]])
+        hints = (rng.integers(-1000, 1000, len(pairs)) % (2 * sh + 7) - sh - 3).astype(np.int32)
+        hints[rng.random(len(pairs)) < 0.5] = 0
+        _same(batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, diag_hints=hints),
+              oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, diag_hints=hints))
+
+
+@pytest.mark.parametrize("bw", [16, 64, 128])
+def test_wave_kernel_heavy_tailed_lengths(ck, bw):
+    """Pareto lengths to 8000: long pairs take the warp-per-pair kernel in a
+    large call, the rest the strip kernel."""
+    s = synth.generate_families(300, 4, median=0, lo=30, hi=8000, seed=bw, length_dist="pareto")
+    pairs = synth.mixed_pairs(s, 30000, seed=bw, min_ratio=0.5)
+    with wave_config(0, 512):
+        r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
+        c = ck.sw_counters()
+        _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+    assert 0 < c["wave"] < c["batched"]
+
+
+def test_wave_kernel_search_shapes(ck):
+    """One query against a few hundred targets at the search band width."""
+    s = synth.generate_families(60, 8, median=350, lo=30, hi=2000, seed=5)
+    rng = np.random.default_rng(1)
+    pairs = np.stack([np.full(450, 3, np.int32), rng.integers(0, s.n, 450).astype(np.int32)], 1)
+    r = batch_sw(pairs, s.flat, s.offsets, s.lengths, 238, BLOSUM62)
+    c = ck.sw_counters()
+    _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, 238, BLOSUM62))
+    assert c["wave"] == c["batched"] == len(pairs)
 
 
 def test_engines_agree_and_counters(ck):
