@@ -514,9 +514,12 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             const int32_t j = T - s + c0;
             int32_t hin = __shfl_sync(0xffffffffu, hout, (lane + 31) & 31);
             int32_t ein = __shfl_sync(0xffffffffu, eout, (lane + 31) & 31);
-            if (s == 0 || j > s * R + h + w) { hin = 0; ein = NEG_E; }
-            const int32_t hdiag = hprev;
+            // H(row above, j - 1) arrived the step before; both it and this
+            // step's values are judged against the strip held now
+            const int32_t top = s * R + h + w;  // last in-band column of the row above
+            const int32_t hdiag = (s == 0 || j - 1 > top) ? 0 : hprev;
             hprev = hin;
+            if (s == 0 || j > top) { hin = 0; ein = NEG_E; }
             int32_t cm = 0;
             if (j >= J0 && j <= J1) {
                 const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
