@@ -478,6 +478,7 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     if (key == CK_CFG_STRIP_VARIANT) return sw_set_variant(value);
     if (key == CK_CFG_WAVE_MIN_ROWS) return sw_set_wave(0, value);
     if (key == CK_CFG_WAVE_ALL_BELOW) return sw_set_wave(1, value);
+    if (key == CK_CFG_WAVE_ADAPTIVE) return sw_set_wave(2, value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -489,6 +490,7 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (key == CK_CFG_STRIP_VARIANT) { *value = sw_variant(); return CK_OK; }
     if (key == CK_CFG_WAVE_MIN_ROWS) { *value = sw_wave(0); return CK_OK; }
     if (key == CK_CFG_WAVE_ALL_BELOW) { *value = sw_wave(1); return CK_OK; }
+    if (key == CK_CFG_WAVE_ADAPTIVE) { *value = sw_wave(2); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

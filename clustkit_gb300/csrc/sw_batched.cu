@@ -145,7 +145,7 @@ __host__ __device__ inline int32_t wave_rows_per_strip(int32_t la, int32_t w) {
 __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restrict__ seq_ok,
                                uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
                                int32_t *__restrict__ fallback, int32_t *__restrict__ counters,
-                               unsigned long long *__restrict__ cells, int32_t wave_min_rows,
+                               unsigned long long *__restrict__ cells, int32_t wave_all,
                                int32_t *err) {
     // counters[0] = eligible, counters[1] = fallback count, counters[6] = wave pairs
     int64_t local_cells = 0;
@@ -164,7 +164,7 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
                 seq_codes_ok(in, g.b_idx, seq_ok)) {
                 int32_t cb = g.lb < key::ROWS_MAX ? g.lb : key::ROWS_MAX;
                 k = ((uint32_t)g.la << 13) | (uint32_t)cb;
-                if (g.la >= wave_min_rows && wave_rows_per_strip(g.la, g.w) > 0) {
+                if (wave_all && wave_rows_per_strip(g.la, g.w) > 0) {
                     k |= 1u << 26;  // warp-per-pair kernel; sorts ahead of the strip pairs
                     wave++;
                 }
@@ -187,6 +187,34 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
         if (elig) atomicAdd(&counters[0], elig);
         if (wave) atomicAdd(&counters[6], wave);
     }
+}
+
+// Long pairs of a large call: after the sort (rows descending) the leading
+// pairs whose one-lane time would exceed half the strip kernel's expected
+// run time go to the warp-per-pair kernel.  A pair of `rows` rows costs one
+// lane about rows * (2w + 1) cell steps; the whole call about
+// cells / lanes steps per lane.  Pairs at or above max(min_rows, that
+// bound) are counted by a binary search over the sorted keys.
+__global__ void wave_split_kernel(const uint32_t *__restrict__ sorted_keys, int32_t *counters,
+                                  int32_t band_width, int32_t min_rows, int32_t adaptive,
+                                  int64_t lanes) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int32_t n_elig = counters[0];
+    unsigned long long cells = 0;
+    memcpy(&cells, counters + 4, sizeof(cells));
+    int64_t rows_thr = min_rows;
+    if (adaptive) {
+        const int64_t per_lane = (int64_t)(cells / (unsigned long long)(lanes > 0 ? lanes : 1));
+        const int64_t r = (per_lane / 2) / (2 * (int64_t)band_width + 1) + 1;
+        if (r > rows_thr) rows_thr = r;
+    }
+    // keys are (rows << 13 | cols), descending: count the prefix with rows >= rows_thr
+    int32_t lo = 0, hi = n_elig;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if ((int64_t)(sorted_keys[mid] >> 13) >= rows_thr) lo = mid + 1; else hi = mid;
+    }
+    counters[6] = lo;
 }
 
 // ----------------------------------------------------------------- strip kernel
@@ -606,20 +634,25 @@ static int32_t pow2_at_least(int64_t x) {
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
 static int32_t g_rows_per_strip = 16;
 static int32_t g_variant = 1;
-// pairs with at least this many rows go to the warp-per-pair kernel ...
-static int32_t g_wave_min_rows = 1024;
-// ... and every pair does when a call has at most this many pairs
+// every pair runs one warp per pair when a call has at most this many pairs;
+// in larger calls, long pairs do: rows >= max(min rows, the adaptive bound)
 static int32_t g_wave_all_below = 24576;
+static int32_t g_wave_min_rows = 256;
+static int32_t g_wave_adaptive = 1;
 
 int32_t sw_set_wave(int32_t key, int32_t v) {
     if (v < 0) {
-        set_error(CK_ERR_INVALID_ARGUMENT, "warp-per-pair thresholds must be >= 0");
+        set_error(CK_ERR_INVALID_ARGUMENT, "warp-per-pair settings must be >= 0");
         return CK_ERR_INVALID_ARGUMENT;
     }
-    if (key == 0) g_wave_min_rows = v; else g_wave_all_below = v;
+    if (key == 0) g_wave_min_rows = v;
+    else if (key == 1) g_wave_all_below = v;
+    else g_wave_adaptive = v ? 1 : 0;
     return CK_OK;
 }
-int32_t sw_wave(int32_t key) { return key == 0 ? g_wave_min_rows : g_wave_all_below; }
+int32_t sw_wave(int32_t key) {
+    return key == 0 ? g_wave_min_rows : key == 1 ? g_wave_all_below : g_wave_adaptive;
+}
 
 int32_t sw_set_variant(int32_t v) {
     if (v < 0 || v > 3) {
@@ -737,8 +770,9 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
     if (M > 0) {
         int64_t want = (M + 255) / 256;
         int blocks = (int)(want < 16 * (int64_t)sm_count() ? want : 16 * (int64_t)sm_count());
-        const int32_t wave_rows = M <= (int64_t)g_wave_all_below ? 0 : g_wave_min_rows;
-        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, wave_rows, d_err);
+        const bool wave_all = M <= (int64_t)g_wave_all_below;
+        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, wave_all ? 1 : 0,
+                                               d_err);
         CK_CUDA(cudaGetLastError());
         cub::DoubleBuffer<uint32_t> dk(k0, k1), dv(v0, v1);
         size_t temp = 0;
@@ -749,6 +783,15 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
         int32_t wmax = 0;
         CK_TRY(widest_band(in, st, &wmax));
         const uint32_t *order = dv.Current();
+        // long pairs of a large call: only with one band width for every long
+        // pair (clustkit widens the band to the longer length when it is <= 0)
+        // that the warp-per-pair kernel can take at any length
+        if (!wave_all && in.band_width > 0 && wave_rows_per_strip(1 << 13, in.band_width) > 0 &&
+            g_wave_min_rows < (1 << 13)) {
+            wave_split_kernel<<<1, 32, 0, st>>>(dk.Current(), cnt, in.band_width, g_wave_min_rows,
+                                                g_wave_adaptive, (int64_t)sm_count() * 2 * STRIP_THREADS);
+            CK_CUDA(cudaGetLastError());
+        }
         // profiling events bracket the two alignment kernels (wave, then strip)
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));

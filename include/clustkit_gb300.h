@@ -160,15 +160,20 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_STRIP_VARIANT   0..3: bit 0 prefetches the next columns' inputs two
  *                          columns ahead (else one), bit 1 runs interior
  *                          columns four at a time (else two)
- *   CK_CFG_WAVE_MIN_ROWS   pairs with at least this many rows (shorter side)
- *                          run one warp per pair instead of one lane per pair
- *                          (default 1024)
  *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs run every pair
- *                          one warp per pair (default 24576) */
+ *                          one warp per pair (default 24576)
+ *   CK_CFG_WAVE_MIN_ROWS   in larger calls with band_width > 0, pairs with at
+ *                          least this many rows (shorter side) run one warp
+ *                          per pair instead of one lane per pair (default 256)
+ *   CK_CFG_WAVE_ADAPTIVE   1 (default): raise that row bound to where a pair's
+ *                          one-lane time would pass half the call's expected
+ *                          strip-kernel time, from the call's cell count; 0:
+ *                          use CK_CFG_WAVE_MIN_ROWS as given */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
 #define CK_CFG_WAVE_ALL_BELOW 3
+#define CK_CFG_WAVE_ADAPTIVE 4
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

@@ -66,7 +66,7 @@ def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist, route):
                                 length_dist=dist)
     pairs = synth.mixed_pairs(s, 4000, seed=bw, min_ratio=0.0)
     ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
-    with wave_config(*((0, 1 << 30) if route == "strip" else (24576, 1024))):
+    with wave_config(*((0, 1 << 30) if route == "strip" else (24576, 256, 1))):
         r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, 0.3, engine=engine)
     _same(r, ref)
     assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
@@ -98,17 +98,19 @@ def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
 
 
 @contextlib.contextmanager
-def wave_config(all_below, min_rows):
+def wave_config(all_below, min_rows, adaptive=0):
     """Route pairs between the warp-per-pair and the lane-per-pair kernels."""
-    from clustkit_gb300._lib import CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, get_config, set_config
-    keep = (get_config(CFG_WAVE_ALL_BELOW), get_config(CFG_WAVE_MIN_ROWS))
-    set_config(CFG_WAVE_ALL_BELOW, all_below)
-    set_config(CFG_WAVE_MIN_ROWS, min_rows)
+    from clustkit_gb300._lib import (CFG_WAVE_ADAPTIVE, CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, get_config,
+                                     set_config)
+    keys = (CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_ADAPTIVE)
+    keep = [get_config(k) for k in keys]
+    for k, v in zip(keys, (all_below, min_rows, adaptive)):
+        set_config(k, v)
     try:
         yield
     finally:
-        set_config(CFG_WAVE_ALL_BELOW, keep[0])
-        set_config(CFG_WAVE_MIN_ROWS, keep[1])
+        for k, v in zip(keys, keep):
+            set_config(k, v)
 
 
 # every pair on the warp-per-pair kernel; a split at 64 rows; only long pairs
@@ -141,10 +143,18 @@ def test_wave_kernel_heavy_tailed_lengths(ck, bw):
     large call, the rest the strip kernel."""
     s = synth.generate_families(300, 4, median=0, lo=30, hi=8000, seed=bw, length_dist="pareto")
     pairs = synth.mixed_pairs(s, 30000, seed=bw, min_ratio=0.5)
+    ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
     with wave_config(0, 512):
         r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
         c = ck.sw_counters()
-        _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+    _same(r, ref)
+    assert 0 < c["wave"] < c["batched"]
+    # the adaptive split sends at least the pairs whose one-lane time would
+    # dominate the call (here the longest ones)
+    with wave_config(0, 256, 1):
+        r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
+        c = ck.sw_counters()
+    _same(r, ref)
     assert 0 < c["wave"] < c["batched"]
 
 
