@@ -190,11 +190,12 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
 }
 
 // Long pairs of a large call: after the sort (rows descending) the leading
-// pairs whose one-lane time would exceed half the strip kernel's expected
-// run time go to the warp-per-pair kernel.  A pair of `rows` rows costs one
-// lane about rows * (2w + 1) cell steps; the whole call about
-// cells / lanes steps per lane.  Pairs at or above max(min_rows, that
-// bound) are counted by a binary search over the sorted keys.
+// pairs whose one-lane time would exceed the call's expected run time go
+// one warp per pair.  A pair of `rows` rows costs one lane about
+// rows * (2w + 1) cell steps; the whole call about cells / lanes steps per
+// lane (the longest pairs start first, so a pair below that bound does not
+// set the tail).  Pairs at or above max(min_rows, that bound) are counted by
+// a binary search over the sorted keys.
 __global__ void wave_split_kernel(const uint32_t *__restrict__ sorted_keys, int32_t *counters,
                                   int32_t band_width, int32_t min_rows, int32_t adaptive,
                                   int64_t lanes) {
@@ -205,7 +206,7 @@ __global__ void wave_split_kernel(const uint32_t *__restrict__ sorted_keys, int3
     int64_t rows_thr = min_rows;
     if (adaptive) {
         const int64_t per_lane = (int64_t)(cells / (unsigned long long)(lanes > 0 ? lanes : 1));
-        const int64_t r = (per_lane / 2) / (2 * (int64_t)band_width + 1) + 1;
+        const int64_t r = per_lane / (2 * (int64_t)band_width + 1) + 1;
         if (r > rows_thr) rows_thr = r;
     }
     // keys are (rows << 13 | cols), descending: count the prefix with rows >= rows_thr
@@ -261,9 +262,14 @@ __device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &h
         if (!MASKED || ((r < alive) && ((uint32_t)(j - r - lo0) <= w2))) {
             const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
             const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
-            const int32_t eT = __viaddmax_s32(eu, EXT, fadd(hu, OPEN_E, one)) | TBIT;
+            // E's extension term comes from E of the row above, known before
+            // that row's H: only H_up + OPEN_E and the max-of-three sit on the
+            // row-to-row dependency chain.  E's tie bit plays no part in H
+            // (E, F, diag and zero differ in priority), so it is set off the chain.
+            const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, EXT, one));
             const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
-            const int32_t hn = __vimax3_s32(diagc, eT, fTn) & CLEAN;
+            const int32_t hn = __vimax3_s32(diagc, eR, fTn) & CLEAN;
+            const int32_t eT = eR | TBIT;
             hdiag = S.hc[r];
             S.hc[r] = hn;
             S.fT[r] = fTn;
@@ -413,31 +419,50 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
     write_result(out, in, p, score, gbest & MATCH_MASK, la, la, lb);
 }
 
+// increment table + per-row first-max trackers (16 rows for the warp-per-pair phase)
 template <int R>
 __host__ __device__ constexpr size_t strip_smem() {
-    return INC_SMEM + (size_t)R * STRIP_THREADS * sizeof(int32_t);
+    return INC_SMEM + (size_t)(R > 16 ? R : 16) * STRIP_THREADS * sizeof(int32_t);
 }
 
+__device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &out, int64_t p,
+                                                 const char *s_inc, int32_t *s_best, int32_t lane,
+                                                 int32_t *fallback, int32_t *fallback_count,
+                                                 int32_t *err, int32_t one);
+
+// Persistent alignment kernel.  Its warps first take the leading
+// counters[6] sorted pairs one warp per pair (long pairs, or every pair of a
+// small call), then the rest 32 pairs per warp, one lane per pair, in
+// register strips of R rows.  Long pairs thus start first and the lane-per-
+// pair groups fill in around them.
 template <int R, int V>
 __global__ void __launch_bounds__(STRIP_THREADS, 2)
 sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
-                int32_t *__restrict__ fallback, int32_t *__restrict__ fallback_count,
-                int32_t *err, int32_t one) {
+                int32_t *__restrict__ wave_ticket, int32_t *__restrict__ fallback,
+                int32_t *__restrict__ fallback_count, int32_t *err, int32_t one) {
     extern __shared__ int32_t s_inc[];
-    if (counters[0] <= counters[6]) return;  // every pair went to the warp-per-pair kernel
+    if (counters[0] <= 0) return;
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
     __syncthreads();
     int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
     const int32_t lane = threadIdx.x & 31;
+    const int32_t n_wave = counters[6];
+    for (;;) {
+        __syncwarp();
+        int32_t q = 0;
+        if (lane == 0) q = atomicAdd(wave_ticket, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n_wave) break;
+        align_pair_wave_any(in, out, (int64_t)order[q], (const char *)s_inc, s_best, lane, fallback,
+                            fallback_count, err, one);
+    }
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int2 *win = window + (size_t)gwarp * (size_t)W * 32 + lane;
-    // the first counters[6] sorted pairs belong to the warp-per-pair kernel
-    const int32_t n_skip = counters[6];
-    const int32_t n_elig = counters[0] - n_skip;
+    const int32_t n_elig = counters[0] - n_wave;
     const int32_t n_groups = (n_elig + 31) >> 5;
-    order += n_skip;
+    order += n_wave;
     for (;;) {
         __syncwarp();
         int32_t grp = 0;
@@ -590,37 +615,16 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
     write_result(out, in, p, best, best > 0 ? (lbest & MATCH_MASK) : 0, la, la, lb);
 }
 
-__global__ void __launch_bounds__(STRIP_THREADS, 2)
-sw_wave_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
-               const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
-               int32_t *__restrict__ ticket, int32_t *__restrict__ fallback,
-               int32_t *__restrict__ fallback_count, int32_t *err, int32_t one) {
-    extern __shared__ int32_t s_inc[];
-    const int32_t n_wave = counters[6];
-    if (n_wave <= 0) return;
-    for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
-    __syncthreads();
-    int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
-    const int32_t lane = threadIdx.x & 31;
-    for (;;) {
-        __syncwarp();
-        int32_t q = 0;
-        if (lane == 0) q = atomicAdd(ticket, 1);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= n_wave) break;
-        const int64_t p = (int64_t)order[q];
-        const PairGeom g = pair_geometry(in, p, err);
-        switch (wave_rows_per_strip(g.la, g.w)) {
-            case 4:
-                align_pair_wave<4>(in, out, p, g, (const char *)s_inc, s_best, lane, fallback, fallback_count, one);
-                break;
-            case 8:
-                align_pair_wave<8>(in, out, p, g, (const char *)s_inc, s_best, lane, fallback, fallback_count, one);
-                break;
-            default:
-                align_pair_wave<16>(in, out, p, g, (const char *)s_inc, s_best, lane, fallback, fallback_count, one);
-                break;
-        }
+// One sorted wave pair, at the rows per strip its shape allows.
+__device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &out, int64_t p,
+                                                 const char *s_inc, int32_t *s_best, int32_t lane,
+                                                 int32_t *fallback, int32_t *fallback_count,
+                                                 int32_t *err, int32_t one) {
+    const PairGeom g = pair_geometry(in, p, err);
+    switch (wave_rows_per_strip(g.la, g.w)) {
+        case 4: align_pair_wave<4>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
+        case 8: align_pair_wave<8>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
+        default: align_pair_wave<16>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
     }
 }
 
@@ -664,22 +668,6 @@ int32_t sw_set_variant(int32_t v) {
 }
 int32_t sw_variant() { return g_variant; }
 
-static int32_t launch_wave(const SwIn &in, const SwOut &out, const uint32_t *order,
-                           const int32_t *counters, const int32_t *inc, int32_t *ticket,
-                           int32_t *fallback, int32_t *fb_count, int32_t *err, cudaStream_t st,
-                           SwCounters *ctr) {
-    const size_t smem = strip_smem<16>();
-    CK_CUDA(cudaFuncSetAttribute(sw_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw_wave_kernel, STRIP_THREADS, smem));
-    if (per_sm < 1) per_sm = 1;
-    sw_wave_kernel<<<sm_count() * per_sm, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, ticket,
-                                                                     fallback, fb_count, err, 1);
-    CK_CUDA(cudaGetLastError());
-    if (ctr) ctr->launches += 1;
-    return CK_OK;
-}
-
 template <int R>
 static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
                                const int32_t *counters, const int32_t *inc, int32_t wmax,
@@ -718,7 +706,7 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     int2 *window = (int2 *)scratch(SLOT_WINDOW, (size_t)blocks * per_block, &status);
     if (!window) return status;
     kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
-                                              fallback, fb_count, err, 1);
+                                              ticket + 5, fallback, fb_count, err, 1);
     CK_CUDA(cudaGetLastError());
     if (ctr) ctr->launches += 1;
     return CK_OK;
@@ -792,10 +780,9 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
                                                 g_wave_adaptive, (int64_t)sm_count() * 2 * STRIP_THREADS);
             CK_CUDA(cudaGetLastError());
         }
-        // profiling events bracket the two alignment kernels (wave, then strip)
+        // profiling events bracket the alignment kernel
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
-        CK_TRY(launch_wave(in, out, order, cnt, inc, cnt + 7, fb, cnt + 1, d_err, st, ctr));
         switch (g_rows_per_strip) {
             case 8:
                 CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));

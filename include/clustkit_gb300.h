@@ -166,8 +166,8 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *                          least this many rows (shorter side) run one warp
  *                          per pair instead of one lane per pair (default 256)
  *   CK_CFG_WAVE_ADAPTIVE   1 (default): raise that row bound to where a pair's
- *                          one-lane time would pass half the call's expected
- *                          strip-kernel time, from the call's cell count; 0:
+ *                          one-lane time would pass the call's expected
+ *                          kernel time, from the call's cell count; 0:
  *                          use CK_CFG_WAVE_MIN_ROWS as given */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
