@@ -494,14 +494,18 @@ def run_search(args, n_db_fam=50000):
     plain_qps = n_plain / (time.perf_counter() - tp0)
     # device time per stage of a one-query batch (separate pass: events add syncs)
     slot.enable_stage_timing()
-    stages = []
+    stages, cells1 = [], []
     for q in qs[:50]:
         search_batch(db, [q], top_k=10, slot=slot)
         stages.append(slot.stage_ms())
-    full = []
+        cells1.append(slot.last_cells())
+    full, cells64 = [], []
     for r in range(5):
         search_batch(db, qs[64 * r:64 * (r + 1)], top_k=10, slot=slot)
         full.append(slot.stage_ms())
+        cells64.append(slot.last_cells())
+    sw1 = np.array([x[2] for x in stages])
+    sw64 = np.array([x[2] for x in full])
     slot.close()
     full_med = np.median(np.array(full), axis=0)
     st_med = np.median(np.array(stages), axis=0)
@@ -510,7 +514,10 @@ def run_search(args, n_db_fam=50000):
              "device_stage_ms_median": {"h2d": float(st_med[0]), "phase_a": float(st_med[1]),
                                         "sw": float(st_med[2]), "d2h": float(st_med[3])},
              "device_stage_ms_median_batch64": {"h2d": float(full_med[0]), "phase_a": float(full_med[1]),
-                                                "sw": float(full_med[2]), "d2h": float(full_med[3])}}
+                                                "sw": float(full_med[2]), "d2h": float(full_med[3])},
+             "sw_gcups_one_query": float(np.sum(cells1) / np.sum(sw1) / 1e6),
+             "sw_gcups_batch64": float(np.sum(cells64) / np.sum(sw64) / 1e6),
+             "cells_per_query": float(np.mean(cells1))}
     server = SearchServer(db, top_k=10, max_cands=500).start()
     sweep = []
     rng = np.random.default_rng(3)

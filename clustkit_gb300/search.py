@@ -187,6 +187,20 @@ class _Slot:
         torch = _torch()
         self.stage_events = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
 
+    def last_cells(self) -> int:
+        """Banded DP cells of the last batch's query/candidate pairs (after its event)."""
+        from .cells import band_cells, effective_band
+        nq, lens = self.batch if self.batch is not None else self._last_batch
+        K = self.max_cands
+        n = self.h_n.numpy()[:nq]
+        tg = self.h_targets.numpy()[: nq * K].reshape(nq, K)
+        keep = np.arange(K)[None, :] < n[:, None]
+        qi, ci = np.nonzero(keep)
+        ql = lens[qi].astype(np.int64)
+        tl = self.db.lengths_host[tg[qi, ci]].astype(np.int64)
+        la, lb = np.minimum(ql, tl), np.maximum(ql, tl)
+        return int(band_cells(la, lb, effective_band(la, lb, self.db.band_width)).sum())
+
     def stage_ms(self):
         """(h2d, phase_a, sw, d2h) milliseconds of the last batch (after its event)."""
         ev = self.stage_events
@@ -283,6 +297,7 @@ class _Slot:
         for q in range(nq):
             sel = order[first[q]:min(first[q + 1], first[q] + top_k)]
             out.append([SearchHit(q, int(t[o]), float(si[o]), int(sc[o]), float(rank[o])) for o in sel])
+        self._last_batch = self.batch
         self.batch = None
         return out
 
