@@ -430,6 +430,11 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if rank == 0 and (args.uneven == "on" or (args.uneven == "auto" and not args.quick)):
+        try:
+            line["uneven"] = run_uneven(args)
+        except Exception as e:  # the SW line stands; the failure is reported in it
+            line["uneven"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and (args.search == "on" or (args.search == "auto" and not args.quick)):
         try:
             line["search"] = run_search(args)
@@ -440,6 +445,39 @@ def run_ours(args, world, rank, local):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- uneven lengths / autotuner
+def run_uneven(args):
+    """Heavy-tailed lengths (Pareto alpha 1.5, 30..8000), 2M pairs (half within
+    family, half random, length ratio >= 0.5); per band width the default
+    setting, the autotuned one and the plain kernel, all pairs compared."""
+    from clustkit_gb300 import _lib, synth, tune
+    n_fam, n_pairs = (200, 200_000) if args.quick else (2000, 2_000_000)
+    s = synth.generate_families(n_fam, 10, median=0, lo=30, hi=8000, seed=17, length_dist="pareto")
+    pairs = synth.mixed_pairs(s, n_pairs, seed=5, within_frac=0.5, min_ratio=0.5)
+    out = {"workload": f"uneven: {s.n} seqs Pareto(1.5) 30..8000, {len(pairs)} pairs (50% within family, "
+                       f"ratio >= 0.5)", "by_band": {}}
+    for bw in (16, 32, 64, 128):
+        call = tune._DeviceCall(pairs, s.flat, s.offsets, s.lengths, bw)
+        tune.apply(tune.DEFAULT)
+        ms_default = call.time_ms(3)
+        res = tune.autotune(pairs, s.flat, s.offsets, s.lengths, bw, use_cache=False)
+        ms_tuned = call.time_ms(3)
+        tuned = call.results()
+        wave = _lib.sw_counters()["wave"]
+        ms_plain = call.time_ms(1, warmup=0, engine=1)
+        plain = call.results()
+        tune.apply(tune.DEFAULT)
+        same = all(np.array_equal(tuned[k], plain[k]) for k in ("scores", "matches", "shorter", "mask"))
+        g = lambda ms: res.cells / (ms * 1e-3) / 1e9
+        out["by_band"][str(bw)] = {"cells": res.cells, "gcups_default": g(ms_default), "gcups_tuned": g(ms_tuned),
+                                   "gcups_plain": g(ms_plain), "tuned_vs_plain": ms_plain / ms_tuned,
+                                   "config": res.config, "wave_pairs": wave, "trials": len(res.trials),
+                                   "bit_exact_vs_plain": bool(same)}
+        log(f"uneven bw={bw}: {out['by_band'][str(bw)]}")
+        del call
+    return out
 
 
 # ----------------------------------------------------------------------------- search / serving
@@ -563,10 +601,20 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
     ap.add_argument("--search", choices=["auto", "on", "off", "only"], default="auto",
                     help="search/serving leg (auto: on for the full workload, off with --quick)")
+    ap.add_argument("--uneven", choices=["auto", "on", "off", "only"], default="auto",
+                    help="heavy-tailed lengths + autotuner leg (auto: on for the full workload)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.uneven == "only":
+        import torch
+        from clustkit_gb300 import _lib
+        torch.cuda.set_device(local)
+        _lib.load()
+        _lib.require_gpu()
+        print(json.dumps({"metric": "banded-SW GCUPS, heavy-tailed lengths, autotuned vs default vs plain",
+                          "uneven": run_uneven(args)}), flush=True)
     elif args.search == "only":
         import torch
         from clustkit_gb300 import _lib

@@ -1,0 +1,174 @@
+"""Autotuner for the batched Smith-Waterman engine.
+
+The batched engine (csrc/sw_batched.cu) has three kinds of tunables, the
+GB300 counterparts of "bin edges, band tiling and CTA shape":
+
+* bin edge -- which pairs run one warp per pair instead of one lane per pair:
+  every pair of a call with at most ``wave_all_below`` pairs, and in larger
+  calls the pairs with at least ``wave_min_rows`` rows, raised (when
+  ``wave_adaptive``) to where a pair's one-lane time would pass the call's
+  expected time;
+* band tiling -- rows a lane keeps in registers per strip (8, 16, 24);
+* strip variant -- prefetch distance (1 or 2 columns) and interior unroll
+  (2 or 4 columns), i.e. the shape of a lane's inner loop.
+
+``autotune`` times candidates on the caller's own pairs (device-resident,
+CUDA events around the whole call, L2 flushed between runs) by coordinate
+descent -- bin edge, then tiling x variant, then the bin edge again -- and
+returns the fastest setting with the table of every trial.  Settings are
+process-wide (``apply``); every setting gives identical results, only the
+time changes.  Results are cached per (band width, length profile).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .blosum import BLOSUM62
+from .cells import band_cells, effective_band
+
+KEYS = {
+    "rows_per_strip": _lib.CFG_ROWS_PER_STRIP,
+    "strip_variant": _lib.CFG_STRIP_VARIANT,
+    "wave_min_rows": _lib.CFG_WAVE_MIN_ROWS,
+    "wave_all_below": _lib.CFG_WAVE_ALL_BELOW,
+    "wave_adaptive": _lib.CFG_WAVE_ADAPTIVE,
+}
+
+DEFAULT = {"rows_per_strip": 16, "strip_variant": 1, "wave_min_rows": 256, "wave_all_below": 24576,
+           "wave_adaptive": 1}
+
+# bin-edge candidates: (wave_min_rows, wave_adaptive); 1 << 30 = never by length
+BIN_EDGES = [(256, 1), (512, 0), (1024, 0), (2048, 0), (4096, 0), (1 << 30, 0)]
+TILINGS = [(r, v) for r in (8, 16, 24) for v in (0, 1, 2, 3)]
+
+_cache: dict = {}
+
+
+def current() -> dict:
+    return {k: _lib.get_config(v) for k, v in KEYS.items()}
+
+
+def apply(config: dict) -> None:
+    for k, v in config.items():
+        _lib.set_config(KEYS[k], int(v))
+
+
+@dataclass
+class TuneResult:
+    config: dict
+    ms: float
+    gcups: float
+    cells: int
+    trials: list = field(default_factory=list)  # (config, ms)
+
+
+class _DeviceCall:
+    """One pair set resident on the device, timed through ck_sw_batch_device."""
+
+    def __init__(self, pairs, flat, offsets, lengths, band_width):
+        import torch
+        self.torch = torch
+        self.lib = _lib.load()
+        _lib.require_gpu()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        self.pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        self.M = int(self.pairs.shape[0])
+        self.d_pairs, self.d_flat = T(self.pairs), T(np.asarray(flat, np.uint8))
+        self.d_off, self.d_len = T(np.asarray(offsets, np.int64)), T(np.asarray(lengths, np.int32))
+        self.n = int(len(lengths))
+        self.flat_len = int(len(flat))
+        self.bw = int(band_width)
+        self.sub = np.ascontiguousarray(BLOSUM62)
+        self.out = [torch.empty(self.M, dtype=dt, device=dev) for dt in
+                    (torch.float32, torch.int32, torch.int32, torch.int32, torch.uint8)]
+        self.stream = torch.cuda.current_stream(dev)
+        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def run(self, engine=0):
+        o = self.out
+        _lib.check(self.lib.ck_sw_batch_device(
+            self.d_pairs.data_ptr(), self.M, self.d_flat.data_ptr(), self.flat_len, self.d_off.data_ptr(),
+            self.d_len.data_ptr(), self.n, self.bw, self.sub.ctypes.data, 0.0, None, _lib.PASS_SCORE, engine,
+            o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), o[3].data_ptr(), o[4].data_ptr(),
+            self.stream.cuda_stream))
+
+    def time_ms(self, repeats=2, warmup=1, engine=0) -> float:
+        torch = self.torch
+        for _ in range(warmup):
+            self.run(engine)
+        best = float("inf")
+        for k in range(repeats):
+            self.flush.fill_(k & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(self.stream)
+            self.run(engine)
+            b.record(self.stream)
+            b.synchronize()
+            best = min(best, a.elapsed_time(b))
+        _lib.check(self.lib.ck_sw_status_device(self.stream.cuda_stream))
+        return best
+
+    def results(self):
+        return {k: t.cpu().numpy() for k, t in zip(("sims", "scores", "matches", "shorter", "mask"), self.out)}
+
+
+def profile_key(lengths, pairs, band_width):
+    """Cache key: band width and the log2 buckets of the rows' 50/90/99/99.9 percentiles."""
+    L = np.asarray(lengths)
+    p = np.asarray(pairs).reshape(-1, 2)
+    rows = np.minimum(L[p[:, 0]], L[p[:, 1]]) if len(p) else np.zeros(1)
+    q = np.percentile(rows, [50, 90, 99, 99.9]) if len(p) else np.zeros(4)
+    return (int(band_width), tuple(int(np.log2(max(x, 1))) for x in q), int(np.log2(max(len(p), 1))))
+
+
+def autotune(pairs, flat, offsets, lengths, band_width: int, repeats: int = 2,
+             use_cache: bool = True, apply_best: bool = True) -> TuneResult:
+    """Time the engine's settings on these pairs and return (and apply) the fastest."""
+    key = profile_key(lengths, pairs, band_width)
+    if use_cache and key in _cache:
+        res = _cache[key]
+        if apply_best:
+            apply(res.config)
+        return res
+    call = _DeviceCall(pairs, flat, offsets, lengths, band_width)
+    L = np.asarray(lengths, np.int64)
+    p = call.pairs
+    la = np.minimum(L[p[:, 0]], L[p[:, 1]])
+    lb = np.maximum(L[p[:, 0]], L[p[:, 1]])
+    cells = int(band_cells(la, lb, effective_band(la, lb, band_width)).sum())
+    keep = current()
+    trials = []
+    best = dict(keep)
+    best_ms = None
+
+    def trial(cfg):
+        nonlocal best, best_ms
+        apply(cfg)
+        ms = call.time_ms(repeats)
+        trials.append((dict(cfg), ms))
+        if best_ms is None or ms < best_ms:
+            best, best_ms = dict(cfg), ms
+
+    try:
+        base = dict(DEFAULT)
+        for mr, ad in BIN_EDGES:
+            trial({**base, "wave_min_rows": mr, "wave_adaptive": ad})
+        edge = {k: best[k] for k in ("wave_min_rows", "wave_adaptive")}
+        for r, v in TILINGS:
+            trial({**base, **edge, "rows_per_strip": r, "strip_variant": v})
+        tiling = {k: best[k] for k in ("rows_per_strip", "strip_variant")}
+        for mr, ad in BIN_EDGES:
+            cfg = {**base, **tiling, "wave_min_rows": mr, "wave_adaptive": ad}
+            if not any(c == cfg for c, _ in trials):
+                trial(cfg)
+    finally:
+        apply(keep)
+    res = TuneResult(best, best_ms, cells / (best_ms * 1e-3) / 1e9 if best_ms else 0.0, cells, trials)
+    _cache[key] = res
+    if apply_best:
+        apply(best)
+    return res

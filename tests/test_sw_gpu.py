@@ -318,3 +318,23 @@ def test_device_pointer_entry_point(ck):
         assert np.array_equal(d_scores.cpu().numpy(), ref["scores"])
         assert np.array_equal(d_matches.cpu().numpy(), ref["matches"])
         assert np.array_equal(d_sims.cpu().numpy(), ref["sims"])
+
+
+def test_autotuner_settings_agree(ck):
+    """Every setting the autotuner tries gives the same results; it picks one of them."""
+    from clustkit_gb300 import tune
+    s = synth.generate_families(60, 10, median=0, lo=30, hi=4000, seed=8, length_dist="pareto")
+    pairs = synth.mixed_pairs(s, 40000, seed=3, min_ratio=0.5)
+    keep = tune.current()
+    try:
+        res = tune.autotune(pairs, s.flat, s.offsets, s.lengths, 64, repeats=1, use_cache=False,
+                            apply_best=False)
+        assert res.config in [c for c, _ in res.trials] and res.ms > 0 and res.cells > 0
+        call = tune._DeviceCall(pairs, s.flat, s.offsets, s.lengths, 64)
+        ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, 64, BLOSUM62)
+        for cfg, _ in res.trials[::5] + [(res.config, 0)]:
+            tune.apply(cfg)
+            call.run()
+            _same(call.results(), ref)
+    finally:
+        tune.apply(keep)
