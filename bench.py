@@ -465,6 +465,8 @@ def run_uneven(args):
         res = tune.autotune(pairs, s.flat, s.offsets, s.lengths, bw, use_cache=False)
         ms_tuned = call.time_ms(3)
         tuned = call.results()
+        from clustkit_gb300.pairwise import batch_sw  # host entry point: reads the routing counters
+        batch_sw(pairs, s.flat, s.offsets, s.lengths, bw)
         wave = _lib.sw_counters()["wave"]
         ms_plain = call.time_ms(1, warmup=0, engine=1)
         plain = call.results()

@@ -29,6 +29,7 @@ struct ScratchSet {
     void *buf[SLOT_COUNT] = {};
     size_t cap[SLOT_COUNT] = {};
     int32_t *err = nullptr;
+    bool frozen = false;  // buffers may be baked into a captured CUDA graph: never reallocate
 };
 
 struct DeviceState {
@@ -120,6 +121,12 @@ void *scratch(int slot, size_t bytes, int32_t *status) {
     if (!s) return nullptr;
     if (bytes == 0) bytes = 1;
     if (s->cap[slot] < bytes) {
+        if (s->frozen) {
+            set_error(CK_ERR_UNSUPPORTED, "context scratch is frozen (its buffers may be captured in a "
+                                          "CUDA graph) and too small for this call");
+            *status = CK_ERR_UNSUPPORTED;
+            return nullptr;
+        }
         if (s->buf[slot]) {
             cudaError_t e = cudaFree(s->buf[slot]);  // synchronises with work still using it
             s->buf[slot] = nullptr;
@@ -403,6 +410,17 @@ int32_t ck_ctx_create(int32_t *out_handle) {
         if (!g_ctx[i]) { g_ctx[i] = set; *out_handle = (int32_t)i + 1; return CK_OK; }
     g_ctx.push_back(set);
     *out_handle = (int32_t)g_ctx.size();
+    return CK_OK;
+}
+
+int32_t ck_ctx_freeze(int32_t handle, int32_t frozen) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    if (handle < 1 || handle > (int32_t)g_ctx.size() || !g_ctx[handle - 1]) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "unknown context handle");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    g_ctx[handle - 1]->frozen = frozen != 0;
     return CK_OK;
 }
 

@@ -12,7 +12,6 @@
 // counts saturate at 32767 as clustkit's int16 counters do; targets with
 // count >= min_total_hits survive; at most top_k survive per query, chosen by
 // count (ties: lower target id first), returned in target-id order.
-#include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -198,10 +197,8 @@ __global__ void __launch_bounds__(SELECT_THREADS)
 phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits,
                       int32_t top_k, int32_t *__restrict__ out_targets,
                       int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
-    using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
-    __shared__ typename BlockScan::TempStorage scan_tmp;
     __shared__ int32_t hist[256];
-    __shared__ int32_t sh_thr, sh_take_eq, sh_total, sh_run_eq, sh_run_sel;
+    __shared__ int32_t sh_thr, sh_take_eq, sh_total;
     const int32_t q = blockIdx.x;
     const int32_t *c = counts + (int64_t)q * num_db;
     const int tid = threadIdx.x;
@@ -252,27 +249,57 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
         __syncthreads();
     }
     const int32_t thr = sh_thr, take_eq = sh_take_eq;
-    if (tid == 0) { sh_run_eq = 0; sh_run_sel = 0; }
+    // Ordered compaction.  Warp w owns ids [w * chunk, (w + 1) * chunk), read
+    // 32 at a time (coalesced); a first pass counts its strict survivors
+    // (v > thr) and its ties (v == thr), one prefix over the 32 warps gives
+    // each warp its tie rank base and output base, a second pass writes.
+    // Ties are taken in id order, the first take_eq of them.
+    const int warp = tid >> 5, lane = tid & 31;
+    constexpr int NW = SELECT_THREADS / 32;
+    const int32_t chunk = ((num_db + NW - 1) / NW + 31) & ~31;
+    const int32_t b0 = warp * chunk;
+    const int32_t b1 = min(num_db, b0 + chunk);
+    const uint32_t lt = (1u << lane) - 1u;
+    int32_t n_strict = 0, n_eq = 0;
+    for (int32_t base = b0; base < b1; base += 32) {
+        const int32_t t = base + lane;
+        const int32_t v = t < b1 ? val(t) : -1;
+        const bool surv = t < b1 && v >= min_hits;
+        n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v > thr)));
+        n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v == thr));
+    }
+    __shared__ int32_t w_strict[NW], w_eq[NW], w_eq_base[NW], w_out_base[NW];
+    if (lane == 0) { w_strict[warp] = n_strict; w_eq[warp] = n_eq; }
     __syncthreads();
-    for (int32_t base = 0; base < num_db; base += blockDim.x) {
-        const int32_t t = base + tid;
-        const int32_t v = t < num_db ? val(t) : -1;
-        const bool surv = t < num_db && v >= min_hits;
-        const int32_t is_eq = (surv && thr >= 0 && v == thr) ? 1 : 0;
-        int32_t eq_rank, eq_tot;
-        BlockScan(scan_tmp).ExclusiveSum(is_eq, eq_rank, eq_tot);
-        __syncthreads();
-        const bool sel = surv && (thr < 0 || v > thr || (is_eq && sh_run_eq + eq_rank < take_eq));
-        int32_t pos, sel_tot;
-        BlockScan(scan_tmp).ExclusiveSum(sel ? 1 : 0, pos, sel_tot);
+    if (tid == 0) {
+        int32_t eq_acc = 0, out_acc = 0;
+        for (int w = 0; w < NW; ++w) {
+            w_eq_base[w] = eq_acc;
+            w_out_base[w] = out_acc;
+            int32_t take = take_eq - eq_acc;
+            take = take < 0 ? 0 : (take > w_eq[w] ? w_eq[w] : take);
+            eq_acc += w_eq[w];
+            out_acc += w_strict[w] + (thr >= 0 ? take : 0);
+        }
+    }
+    __syncthreads();
+    int32_t eq_seen = w_eq_base[warp], written = w_out_base[warp];
+    for (int32_t base = b0; base < b1; base += 32) {
+        const int32_t t = base + lane;
+        const int32_t v = t < b1 ? val(t) : -1;
+        const bool surv = t < b1 && v >= min_hits;
+        const bool strict = surv && (thr < 0 || v > thr);
+        const bool is_eq = surv && thr >= 0 && v == thr;
+        const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
+        const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
+        const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
         if (sel) {
-            const int64_t o = (int64_t)q * top_k + sh_run_sel + pos;
+            const int64_t o = (int64_t)q * top_k + written + __popc(sel_b & lt);
             out_targets[o] = t;
             if (out_scores) out_scores[o] = v;
         }
-        __syncthreads();
-        if (tid == 0) { sh_run_eq += eq_tot; sh_run_sel += sel_tot; }
-        __syncthreads();
+        eq_seen += __popc(eq_b);
+        written += __popc(sel_b);
     }
     if (tid == 0) out_n[q] = sh_total < top_k ? sh_total : top_k;
 }

@@ -145,11 +145,10 @@ __host__ __device__ inline int32_t wave_rows_per_strip(int32_t la, int32_t w) {
 __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restrict__ seq_ok,
                                uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
                                int32_t *__restrict__ fallback, int32_t *__restrict__ counters,
-                               unsigned long long *__restrict__ cells, int32_t wave_all,
-                               int32_t *err) {
-    // counters[0] = eligible, counters[1] = fallback count, counters[6] = wave pairs
+                               unsigned long long *__restrict__ cells, int32_t *err) {
+    // counters[0] = eligible, counters[1] = fallback count
     int64_t local_cells = 0;
-    int32_t elig = 0, wave = 0;
+    int32_t elig = 0;
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < M;
          p += (int64_t)gridDim.x * blockDim.x) {
         PairGeom g = pair_geometry(in, p, err);
@@ -164,10 +163,6 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
                 seq_codes_ok(in, g.b_idx, seq_ok)) {
                 int32_t cb = g.lb < key::ROWS_MAX ? g.lb : key::ROWS_MAX;
                 k = ((uint32_t)g.la << 13) | (uint32_t)cb;
-                if (wave_all && wave_rows_per_strip(g.la, g.w) > 0) {
-                    k |= 1u << 26;  // warp-per-pair kernel; sorts ahead of the strip pairs
-                    wave++;
-                }
                 elig++;
             } else {
                 int32_t pos = atomicAdd(&counters[1], 1);
@@ -180,27 +175,36 @@ __global__ void sw_prep_kernel(SwIn in, SwOut out, int64_t M, uint8_t *__restric
     for (int o = 16; o; o >>= 1) {
         local_cells += __shfl_xor_sync(0xffffffffu, local_cells, o);
         elig += __shfl_xor_sync(0xffffffffu, elig, o);
-        wave += __shfl_xor_sync(0xffffffffu, wave, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (local_cells) atomicAdd(cells, (unsigned long long)local_cells);
         if (elig) atomicAdd(&counters[0], elig);
-        if (wave) atomicAdd(&counters[6], wave);
     }
 }
 
-// Long pairs of a large call: after the sort (rows descending) the leading
-// pairs whose one-lane time would exceed the call's expected run time go
-// one warp per pair.  A pair of `rows` rows costs one lane about
-// rows * (2w + 1) cell steps; the whole call about cells / lanes steps per
-// lane (the longest pairs start first, so a pair below that bound does not
-// set the tail).  Pairs at or above max(min_rows, that bound) are counted by
-// a binary search over the sorted keys.
+// Which sorted pairs (a prefix: rows descending) run one warp per pair,
+// decided on the device from the call's own counts.  Only when every
+// eligible pair can (wave_rows_per_strip > 0: band half-width <= 263, or at
+// most 512 rows).  A call with at most `all_below` eligible pairs: all of
+// them (too few to fill the GPU one per lane).  Otherwise, with a band width
+// > 0, the long pairs whose one-lane time would exceed the call's expected
+// run time: a pair of `rows` rows costs one lane about rows * (2w + 1) cell
+// steps, the whole call about cells / lanes steps per lane (the longest
+// pairs start first, so a pair below that bound does not set the tail).
+// Pairs at or above max(min_rows, that bound) are counted by a binary search
+// over the sorted keys.
 __global__ void wave_split_kernel(const uint32_t *__restrict__ sorted_keys, int32_t *counters,
-                                  int32_t band_width, int32_t min_rows, int32_t adaptive,
-                                  int64_t lanes) {
+                                  int32_t band_width, int32_t all_below, int32_t min_rows,
+                                  int32_t adaptive, int64_t lanes) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int32_t n_elig = counters[0];
+    counters[6] = 0;
+    if (n_elig <= 0) return;
+    const int32_t max_rows = (int32_t)(sorted_keys[0] >> 13);
+    const bool all_capable = (band_width >= 1 && 2 * band_width < 31 * 16 + 32) || max_rows <= 512;
+    if (!all_capable) return;
+    if (n_elig <= all_below) { counters[6] = n_elig; return; }
+    if (band_width <= 0 || min_rows >= (1 << 13)) return;
     unsigned long long cells = 0;
     memcpy(&cells, counters + 4, sizeof(cells));
     int64_t rows_thr = min_rows;
@@ -636,7 +640,7 @@ static int32_t pow2_at_least(int64_t x) {
 }
 
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
-static int32_t g_rows_per_strip = 16;
+static int32_t g_rows_per_strip = 0;  // 0: by band width (8 up to w = 64, else 16)
 static int32_t g_variant = 1;
 // every pair runs one warp per pair when a call has at most this many pairs;
 // in larger calls, long pairs do: rows >= max(min rows, the adaptive bound)
@@ -675,8 +679,8 @@ static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t 
                                int32_t *err, cudaStream_t st, SwCounters *ctr);
 
 int32_t sw_set_rows_per_strip(int32_t r) {
-    if (r != 8 && r != 16 && r != 24) {
-        set_error(CK_ERR_UNSUPPORTED, "rows per strip must be 8, 16 or 24");
+    if (r != 0 && r != 8 && r != 16 && r != 24) {
+        set_error(CK_ERR_UNSUPPORTED, "rows per strip must be 0 (by band width), 8, 16 or 24");
         return CK_ERR_UNSUPPORTED;
     }
     g_rows_per_strip = r;
@@ -758,32 +762,28 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
     if (M > 0) {
         int64_t want = (M + 255) / 256;
         int blocks = (int)(want < 16 * (int64_t)sm_count() ? want : 16 * (int64_t)sm_count());
-        const bool wave_all = M <= (int64_t)g_wave_all_below;
-        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, wave_all ? 1 : 0,
-                                               d_err);
+        sw_prep_kernel<<<blocks, 256, 0, st>>>(in, out, M, ok, k0, v0, fb, cnt, cells, d_err);
         CK_CUDA(cudaGetLastError());
         cub::DoubleBuffer<uint32_t> dk(k0, k1), dv(v0, v1);
         size_t temp = 0;
-        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, temp, dk, dv, (int)M, 0, 27, st));
+        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, temp, dk, dv, (int)M, 0, 26, st));
         void *tmp = scratch(SLOT_SORT_TEMP, temp > 0 ? temp : 1, &status);
         if (!tmp) return status;
-        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, dk, dv, (int)M, 0, 27, st));
+        CK_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, temp, dk, dv, (int)M, 0, 26, st));
         int32_t wmax = 0;
         CK_TRY(widest_band(in, st, &wmax));
         const uint32_t *order = dv.Current();
-        // long pairs of a large call: only with one band width for every long
-        // pair (clustkit widens the band to the longer length when it is <= 0)
-        // that the warp-per-pair kernel can take at any length
-        if (!wave_all && in.band_width > 0 && wave_rows_per_strip(1 << 13, in.band_width) > 0 &&
-            g_wave_min_rows < (1 << 13)) {
-            wave_split_kernel<<<1, 32, 0, st>>>(dk.Current(), cnt, in.band_width, g_wave_min_rows,
-                                                g_wave_adaptive, (int64_t)sm_count() * 2 * STRIP_THREADS);
-            CK_CUDA(cudaGetLastError());
-        }
+        wave_split_kernel<<<1, 32, 0, st>>>(dk.Current(), cnt, in.band_width, g_wave_all_below,
+                                            g_wave_min_rows, g_wave_adaptive,
+                                            (int64_t)sm_count() * 2 * STRIP_THREADS);
+        CK_CUDA(cudaGetLastError());
         // profiling events bracket the alignment kernel
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
-        switch (g_rows_per_strip) {
+        // narrow bands: a strip's ramps (R - 1 masked columns at each end) weigh
+        // against 2w + 1 interior columns, so fewer rows per strip win there
+        const int32_t rows = g_rows_per_strip ? g_rows_per_strip : (wmax <= 64 ? 8 : 16);
+        switch (rows) {
             case 8:
                 CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;

@@ -37,6 +37,8 @@ from .blosum import BLOSUM62
 from .pairwise import ENGINE_BATCHED, PASS_SCORE
 
 LAMBDA = np.float32(0.267)
+_SUB = np.ascontiguousarray(BLOSUM62, np.int8)
+GRAPH_BUCKETS = (1, 2, 4, 8, 16, 32, 64)
 
 
 def compute_freq_threshold(kmer_freqs, num_sequences: int, percentile: float = 99.5) -> int:
@@ -177,8 +179,11 @@ class _Slot:
         self.batch = None
         # optional stage events: start, after the H2D copy, after Phase A, after SW, end
         self.stage_events = None
+        self.graphs: dict = {}  # batch-size bucket -> captured pipeline
+        self.graph_min_hits = None
 
     def close(self):
+        self.graphs.clear()
         if self.ctx:
             self.db.lib.ck_ctx_destroy(self.ctx)
             self.ctx = 0
@@ -210,9 +215,8 @@ class _Slot:
         if self.stage_events is not None:
             self.stage_events[i].record(self.stream)
 
-    def launch(self, queries: list[np.ndarray], min_total_hits: int):
-        """Enqueue the whole pipeline for a batch on this slot's stream."""
-        torch = _torch()
+    def _fill_host(self, queries, pad_to=None):
+        """Queries into the pinned staging buffers; (nq, lengths, residues)."""
         db = self.db
         nq = len(queries)
         lens = np.array([len(q) for q in queries], np.int32)
@@ -225,47 +229,96 @@ class _Slot:
         hres = self.h_res.numpy()
         if tot:
             hres[:tot] = np.concatenate(queries)
-        self.h_off.numpy()[:nq] = offs + self.res0
-        self.h_len.numpy()[:nq] = lens
+        n_all = nq if pad_to is None else pad_to
+        ho, hl = self.h_off.numpy(), self.h_len.numpy()
+        ho[:nq] = offs + self.res0
+        hl[:nq] = lens
+        ho[nq:n_all] = self.res0  # padding queries: empty
+        hl[nq:n_all] = 0
+        return nq, lens, tot
+
+    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, min_total_hits: int):
+        """The device pipeline of a batch of nq queries on this slot's stream:
+        H2D, Phase A, pair list, SW, D2H.  No host synchronisation, so it can
+        be captured in a CUDA graph."""
+        torch = _torch()
+        db = self.db
         K = self.max_cands
         M = nq * K
         lib = db.lib
+        st = self.stream.cuda_stream
+        self._mark(0)
+        db.d_flat[self.res0:self.res0 + res_bytes].copy_(self.h_res[:res_bytes], non_blocking=True)
+        db.d_offsets[self.seq0:self.seq0 + nq].copy_(self.h_off[:nq], non_blocking=True)
+        db.d_lengths[self.seq0:self.seq0 + nq].copy_(self.h_len[:nq], non_blocking=True)
+        qoff_ptr = db.d_offsets.data_ptr() + self.seq0 * 8
+        qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
+        self._mark(1)
+        _lib.check(lib.ck_search_phase_a_device(
+            self.ctx, db.d_flat.data_ptr(), qoff_ptr, qlen_ptr, nq, max_qlen,
+            db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+            db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
+            self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+        self._mark(2)
+        # dense pair list: (query, target) or (empty, empty) past a query's candidates
+        q = self.d_slotq[:M]
+        valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
+        self.d_pairs[:M, 0] = torch.where(valid, q + self.seq0, torch.full_like(q, db.empty_idx))
+        self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M], torch.full_like(q, db.empty_idx))
+        _lib.check(lib.ck_sw_batch_device_ctx(
+            self.ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
+            db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, db.band_width,
+            _SUB.ctypes.data, 0.0, None, PASS_SCORE, ENGINE_BATCHED,
+            self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(), st))
+        self._mark(3)
+        self.h_n[:nq].copy_(self.d_n[:nq], non_blocking=True)
+        self.h_targets[:M].copy_(self.d_targets[:M], non_blocking=True)
+        self.h_sims[:M].copy_(self.d_sims[:M], non_blocking=True)
+        self.h_scores[:M].copy_(self.d_scores[:M], non_blocking=True)
+        self.h_mask[:M].copy_(self.d_mask[:M], non_blocking=True)
+        self._mark(4)
+
+    def capture_graphs(self, min_total_hits: int, buckets=GRAPH_BUCKETS):
+        """Capture the pipeline once per batch-size bucket in CUDA graphs.
+
+        Every buffer is sized first by an uncaptured run of the largest
+        bucket; the slot's library context is then frozen so no scratch buffer
+        a graph points at is ever reallocated.  A batch then costs one graph
+        replay (queries padded with empty ones up to the bucket)."""
+        torch = _torch()
+        db = self.db
+        buckets = sorted({b for b in buckets if b <= db.arena_queries} | {db.arena_queries})
+        self.stage_events = None
         with torch.cuda.stream(self.stream):
-            st = self.stream.cuda_stream
-            self._mark(0)
-            db.d_flat[self.res0:self.res0 + tot].copy_(self.h_res[:tot], non_blocking=True)
-            db.d_offsets[self.seq0:self.seq0 + nq].copy_(self.h_off[:nq], non_blocking=True)
-            db.d_lengths[self.seq0:self.seq0 + nq].copy_(self.h_len[:nq], non_blocking=True)
-            qoff_ptr = db.d_offsets.data_ptr() + self.seq0 * 8
-            qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
-            self._mark(1)
-            _lib.check(lib.ck_search_phase_a_device(
-                self.ctx, db.d_flat.data_ptr(), qoff_ptr, qlen_ptr, nq, int(lens.max() if nq else 0),
-                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
-                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
-                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
-            self._mark(2)
-            # dense pair list: (query, target) or (empty, empty) past a query's candidates
-            q = self.d_slotq[:M]
-            valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
-            self.d_pairs[:M, 0] = torch.where(valid, q + self.seq0,
-                                              torch.full_like(q, db.empty_idx))
-            self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M],
-                                              torch.full_like(q, db.empty_idx))
-            _lib.check(lib.ck_sw_batch_device_ctx(
-                self.ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
-                db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, db.band_width,
-                np.ascontiguousarray(BLOSUM62).ctypes.data, 0.0, None, PASS_SCORE, ENGINE_BATCHED,
-                self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(),
-                st))
-            self._mark(3)
-            self.h_n[:nq].copy_(self.d_n[:nq], non_blocking=True)
-            self.h_targets[:M].copy_(self.d_targets[:M], non_blocking=True)
-            self.h_sims[:M].copy_(self.d_sims[:M], non_blocking=True)
-            self.h_scores[:M].copy_(self.d_scores[:M], non_blocking=True)
-            self.h_mask[:M].copy_(self.d_mask[:M], non_blocking=True)
-            self._mark(4)
-            self.event.record(self.stream)
+            self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, min_total_hits)
+        self.stream.synchronize()
+        _lib.check(db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream))
+        _lib.check(db.lib.ck_ctx_freeze(self.ctx, 1))
+        for b in buckets:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+                self._enqueue(b, db.arena_residues, db.arena_residues, min_total_hits)
+            self.graphs[b] = g
+        self.graph_min_hits = int(min_total_hits)
+        self.stream.synchronize()
+
+    def launch(self, queries: list[np.ndarray], min_total_hits: int):
+        """Enqueue the whole pipeline for a batch on this slot's stream."""
+        torch = _torch()
+        db = self.db
+        bucket = None
+        if self.graphs and int(min_total_hits) == self.graph_min_hits:
+            bucket = next((b for b in sorted(self.graphs) if b >= len(queries)), None)
+        if bucket is not None:
+            nq, lens, tot = self._fill_host(queries, pad_to=bucket)
+            with torch.cuda.stream(self.stream):
+                self.graphs[bucket].replay()
+                self.event.record(self.stream)
+        else:
+            nq, lens, tot = self._fill_host(queries)
+            with torch.cuda.stream(self.stream):
+                self._enqueue(nq, int(lens.max() if nq else 0), tot, min_total_hits)
+                self.event.record(self.stream)
         self.batch = (nq, lens)
 
     def results(self, top_k: int) -> list[list[SearchHit]]:
@@ -344,7 +397,7 @@ class SearchServer:
     """
 
     def __init__(self, db: DeviceDatabase, top_k: int = 10, max_cands: int = 500,
-                 min_total_hits: int = 2, max_batch: int | None = None):
+                 min_total_hits: int = 2, max_batch: int | None = None, use_graphs: bool = True):
         torch = _torch()
         self.db = db
         self.top_k = top_k
@@ -363,9 +416,12 @@ class SearchServer:
         self.running = False
         self.latencies: list[float] = []
         self.thread = None
-        # warm every slot so its scratch is allocated before serving
+        # allocate every slot's scratch before serving: capture its pipeline in
+        # CUDA graphs (one replay per batch), or warm it with one batch
         warm = [np.arange(40, dtype=np.uint8) % 20]
         for s in self.slots:
+            if use_graphs:
+                s.capture_graphs(min_total_hits)
             s.launch(warm, min_total_hits)
             s.event.synchronize()
             s.results(1)

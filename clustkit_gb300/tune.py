@@ -8,7 +8,8 @@ GB300 counterparts of "bin edges, band tiling and CTA shape":
   calls the pairs with at least ``wave_min_rows`` rows, raised (when
   ``wave_adaptive``) to where a pair's one-lane time would pass the call's
   expected time;
-* band tiling -- rows a lane keeps in registers per strip (8, 16, 24);
+* band tiling -- rows a lane keeps in registers per strip (8, 16, 24; the
+  library's default 0 picks 8 for half-widths up to 64, else 16);
 * strip variant -- prefetch distance (1 or 2 columns) and interior unroll
   (2 or 4 columns), i.e. the shape of a lane's inner loop.
 
@@ -37,7 +38,7 @@ KEYS = {
     "wave_adaptive": _lib.CFG_WAVE_ADAPTIVE,
 }
 
-DEFAULT = {"rows_per_strip": 16, "strip_variant": 1, "wave_min_rows": 256, "wave_all_below": 24576,
+DEFAULT = {"rows_per_strip": 0, "strip_variant": 1, "wave_min_rows": 256, "wave_all_below": 24576,
            "wave_adaptive": 1}
 
 # bin-edge candidates: (wave_min_rows, wave_adaptive); 1 << 30 = never by length

@@ -156,12 +156,16 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 
 /* Tunables of the batched engine, process-wide (the autotuner in
  * clustkit_gb300/tune.py picks them per workload):
- *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24
+ *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24,
+ *                          or 0 (default) for 8 when the band half-width is
+ *                          <= 64, else 16
  *   CK_CFG_STRIP_VARIANT   0..3: bit 0 prefetches the next columns' inputs two
  *                          columns ahead (else one), bit 1 runs interior
  *                          columns four at a time (else two)
- *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs run every pair
- *                          one warp per pair (default 24576)
+ *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs to align (the
+ *                          count is taken on the device, after empty and
+ *                          skipped pairs) run every pair one warp per pair
+ *                          (default 24576)
  *   CK_CFG_WAVE_MIN_ROWS   in larger calls with band_width > 0, pairs with at
  *                          least this many rows (shorter side) run one warp
  *                          per pair instead of one lane per pair (default 256)
@@ -208,6 +212,12 @@ int32_t ck_jaccard_device(const int32_t *d_pairs, int64_t M, const uint64_t *d_s
  * bound to the device current at creation. */
 int32_t ck_ctx_create(int32_t *out_handle);
 int32_t ck_ctx_destroy(int32_t handle);
+/* Freeze (1) or thaw (0) a context's scratch: while frozen, a call that would
+ * need to grow a scratch buffer fails with CK_ERR_UNSUPPORTED instead of
+ * reallocating it, so the buffers stay valid inside CUDA graphs captured from
+ * calls on this context (size them with one uncaptured call of the largest
+ * shape first). */
+int32_t ck_ctx_freeze(int32_t handle, int32_t frozen);
 /* Synchronises `stream` and returns CK_OK or CK_ERR_OUT_OF_RANGE for GPU-side
  * input checks of the context's calls since its last status read. */
 int32_t ck_ctx_status(int32_t handle, void *stream);

@@ -138,9 +138,11 @@ def test_phase_a_cap_and_ties_vs_oracle(ck):
 
 
 @pytest.mark.gpu
-def test_server_results_same_alone_and_in_mix(ck):
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_server_results_same_alone_and_in_mix(ck, use_graphs):
     """Each query's hits are identical whether it is searched alone or lands
-    in concurrent batches of the continuous-batching server."""
+    in concurrent batches of the continuous-batching server (slots replaying
+    captured CUDA graphs, or launching the pipeline call by call)."""
     from clustkit_gb300.search import DeviceDatabase, SearchServer, search_batch
     db_set = synth.generate_families(400, 10, median=200, lo=40, hi=600, seed=92)
     db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_slots=3, arena_queries=16,
@@ -150,7 +152,7 @@ def test_server_results_same_alone_and_in_mix(ck):
     bg = synth.random_sequences(20, median=200, lo=40, hi=600, seed=93)
     qs += [bg.seq(i).copy() for i in range(bg.n)]
     alone = [search_batch(db, [q], top_k=10)[0] for q in qs]
-    server = SearchServer(db, top_k=10, max_batch=7).start()
+    server = SearchServer(db, top_k=10, max_batch=7, use_graphs=use_graphs).start()
     try:
         futs = [server.submit(q) for q in qs]
         mixed = [f.result(timeout=120) for f in futs]
@@ -163,3 +165,42 @@ def test_server_results_same_alone_and_in_mix(ck):
     assert any(len(h) for h in mixed)
     lat = server.latency_percentiles()
     assert lat["n"] == len(qs)
+
+
+def test_frozen_context_refuses_to_grow(ck):
+    """A frozen context (its buffers may sit in a captured graph) keeps
+    working at the sizes it has and fails, instead of reallocating, beyond."""
+    import torch
+    from clustkit_gb300 import _lib
+    from clustkit_gb300.blosum import BLOSUM62
+    lib = _lib.load()
+    s = synth.generate_families(50, 10, median=200, lo=40, hi=600, seed=4)
+    pairs = synth.mixed_pairs(s, 60000, seed=1)
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_pairs, d_flat, d_off, d_len = T(pairs), T(s.flat), T(s.offsets), T(s.lengths)
+    outs = [torch.empty(len(pairs), dtype=dt, device=dev) for dt in (torch.float32, torch.int32, torch.uint8)]
+    sub = np.ascontiguousarray(BLOSUM62, np.int8)
+    h = np.zeros(1, np.int32)
+    _lib.check(lib.ck_ctx_create(h.ctypes.data))
+    ctx = int(h[0])
+    st = torch.cuda.current_stream(dev).cuda_stream
+
+    def call(m):
+        return lib.ck_sw_batch_device_ctx(ctx, d_pairs.data_ptr(), m, d_flat.data_ptr(), len(s.flat),
+                                          d_off.data_ptr(), d_len.data_ptr(), s.n, 100, sub.ctypes.data,
+                                          0.0, None, _lib.PASS_SCORE, 0, outs[0].data_ptr(),
+                                          outs[1].data_ptr(), None, None, outs[2].data_ptr(), st)
+    try:
+        assert call(1000) == 0
+        _lib.check(lib.ck_ctx_status(ctx, st))
+        _lib.check(lib.ck_ctx_freeze(ctx, 1))
+        assert call(1000) == 0
+        assert call(len(pairs)) == 5  # CK_ERR_UNSUPPORTED: would have to grow
+        _lib.check(lib.ck_ctx_freeze(ctx, 0))
+        assert call(len(pairs)) == 0
+        _lib.check(lib.ck_ctx_status(ctx, st))
+        ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, 100, BLOSUM62)
+        assert np.array_equal(outs[1].cpu().numpy(), ref["scores"])
+    finally:
+        lib.ck_ctx_destroy(ctx)
