@@ -55,7 +55,7 @@ SIGNATURES = {
                                       _I32, _I32, _P, _P, _P, _P, _P, _P]),
     "ck_kmer_index_build_device": (_I32, [_I32, _P, _I64, _P, _P, _I64, _I32, _I32, _P, _P, _I64, _P, _P,
                                           _P]),
-    "ck_search_phase_a_device": (_I32, [_I32, _P, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _I32, _I32,
+    "ck_search_phase_a_device": (_I32, [_I32, _P, _I64, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _I32, _I32,
                                         _I32, _I32, _P, _P, _P, _P]),
     "ck_sw_last_counters": (_I32, [_P]),
     "ck_sw_last_wave_pairs": (_I32, [_P]),

@@ -158,7 +158,7 @@ static int32_t index_build_impl(void *pv) {
 // ----------------------------------------------------------------- phase A
 // Grid (blocks, nq): the warps of a query's blocks take its k-mer positions
 // in turn; a warp walks one posting list, lanes adding hits in parallel.
-__global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat,
+__global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len,
                                      const int64_t *__restrict__ qoff,
                                      const int32_t *__restrict__ qlen, int32_t k, int32_t alpha,
                                      const int64_t *__restrict__ kmer_offsets,
@@ -168,7 +168,12 @@ __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat,
     const int32_t q = blockIdx.y;
     const int lane = threadIdx.x & 31;
     const int32_t L = qlen[q];
-    const uint8_t *s = qflat + qoff[q];
+    const int64_t o = qoff[q];
+    if (L < 0 || o < 0 || o + L > qflat_len) {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERRBIT_SEQ_EXTENT);
+        return;
+    }
+    const uint8_t *s = qflat + o;
     int32_t *c = counts + (int64_t)q * num_db;
     const int32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (int32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p <= L - k; p += warps) {
@@ -305,7 +310,7 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
 }
 
 struct PhaseAArgs {
-    const uint8_t *qflat; const int64_t *qoff; const int32_t *qlen; int32_t nq; int32_t max_qlen;
+    const uint8_t *qflat; int64_t qflat_len; const int64_t *qoff; const int32_t *qlen; int32_t nq; int32_t max_qlen;
     int32_t k, alpha; const int64_t *kmer_offsets; const int64_t *kmer_entries;
     const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
     int32_t *out_targets; int32_t *out_scores; int32_t *out_n; cudaStream_t st;
@@ -326,7 +331,7 @@ static int32_t phase_a_impl(void *pv) {
         int bx = (npos + 7) / 8;  // 8 warps per block
         if (bx > 16) bx = 16;
         dim3 grid((unsigned)bx, (unsigned)a.nq);
-        phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qoff, a.qlen, a.k, a.alpha,
+        phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha,
                                                       a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
                                                       a.freq_thresh, a.num_db, counts, err);
         CK_CUDA(cudaGetLastError());
@@ -361,7 +366,8 @@ extern "C" int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat
     return run_in_context(ctx, index_build_impl, &a);
 }
 
-extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, const int64_t *d_qoffsets,
+extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
+                                            const int64_t *d_qoffsets,
                                             const int32_t *d_qlengths, int32_t nq, int32_t max_qlen,
                                             int32_t k, int32_t alpha, const int64_t *d_kmer_offsets,
                                             const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
@@ -370,12 +376,12 @@ extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat,
                                             int32_t *d_out_n, void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
-    if (nq < 0 || nq > 65535 || top_k < 1 || k < 1 || alpha < 1 || num_db < 0 || !d_out_targets || !d_out_n ||
+    if (nq < 0 || nq > 65535 || qflat_len < 0 || top_k < 1 || k < 1 || alpha < 1 || num_db < 0 || !d_out_targets || !d_out_n ||
         (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets || !d_kmer_freqs) {
         set_error(CK_ERR_INVALID_ARGUMENT, "phase A: bad arguments");
         return CK_ERR_INVALID_ARGUMENT;
     }
-    PhaseAArgs a{d_qflat, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha, d_kmer_offsets, d_kmer_entries,
+    PhaseAArgs a{d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha, d_kmer_offsets, d_kmer_entries,
                  d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k, d_out_targets, d_out_scores,
                  d_out_n, (cudaStream_t)stream};
     return run_in_context(ctx, phase_a_impl, &a);

@@ -166,7 +166,7 @@ class _Slot:
         self.d_mask = torch.empty(Q * K, dtype=torch.uint8, device=dev)
         self.d_slotq = torch.arange(Q, dtype=torch.int32, device=dev).repeat_interleave(K)
         self.d_col = torch.arange(K, dtype=torch.int32, device=dev).repeat(Q)
-        pin = lambda n, dt: torch.empty(n, dtype=dt).pin_memory()
+        pin = lambda n, dt: torch.zeros(n, dtype=dt).pin_memory()
         self.h_res = pin(db.arena_residues, torch.uint8)
         self.h_off = pin(Q, torch.int64)
         self.h_len = pin(Q, torch.int32)
@@ -255,7 +255,7 @@ class _Slot:
         qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
         self._mark(1)
         _lib.check(lib.ck_search_phase_a_device(
-            self.ctx, db.d_flat.data_ptr(), qoff_ptr, qlen_ptr, nq, max_qlen,
+            self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
             db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
             db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
             self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
@@ -289,6 +289,7 @@ class _Slot:
         db = self.db
         buckets = sorted({b for b in buckets if b <= db.arena_queries} | {db.arena_queries})
         self.stage_events = None
+        self._fill_host([], pad_to=buckets[-1])  # every query slot an empty query
         with torch.cuda.stream(self.stream):
             self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, min_total_hits)
         self.stream.synchronize()

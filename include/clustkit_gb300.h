@@ -250,9 +250,12 @@ int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat, int64_t f
  * at least min_total_hits hits survive; at most top_k per query, chosen by hit
  * count with ties to the lower target id, are written in target-id order to
  * d_out_targets[q * top_k ...] (hit counts to d_out_scores, may be NULL) and
- * their number to d_out_n[q].  max_qlen bounds the query lengths.  Uses
- * nq * num_db * 4 bytes of context scratch. */
-int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, const int64_t *d_qoffsets,
+ * their number to d_out_n[q].  Every query's extent is checked against
+ * qflat_len on the device (CK_ERR_OUT_OF_RANGE, reported by ck_ctx_status);
+ * max_qlen sizes the grid only.  Uses nq * num_db * 4 bytes of context
+ * scratch. */
+int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
+                                 const int64_t *d_qoffsets,
                                  const int32_t *d_qlengths, int32_t nq, int32_t max_qlen, int32_t k,
                                  int32_t alpha, const int64_t *d_kmer_offsets,
                                  const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
