@@ -167,6 +167,7 @@ def test_server_results_same_alone_and_in_mix(ck, use_graphs):
     assert lat["n"] == len(qs)
 
 
+@pytest.mark.gpu
 def test_frozen_context_refuses_to_grow(ck):
     """A frozen context (its buffers may sit in a captured graph) keeps
     working at the sizes it has and fails, instead of reallocating, beyond."""
