@@ -205,6 +205,7 @@ enum ScratchSlot {
     SLOT_SEQ_OK,
     SLOT_MAXLEN,
     SLOT_SEARCH_COUNTS,
+    SLOT_SEARCH_CAND,
     SLOT_SEARCH_TMP0,
     SLOT_SEARCH_TMP1,
     SLOT_SEARCH_TMP2,

@@ -12,6 +12,7 @@
 // counts saturate at 32767 as clustkit's int16 counters do; targets with
 // count >= min_total_hits survive; at most top_k survive per query, chosen by
 // count (ties: lower target id first), returned in target-id order.
+#include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -156,6 +157,10 @@ static int32_t index_build_impl(void *pv) {
 }
 
 // ----------------------------------------------------------------- phase A
+// Targets that reach min_hits are listed as they cross it; up to CAND_CAP per
+// query the select works on that list, beyond it on the full count row.
+constexpr int32_t CAND_CAP = 4096;
+
 // Grid (blocks, nq): the warps of a query's blocks take its k-mer positions
 // in turn; a warp walks one posting list, lanes adding hits in parallel.
 __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len,
@@ -164,7 +169,9 @@ __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t 
                                      const int64_t *__restrict__ kmer_offsets,
                                      const int64_t *__restrict__ kmer_entries,
                                      const int32_t *__restrict__ kmer_freqs, int32_t freq_thresh,
-                                     int32_t num_db, int32_t *__restrict__ counts, int32_t *err) {
+                                     int32_t num_db, int32_t *__restrict__ counts, int32_t min_hits,
+                                     int32_t *__restrict__ cand, int32_t *__restrict__ n_cand,
+                                     int32_t *err) {
     const int32_t q = blockIdx.y;
     const int lane = threadIdx.x & 31;
     const int32_t L = qlen[q];
@@ -188,8 +195,15 @@ __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t 
         const int64_t b = kmer_offsets[v], e = kmer_offsets[v + 1];
         for (int64_t h = b + lane; h < e; h += 32) {
             const int32_t t = (int32_t)(kmer_entries[h] >> 32);
-            if (t >= 0 && t < num_db) atomicAdd(&c[t], 1);
-            else atomicOr(err, ERRBIT_PAIR_INDEX);
+            if (t >= 0 && t < num_db) {
+                // the hit that lifts a target to min_hits lists it (once: counts only grow)
+                if (atomicAdd(&c[t], 1) == min_hits - 1) {
+                    const int32_t pos = atomicAdd(&n_cand[q], 1);
+                    if (pos < CAND_CAP) cand[(int64_t)q * CAND_CAP + pos] = t;
+                }
+            } else {
+                atomicOr(err, ERRBIT_PAIR_INDEX);
+            }
         }
     }
 }
@@ -198,14 +212,109 @@ constexpr int SELECT_THREADS = 1024;
 
 // One block per query: the top_k surviving targets by (count desc, id asc),
 // written in id order.  Counts are clamped to 32767 first.
+// The same selection over a query's candidate list (every listed target
+// has count >= min_hits, and every such target is listed): sort the ids
+// (bitonic, shared memory), find the threshold by histogram, compact in id
+// order with block scans.
+__device__ void select_from_list(const int32_t *__restrict__ c, const int32_t *__restrict__ list,
+                                 int32_t n, int32_t q, int32_t top_k, int32_t *__restrict__ out_targets,
+                                 int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
+    using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
+    __shared__ typename BlockScan::TempStorage scan_tmp;
+    __shared__ int32_t s_id[CAND_CAP];
+    __shared__ int32_t hist[256];
+    __shared__ int32_t sh_thr, sh_take_eq, sh_run_eq, sh_run_sel;
+    const int tid = threadIdx.x;
+    int32_t P = 1;
+    while (P < n) P <<= 1;
+    for (int32_t i = tid; i < P; i += SELECT_THREADS) s_id[i] = i < n ? list[i] : INT32_MAX;
+    __syncthreads();
+    for (int32_t k = 2; k <= P; k <<= 1) {
+        for (int32_t j = k >> 1; j > 0; j >>= 1) {
+            for (int32_t i = tid; i < P; i += SELECT_THREADS) {
+                const int32_t l = i ^ j;
+                if (l > i) {
+                    const int32_t a = s_id[i], b = s_id[l];
+                    if (((i & k) == 0) == (a > b)) { s_id[i] = b; s_id[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    auto val = [&](int32_t t) { const int32_t v = c[t]; return v > 32767 ? 32767 : v; };
+    for (int i = tid; i < 256; i += SELECT_THREADS) hist[i] = 0;
+    if (tid == 0) { sh_thr = -1; sh_take_eq = 0; sh_run_eq = 0; sh_run_sel = 0; }
+    __syncthreads();
+    if (n > top_k) {
+        for (int32_t i = tid; i < n; i += SELECT_THREADS) atomicAdd(&hist[val(s_id[i]) >> 7], 1);
+        __syncthreads();
+        if (tid == 0) {
+            int32_t above = 0, b = 255;
+            for (; b >= 0; --b) {
+                if (above + hist[b] >= top_k) break;
+                above += hist[b];
+            }
+            sh_thr = b;
+            sh_take_eq = above;
+        }
+        __syncthreads();
+        const int32_t coarse = sh_thr, above_coarse = sh_take_eq;
+        for (int i = tid; i < 128; i += SELECT_THREADS) hist[i] = 0;
+        __syncthreads();
+        for (int32_t i = tid; i < n; i += SELECT_THREADS) {
+            const int32_t v = val(s_id[i]);
+            if ((v >> 7) == coarse) atomicAdd(&hist[v & 127], 1);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int32_t above = above_coarse, lo = 127;
+            for (; lo >= 0; --lo) {
+                if (above + hist[lo] >= top_k) break;
+                above += hist[lo];
+            }
+            sh_thr = (coarse << 7) | lo;
+            sh_take_eq = top_k - above;
+        }
+        __syncthreads();
+    }
+    const int32_t thr = sh_thr, take_eq = sh_take_eq;
+    for (int32_t base = 0; base < n; base += SELECT_THREADS) {
+        const int32_t i = base + tid;
+        const int32_t t = i < n ? s_id[i] : 0;
+        const int32_t v = i < n ? val(t) : -1;
+        const int32_t is_eq = (i < n && thr >= 0 && v == thr) ? 1 : 0;
+        int32_t eq_rank, eq_tot;
+        BlockScan(scan_tmp).ExclusiveSum(is_eq, eq_rank, eq_tot);
+        __syncthreads();
+        const bool sel = i < n && (thr < 0 || v > thr || (is_eq && sh_run_eq + eq_rank < take_eq));
+        int32_t pos, sel_tot;
+        BlockScan(scan_tmp).ExclusiveSum(sel ? 1 : 0, pos, sel_tot);
+        if (sel) {
+            const int64_t o = (int64_t)q * top_k + sh_run_sel + pos;
+            out_targets[o] = t;
+            if (out_scores) out_scores[o] = v;
+        }
+        __syncthreads();
+        if (tid == 0) { sh_run_eq += eq_tot; sh_run_sel += sel_tot; }
+        __syncthreads();
+    }
+    if (tid == 0) out_n[q] = n < top_k ? n : top_k;
+}
+
 __global__ void __launch_bounds__(SELECT_THREADS)
 phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits,
-                      int32_t top_k, int32_t *__restrict__ out_targets,
+                      int32_t top_k, const int32_t *__restrict__ cand,
+                      const int32_t *__restrict__ n_cand, int32_t *__restrict__ out_targets,
                       int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
-    __shared__ int32_t hist[256];
-    __shared__ int32_t sh_thr, sh_take_eq, sh_total;
     const int32_t q = blockIdx.x;
     const int32_t *c = counts + (int64_t)q * num_db;
+    if (min_hits >= 1 && n_cand[q] <= CAND_CAP) {
+        select_from_list(c, cand + (int64_t)q * CAND_CAP, n_cand[q], q, top_k, out_targets, out_scores,
+                         out_n);
+        return;
+    }
+    __shared__ int32_t hist[256];
+    __shared__ int32_t sh_thr, sh_take_eq, sh_total;
     const int tid = threadIdx.x;
     auto val = [&](int32_t t) { const int32_t v = c[t]; return v > 32767 ? 32767 : v; };
 
@@ -325,7 +434,11 @@ static int32_t phase_a_impl(void *pv) {
     const size_t nc = (size_t)a.nq * (size_t)a.num_db;
     int32_t *counts = (int32_t *)scratch(SLOT_SEARCH_COUNTS, nc * 4 + 4, &status);
     if (!counts) return status;
+    int32_t *cand = (int32_t *)scratch(SLOT_SEARCH_CAND, (size_t)a.nq * (CAND_CAP + 1) * 4, &status);
+    if (!cand) return status;
+    int32_t *n_cand = cand + (size_t)a.nq * CAND_CAP;
     CK_CUDA(cudaMemsetAsync(counts, 0, nc * 4, a.st));
+    CK_CUDA(cudaMemsetAsync(n_cand, 0, (size_t)a.nq * 4, a.st));
     const int32_t npos = a.max_qlen - a.k + 1;
     if (npos > 0) {
         int bx = (npos + 7) / 8;  // 8 warps per block
@@ -333,11 +446,12 @@ static int32_t phase_a_impl(void *pv) {
         dim3 grid((unsigned)bx, (unsigned)a.nq);
         phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha,
                                                       a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
-                                                      a.freq_thresh, a.num_db, counts, err);
+                                                      a.freq_thresh, a.num_db, counts, a.min_hits, cand,
+                                                      n_cand, err);
         CK_CUDA(cudaGetLastError());
     }
-    phase_a_select_kernel<<<a.nq, SELECT_THREADS, 0, a.st>>>(counts, a.num_db, a.min_hits, a.top_k,
-                                                             a.out_targets, a.out_scores, a.out_n);
+    phase_a_select_kernel<<<a.nq, SELECT_THREADS, 0, a.st>>>(counts, a.num_db, a.min_hits, a.top_k, cand,
+                                                             n_cand, a.out_targets, a.out_scores, a.out_n);
     CK_CUDA(cudaGetLastError());
     return CK_OK;
 }

@@ -113,6 +113,38 @@ def test_search_batch_matches_reference(ck, golden):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("min_hits", [1, 2])
+def test_phase_a_candidate_list_overflow(ck, min_hits):
+    """Queries whose targets at >= min_hits outnumber the select's candidate
+    list (4,096) take the full-row path; the result is the same."""
+    from clustkit_gb300.search import DeviceDatabase, _Slot
+    db_set = synth.generate_families(5000, 8, median=300, lo=40, hi=800, seed=12)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=4,
+                        arena_residues=4 * 3000)
+    off, ent, fr = db.index_arrays()
+    bg = synth.random_sequences(2, median=2500, lo=2400, hi=2600, seed=13)
+    qs = [bg.seq(0).copy(), bg.seq(1).copy(), db_set.seq(7).copy()]
+    cap = 500
+    slot = _Slot(db, 0, cap)
+    try:
+        slot.launch(qs, min_hits)
+        slot.event.synchronize()
+        n = slot.h_n.numpy()[:len(qs)]
+        tg = slot.h_targets.numpy().reshape(-1, cap)
+        over = 0
+        for qi, q in enumerate(qs):
+            ids, _ = so.phase_a(q, 5, 20, off, ent, fr, db.freq_thresh, db_set.n, min_hits, cap)
+            assert np.array_equal(tg[qi, :n[qi]], ids), qi
+            allc, _ = so.phase_a(q, 5, 20, off, ent, fr, db.freq_thresh, db_set.n, min_hits, 10 ** 9)
+            over += len(allc) > 4096
+        slot.results(3)
+        if min_hits == 1:
+            assert over >= 1  # the long background queries overflow the list
+    finally:
+        slot.close()
+
+
+@pytest.mark.gpu
 def test_phase_a_cap_and_ties_vs_oracle(ck):
     from clustkit_gb300.search import DeviceDatabase, _Slot
     db_set = synth.generate_families(300, 8, median=150, lo=40, hi=400, seed=91)
