@@ -89,8 +89,22 @@ __device__ __forceinline__ bool seq_codes_ok(const SwIn &in, int32_t i, uint8_t 
     if (m) return m == 1;
     const uint8_t *s = in.flat + in.offsets[i];
     const int32_t L = in.lengths[i];
-    bool good = true;
-    for (int32_t t = 0; t < L && good; ++t) good = __ldg(s + t) <= 20;
+    // bytes up to a 16-byte boundary, then 16 per load (four compared per
+    // instruction), then the tail
+    int32_t head = (int32_t)((16u - ((uint32_t)(uintptr_t)s & 15u)) & 15u);
+    if (head > L) head = L;
+    uint32_t bad = 0;
+    for (int32_t t = 0; t < head; ++t) bad |= __ldg(s + t) > 20 ? 1u : 0u;
+    const uint4 *v = (const uint4 *)(s + head);
+    const int32_t nv = (L - head) >> 4;
+#pragma unroll 4
+    for (int32_t k = 0; k < nv; ++k) {
+        const uint4 x = __ldg(v + k);
+        bad |= __vcmpgtu4(x.x, 0x14141414u) | __vcmpgtu4(x.y, 0x14141414u) |
+               __vcmpgtu4(x.z, 0x14141414u) | __vcmpgtu4(x.w, 0x14141414u);
+    }
+    for (int32_t t = head + nv * 16; t < L; ++t) bad |= __ldg(s + t) > 20 ? 1u : 0u;
+    const bool good = bad == 0;
     ok[i] = good ? 1 : 2;
     return good;
 }
