@@ -40,6 +40,7 @@ sys.path.insert(0, str(REPO))
 
 BAND_WIDTH = 100
 THRESHOLD = 0.3
+THRESHOLD_MILLION = 0.4
 WORKLOAD = {"workload": "align-50k: 5000 families x 10, median 350 [30,2000], k=5 s=128, "
                         "LSH b=1 L=512 (t=0.3 high), Jaccard pre-filter, SW bw=100 BLOSUM62 -11/-1",
             "n_sequences": 50000, "threshold": THRESHOLD, "band_width": BAND_WIDTH,
@@ -430,6 +431,11 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if rank == 0 and args.million == "on":
+        try:
+            line["million"] = run_million(args)
+        except Exception as e:
+            line["million"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and (args.uneven == "on" or (args.uneven == "auto" and not args.quick)):
         try:
             line["uneven"] = run_uneven(args)
@@ -479,6 +485,98 @@ def run_uneven(args):
                                    "bit_exact_vs_plain": bool(same)}
         log(f"uneven bw={bw}: {out['by_band'][str(bw)]}")
         del call
+    return out
+
+
+# ----------------------------------------------------------------------------- 1M-sequence streaming
+def run_million(args):
+    """1,000,000 sequences (100,000 families x 10, median 300, 30..1500), t = 0.4:
+    sketches on the GPU, LSH on the GPU, the Jaccard pre-filter on the GPU, then
+    every surviving pair through the batched SW engine in device-resident
+    chunks.  Reports each stage's time, GCUPS and pairs/s of the SW stream."""
+    import torch
+    from clustkit_gb300 import _lib, synth
+    from clustkit_gb300.blosum import BLOSUM62
+    from clustkit_gb300.cells import band_cells, effective_band
+    from clustkit_gb300.lsh import auto_lsh_params, lsh_candidates_device
+    from clustkit_gb300.pairwise import ENGINE_BATCHED, PASS_CPU
+    lib = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n_fam = 10_000 if args.quick else 100_000
+    t0 = time.time()
+    s = synth.generate_families(n_fam, 10, median=300, lo=30, hi=1500, seed=31)
+    t_gen = time.time() - t0
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_flat, d_off, d_len = T(s.flat), T(s.offsets), T(s.lengths)
+    stream = torch.cuda.current_stream(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    e0, e1, e2, e3 = ev(), ev(), ev(), ev()
+    sk = torch.empty((s.n, 128), dtype=torch.int64, device=dev)
+    e0.record(stream)
+    _lib.check(lib.ck_sketch_device(d_flat.data_ptr(), len(s.flat), d_off.data_ptr(), d_len.data_ptr(), s.n, 5,
+                                    128, 20, 42, sk.data_ptr(), stream.cuda_stream))
+    e1.record(stream)
+    lp = auto_lsh_params(THRESHOLD_MILLION, "medium", 5)
+    t1 = time.time()
+    cand = lsh_candidates_device(sk, lp["num_tables"], lp["num_bands"], 42)
+    torch.cuda.synchronize()
+    t_lsh = time.time() - t1
+    n_cand = int(cand.shape[0])
+    # Jaccard pre-filter (clustkit/pairwise.py:949-1001): the 2000-pair cost check
+    # drawn with RandomState(0) on the host, the filter itself on the device
+    floor = max(0.001, 0.3 * THRESHOLD_MILLION ** 5)
+    sims = torch.empty(n_cand, dtype=torch.float32, device=dev)
+    mask = torch.empty(n_cand, dtype=torch.uint8, device=dev)
+    e2.record(stream)
+    _lib.check(lib.ck_jaccard_device(cand.data_ptr(), n_cand, sk.data_ptr(), s.n, 128, float(np.float32(floor)),
+                                     sims.data_ptr(), mask.data_ptr(), stream.cuda_stream))
+    e3.record(stream)
+    rng = np.random.RandomState(0)
+    sample = rng.choice(n_cand, size=min(2000, n_cand), replace=False) if n_cand > 2000 else np.arange(n_cand)
+    est = float((sims[T(sample)].cpu().numpy() < np.float32(floor)).mean()) if n_cand else 0.0
+    pairs = cand[mask.bool()] if est >= 0.05 else cand
+    del cand, sims, mask
+    M = int(pairs.shape[0])
+    L = s.lengths.astype(np.int64)
+    ph = pairs.cpu().numpy()
+    la = np.minimum(L[ph[:, 0]], L[ph[:, 1]])
+    lb = np.maximum(L[ph[:, 0]], L[ph[:, 1]])
+    cells = int(band_cells(la, lb, effective_band(la, lb, BAND_WIDTH)).sum())
+    del ph, la, lb
+    chunk = 20_000_000
+    outs = [torch.empty(min(chunk, max(M, 1)), dtype=dt, device=dev)
+            for dt in (torch.float32, torch.int32, torch.int32, torch.int32, torch.uint8)]
+    sub = np.ascontiguousarray(BLOSUM62)
+
+    def sw_stream():
+        for c0 in range(0, M, chunk):
+            m = min(chunk, M - c0)
+            _lib.check(lib.ck_sw_batch_device(
+                pairs[c0:].data_ptr(), m, d_flat.data_ptr(), len(s.flat), d_off.data_ptr(), d_len.data_ptr(),
+                s.n, BAND_WIDTH, sub.ctypes.data, THRESHOLD_MILLION, None, PASS_CPU, ENGINE_BATCHED,
+                outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(), outs[3].data_ptr(), outs[4].data_ptr(),
+                stream.cuda_stream))
+
+    sw_stream()  # warm-up (scratch sized for the largest chunk)
+    torch.cuda.synchronize()
+    a, b = ev(), ev()
+    a.record(stream)
+    sw_stream()
+    b.record(stream)
+    b.synchronize()
+    _lib.check(lib.ck_sw_status_device(stream.cuda_stream))
+    sw_ms = a.elapsed_time(b)
+    gcups = cells / (sw_ms * 1e-3) / 1e9
+    out = {"workload": f"million: {s.n} seqs ({n_fam} families x 10, median 300, 30..1500), t={THRESHOLD_MILLION}, "
+                       f"k=5 s=128, LSH b={lp['num_bands']} L={lp['num_tables']}, Jaccard floor {floor:.6f}, "
+                       f"bw={BAND_WIDTH}",
+           "generate_s": t_gen, "sketch_ms": e0.elapsed_time(e1), "lsh_s": t_lsh, "lsh_candidates": n_cand,
+           "jaccard_ms": e2.elapsed_time(e3), "prefilter_applied": est >= 0.05, "pairs": M, "cells": cells,
+           "sw_ms": sw_ms, "gcups": gcups, "pairs_per_s": M / (sw_ms * 1e-3), "chunk_pairs": chunk,
+           "roofline_frac": gcups * 1e9 * 6 / 20.06e12,
+           "hbm_gbs_est": gcups * 1.08,
+           "hbm_basis": "1.08 DRAM bytes per cell, the strip kernel's measured traffic on the 50k set"}
+    log(f"million: {out}")
     return out
 
 
@@ -605,10 +703,20 @@ def main():
                     help="search/serving leg (auto: on for the full workload, off with --quick)")
     ap.add_argument("--uneven", choices=["auto", "on", "off", "only"], default="auto",
                     help="heavy-tailed lengths + autotuner leg (auto: on for the full workload)")
+    ap.add_argument("--million", choices=["off", "on", "only"], default="off",
+                    help="1M-sequence leg: GPU sketches, GPU LSH, pre-filter, SW in device-resident chunks")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.million == "only":
+        import torch
+        from clustkit_gb300 import _lib
+        torch.cuda.set_device(local)
+        _lib.load()
+        _lib.require_gpu()
+        print(json.dumps({"metric": "banded-SW GCUPS streaming 1M sequences' LSH pairs in device-resident chunks",
+                          "million": run_million(args)}), flush=True)
     elif args.uneven == "only":
         import torch
         from clustkit_gb300 import _lib

@@ -1,18 +1,20 @@
-"""Host-side LSH candidate generation (input producer for the Align phase).
+"""LSH candidate generation (the input producer of the Align phase).
 
-This restates clustkit's CPU LSH (clustkit/lsh.py:20-178) in vectorised numpy
-so that the benchmarks and tests can build the candidate-pair list the Align
-phase consumes, exactly as clustkit would.  It is not part of the GPU hot
-path.
+``lsh_candidates_device`` runs clustkit's LSH (clustkit/lsh.py:20-178) on the
+GPU (csrc/lsh.cu); ``lsh_candidates`` restates it in vectorised numpy on the
+host, with numpy's own argsort, for small inputs and as the tie-order
+reference.  Both:
 
 * band indices and per-table seeds come from ``np.random.RandomState(seed)``
   in the same draw order (lsh.py:116-123);
 * a bucket id is ``h = seed; h = h*0x517CC1B727220A95 + sketch[idx]`` over the
   band, then ``h = (h ^ h>>33) * 0xC4CEB9FE1A85EC53; h ^= h>>33``
   (lsh.py:20-29), all in wrapping uint64;
-* per table the ids are ordered with ``np.argsort`` (the same call, so ties
-  come out in the same order) and every bucket contributes all pairs among its
-  first 1000 members (lsh.py:51-90, 153-156);
+* per table the sequences are ordered by bucket id and every bucket
+  contributes all pairs among its first 1000 members (lsh.py:51-90, 153-156)
+  -- the host version with ``np.argsort`` (the same call as clustkit, so ties
+  come out in the same order), the device version with a stable radix sort
+  (members in ascending id; identical unless a bucket has more than 1000);
 * pairs are packed ``i*N + j`` with ``i < j``, sorted and de-duplicated
   (lsh.py:163-178).
 """
@@ -102,6 +104,38 @@ def lsh_candidates(sketches: np.ndarray, num_tables: int, num_bands: int, seed: 
     pairs[:, 0] = (allp // n).astype(np.int32)
     pairs[:, 1] = (allp % n).astype(np.int32)
     return pairs
+
+
+def lsh_candidates_device(sketches, num_tables: int, num_bands: int, seed: int = 42, ctx: int = 0):
+    """(M, 2) int32 torch tensor on the sketches' device: the de-duplicated
+    candidate pairs (i < j, sorted), computed on the GPU.  ``sketches`` is a
+    uint64 numpy array or an int64/uint64-bit torch CUDA tensor [N, s]."""
+    import torch
+
+    from . import _lib
+    lib = _lib.load()
+    _lib.require_gpu()
+    if isinstance(sketches, np.ndarray):
+        sk = torch.from_numpy(np.ascontiguousarray(sketches, np.uint64).view(np.int64)).cuda()
+    else:
+        sk = sketches.contiguous()
+    n, s = int(sk.shape[0]), int(sk.shape[1])
+    idx, seeds = band_parameters(s, num_tables, num_bands, seed)
+    idx = np.ascontiguousarray(idx, np.int32)
+    seeds_u = np.ascontiguousarray(seeds.astype(np.uint64))
+    stream = torch.cuda.current_stream(sk.device).cuda_stream
+    cap = max(64 * n, 1 << 20)
+    count = np.zeros(1, np.int64)
+    for _ in range(2):
+        out = torch.empty((cap, 2), dtype=torch.int32, device=sk.device)
+        st = lib.ck_lsh_candidates_device(ctx, sk.data_ptr(), n, s, num_tables, num_bands, idx.ctypes.data,
+                                          seeds_u.ctypes.data, out.data_ptr(), cap, count.ctypes.data, stream)
+        if st == _lib.CK_ERR_OUT_OF_MEMORY and int(count[0]) > cap:
+            cap = int(count[0])
+            continue
+        _lib.check(st)
+        return out[: int(count[0])]
+    raise _lib.CkError(_lib.CK_ERR_OUT_OF_MEMORY, "LSH output did not fit after resizing")
 
 
 def auto_lsh_params(threshold: float, sensitivity: str, k: int = 5) -> dict:

@@ -244,6 +244,22 @@ int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat, int64_t f
                                    int64_t *d_kmer_entries, int64_t entries_capacity,
                                    int32_t *d_kmer_freqs, int64_t *out_total, void *stream);
 
+/* LSH candidate pairs on the device (clustkit/lsh.py:20-178): d_sketches is
+ * uint64 [n][s]; band_idx_host int32 [num_tables][num_bands] and seeds_host
+ * uint64 [num_tables] are the per-table band positions and seeds (clustkit
+ * draws them with np.random.RandomState(seed), lsh.py:116-123; the caller
+ * passes them in).  Writes the de-duplicated pairs (i < j), sorted by
+ * (i, j), as int32 [count][2] to d_out_pairs and their number to *out_count;
+ * when count > capacity nothing is written, *out_count holds the count and the
+ * call returns CK_ERR_OUT_OF_MEMORY.  Identical to clustkit whenever no bucket
+ * has more than 1000 members; in a larger bucket the 1000 lowest sequence ids
+ * are kept (clustkit keeps the first 1000 of numpy's unstable argsort).
+ * Blocking; scratch ~ n*s*8 + 16*(pairs over all tables) bytes. */
+int32_t ck_lsh_candidates_device(int32_t ctx, const uint64_t *d_sketches, int64_t n, int32_t s,
+                                 int32_t num_tables, int32_t num_bands, const int32_t *band_idx_host,
+                                 const uint64_t *seeds_host, int32_t *d_out_pairs, int64_t capacity,
+                                 int64_t *out_count, void *stream);
+
 /* Phase-A k-mer scoring of a query batch (clustkit/kmer_index.py:470-534 with
  * the per-query cap of :858-902): hits per database sequence from the query's
  * valid k-mers with frequency <= freq_thresh, saturating at 32767; targets with
