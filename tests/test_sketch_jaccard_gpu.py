@@ -84,3 +84,23 @@ def test_prefilter_golden(ck, golden):
             assert m is None
         else:
             assert np.array_equal(m, g[f"t{tag}_jmask"])
+
+
+@pytest.mark.parametrize("s", [32, 64, 96, 128, 200, 256])
+def test_jaccard_sizes_duplicates_padding_vs_oracle(ck, s):
+    """Both Jaccard kernels (chunked for s a multiple of 32 up to 256, general
+    otherwise) on sketches with duplicate runs, MAX padding and shared parts."""
+    rng = np.random.default_rng(s)
+    mx = np.uint64(np.iinfo(np.uint64).max)
+    rows = []
+    for r in range(300):
+        hi = [20, 300, 10 ** 6, 2 ** 62][r % 4]
+        n_real = int(rng.integers(0, s + 1))
+        x = np.sort(rng.integers(0, hi, n_real).astype(np.uint64))
+        rows.append(np.concatenate([x, np.full(s - n_real, mx, np.uint64)]))
+    sk = np.stack(rows)
+    sk[150:] = np.sort(np.where(rng.random((150, s)) < 0.5, sk[:150], sk[150:]), 1)
+    pairs = rng.integers(0, 300, size=(20000, 2)).astype(np.int32)
+    pairs[:300, 1] = (pairs[:300, 0] + 150) % 300
+    sims, _ = batch_jaccard(pairs, sk)
+    assert np.array_equal(sims, oracle.jaccard(pairs, sk))
