@@ -431,7 +431,7 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "gpu_launches": int(launches),
     }
-    if rank == 0 and args.million == "on":
+    if rank == 0 and (args.million == "on" or (args.million == "auto" and not args.quick)):
         try:
             line["million"] = run_million(args)
         except Exception as e:
@@ -703,8 +703,9 @@ def main():
                     help="search/serving leg (auto: on for the full workload, off with --quick)")
     ap.add_argument("--uneven", choices=["auto", "on", "off", "only"], default="auto",
                     help="heavy-tailed lengths + autotuner leg (auto: on for the full workload)")
-    ap.add_argument("--million", choices=["off", "on", "only"], default="off",
-                    help="1M-sequence leg: GPU sketches, GPU LSH, pre-filter, SW in device-resident chunks")
+    ap.add_argument("--million", choices=["auto", "off", "on", "only"], default="auto",
+                    help="1M-sequence leg: GPU sketches, GPU LSH, pre-filter, SW in device-resident chunks "
+                         "(auto: on for the full workload)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
