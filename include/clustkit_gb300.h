@@ -260,6 +260,24 @@ int32_t ck_lsh_candidates_device(int32_t ctx, const uint64_t *d_sketches, int64_
                                  const uint64_t *seeds_host, int32_t *d_out_pairs, int64_t capacity,
                                  int64_t *out_count, void *stream);
 
+/* ---------------------------------------------------- graph + components
+ * The step after Align.  ck_graph_csr_device: the symmetric similarity graph
+ * of clustkit/graph.py:7-39 -- edges (i, j) and (j, i) of every pair with
+ * weight d_sims[e] (1.0 when NULL), columns ascending within a row, repeated
+ * entries summed (scipy's canonical CSR) -- into d_indptr int64 [N + 1],
+ * d_indices int32 and d_data float32 (room for 2K entries); *out_nnz = the
+ * number of entries.  ck_connected_components_device: component labels of
+ * the undirected graph on the pairs, numbered in order of each component's
+ * smallest node as scipy's connected_components does (clustkit/cluster.py:
+ * 43-55); *out_n_components, *out_rounds (may be NULL) the union-find rounds.
+ * Both blocking. */
+int32_t ck_graph_csr_device(int32_t ctx, const int32_t *d_pairs, const float *d_sims, int64_t K, int64_t N,
+                            int64_t *d_indptr, int32_t *d_indices, float *d_data, int64_t *out_nnz,
+                            void *stream);
+int32_t ck_connected_components_device(int32_t ctx, const int32_t *d_pairs, int64_t K, int64_t N,
+                                       int32_t *d_labels, int64_t *out_n_components, int32_t *out_rounds,
+                                       void *stream);
+
 /* Phase-A k-mer scoring of a query batch (clustkit/kmer_index.py:470-534 with
  * the per-query cap of :858-902): hits per database sequence from the query's
  * valid k-mers with frequency <= freq_thresh, saturating at 32767; targets with
