@@ -16,6 +16,8 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <vector>
+
 #include "ck_common.cuh"
 
 namespace ck {
@@ -210,215 +212,304 @@ __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t 
 
 constexpr int SELECT_THREADS = 1024;
 
-// One block per query: the top_k surviving targets by (count desc, id asc),
-// written in id order.  Counts are clamped to 32767 first.
-// The same selection over a query's candidate list (every listed target
-// has count >= min_hits, and every such target is listed): sort the ids
-// (bitonic, shared memory), find the threshold by histogram, compact in id
-// order with block scans.
-__device__ void select_from_list(const int32_t *__restrict__ c, const int32_t *__restrict__ list,
-                                 int32_t n, int32_t q, int32_t top_k, int32_t *__restrict__ out_targets,
-                                 int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
-    using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
-    __shared__ typename BlockScan::TempStorage scan_tmp;
-    __shared__ int32_t s_id[CAND_CAP];
-    __shared__ int32_t hist[256];
-    __shared__ int32_t sh_thr, sh_take_eq, sh_run_eq, sh_run_sel;
+// Block-wide radix selection, 8 bits per level from bit `top_shift` down, over
+// the values get(i), i < n, that are >= min_hits: sh[2] = their number; when it
+// exceeds top_k, sh[0] = thr, the top_k-th largest value, and sh[1] = the
+// number of values above thr (so top_k - sh[1] of those equal to thr are
+// taken); else sh[0] = -1.
+template <class Get>
+__device__ void radix_threshold(Get get, int32_t n, int32_t min_hits, int32_t top_k, int top_shift, int32_t *hist,
+                                int32_t *sh) {
+    const int tid = threadIdx.x;
+    if (tid == 0) { sh[0] = 0; sh[1] = 0; sh[2] = 0; }
+    uint32_t mask = 0;
+    for (int shift = top_shift; shift >= 0; shift -= 8) {
+        for (int i = tid; i < 256; i += SELECT_THREADS) hist[i] = 0;
+        __syncthreads();
+        const uint32_t prefix = (uint32_t)sh[0];
+        for (int32_t i = tid; i < n; i += SELECT_THREADS) {
+            const int32_t v = get(i);
+            if (v >= min_hits && ((uint32_t)v & mask) == prefix) atomicAdd(&hist[((uint32_t)v >> shift) & 255u], 1);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (shift == top_shift) {
+                int32_t total = 0;
+                for (int b = 0; b < 256; ++b) total += hist[b];
+                sh[2] = total;
+            }
+            if (sh[2] > top_k) {
+                int32_t above = sh[1], b = 255;
+                for (; b > 0; --b) {
+                    if (above + hist[b] >= top_k) break;
+                    above += hist[b];
+                }
+                sh[0] = (int32_t)(prefix | ((uint32_t)b << shift));
+                sh[1] = above;
+            }
+        }
+        __syncthreads();
+        if (sh[2] <= top_k) break;
+        mask |= 255u << shift;
+    }
+    __syncthreads();
+    if (tid == 0 && sh[2] <= top_k) { sh[0] = -1; sh[1] = 0; }
+    __syncthreads();
+}
+
+// Bitonic sort of n (<= 2 * CAND_CAP 32-bit, or CAND_CAP 64-bit) keys in shared memory, ascending.
+template <class K>
+__device__ void block_bitonic(K *a, int32_t n, K pad) {
     const int tid = threadIdx.x;
     int32_t P = 1;
     while (P < n) P <<= 1;
-    for (int32_t i = tid; i < P; i += SELECT_THREADS) s_id[i] = i < n ? list[i] : INT32_MAX;
+    for (int32_t i = n + tid; i < P; i += SELECT_THREADS) a[i] = pad;
     __syncthreads();
     for (int32_t k = 2; k <= P; k <<= 1) {
         for (int32_t j = k >> 1; j > 0; j >>= 1) {
             for (int32_t i = tid; i < P; i += SELECT_THREADS) {
                 const int32_t l = i ^ j;
                 if (l > i) {
-                    const int32_t a = s_id[i], b = s_id[l];
-                    if (((i & k) == 0) == (a > b)) { s_id[i] = b; s_id[l] = a; }
+                    const K x = a[i], y = a[l];
+                    if (((i & k) == 0) == (x > y)) { a[i] = y; a[l] = x; }
                 }
             }
             __syncthreads();
         }
     }
-    auto val = [&](int32_t t) { const int32_t v = c[t]; return v > 32767 ? 32767 : v; };
-    for (int i = tid; i < 256; i += SELECT_THREADS) hist[i] = 0;
-    if (tid == 0) { sh_thr = -1; sh_take_eq = 0; sh_run_eq = 0; sh_run_sel = 0; }
-    __syncthreads();
-    if (n > top_k) {
-        for (int32_t i = tid; i < n; i += SELECT_THREADS) atomicAdd(&hist[val(s_id[i]) >> 7], 1);
-        __syncthreads();
-        if (tid == 0) {
-            int32_t above = 0, b = 255;
-            for (; b >= 0; --b) {
-                if (above + hist[b] >= top_k) break;
-                above += hist[b];
-            }
-            sh_thr = b;
-            sh_take_eq = above;
-        }
-        __syncthreads();
-        const int32_t coarse = sh_thr, above_coarse = sh_take_eq;
-        for (int i = tid; i < 128; i += SELECT_THREADS) hist[i] = 0;
-        __syncthreads();
-        for (int32_t i = tid; i < n; i += SELECT_THREADS) {
-            const int32_t v = val(s_id[i]);
-            if ((v >> 7) == coarse) atomicAdd(&hist[v & 127], 1);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            int32_t above = above_coarse, lo = 127;
-            for (; lo >= 0; --lo) {
-                if (above + hist[lo] >= top_k) break;
-                above += hist[lo];
-            }
-            sh_thr = (coarse << 7) | lo;
-            sh_take_eq = top_k - above;
-        }
-        __syncthreads();
-    }
-    const int32_t thr = sh_thr, take_eq = sh_take_eq;
-    for (int32_t base = 0; base < n; base += SELECT_THREADS) {
-        const int32_t i = base + tid;
-        const int32_t t = i < n ? s_id[i] : 0;
-        const int32_t v = i < n ? val(t) : -1;
-        const int32_t is_eq = (i < n && thr >= 0 && v == thr) ? 1 : 0;
-        int32_t eq_rank, eq_tot;
-        BlockScan(scan_tmp).ExclusiveSum(is_eq, eq_rank, eq_tot);
-        __syncthreads();
-        const bool sel = i < n && (thr < 0 || v > thr || (is_eq && sh_run_eq + eq_rank < take_eq));
-        int32_t pos, sel_tot;
-        BlockScan(scan_tmp).ExclusiveSum(sel ? 1 : 0, pos, sel_tot);
-        if (sel) {
-            const int64_t o = (int64_t)q * top_k + sh_run_sel + pos;
-            out_targets[o] = t;
-            if (out_scores) out_scores[o] = v;
-        }
-        __syncthreads();
-        if (tid == 0) { sh_run_eq += eq_tot; sh_run_sel += sel_tot; }
-        __syncthreads();
-    }
-    if (tid == 0) out_n[q] = n < top_k ? n : top_k;
 }
 
+// One block per query.  The surviving targets (value >= min_hits; values are
+// the counts clamped to `clamp`): all of them in target-id order when at most
+// top_k, else the top_k by value -- ties to the lower target id -- in
+// descending value order, as clustkit's argsort(-scores) gives them
+// (kmer_index.py:893-899, :1320-1325).  Targets come from the query's
+// candidate list when it is complete (min_hits >= 1, at most CAND_CAP listed:
+// sorted by id in shared memory), else from a scan of the whole count row
+// (warp-contiguous ballot compaction).
 __global__ void __launch_bounds__(SELECT_THREADS)
-phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits,
-                      int32_t top_k, const int32_t *__restrict__ cand,
+phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t top_k,
+                      int32_t clamp, int32_t top_shift, const int32_t *__restrict__ cand,
                       const int32_t *__restrict__ n_cand, int32_t *__restrict__ out_targets,
                       int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
-    const int32_t q = blockIdx.x;
-    const int32_t *c = counts + (int64_t)q * num_db;
-    if (min_hits >= 1 && n_cand[q] <= CAND_CAP) {
-        select_from_list(c, cand + (int64_t)q * CAND_CAP, n_cand[q], q, top_k, out_targets, out_scores,
-                         out_n);
-        return;
-    }
+    using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
+    __shared__ typename BlockScan::TempStorage scan_tmp;
+    __shared__ uint64_t s_buf[CAND_CAP];  // sorted candidate ids, later the capped output's sort keys
     __shared__ int32_t hist[256];
-    __shared__ int32_t sh_thr, sh_take_eq, sh_total;
+    __shared__ int32_t sh[4], sh_run_eq, sh_run_sel;
+    const int32_t q = blockIdx.x;
     const int tid = threadIdx.x;
-    auto val = [&](int32_t t) { const int32_t v = c[t]; return v > 32767 ? 32767 : v; };
+    const int32_t *c = counts + (int64_t)q * num_db;
+    int32_t *o_t = out_targets + (int64_t)q * top_k;
+    int32_t *o_s = out_scores ? out_scores + (int64_t)q * top_k : nullptr;
+    auto val = [&](int32_t t) { const int32_t v = c[t]; return v > clamp ? clamp : v; };
+    const bool from_list = min_hits >= 1 && n_cand[q] <= CAND_CAP;
+    int32_t *s_id = (int32_t *)s_buf;
 
-    for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0;
-    __syncthreads();
-    for (int32_t t = tid; t < num_db; t += blockDim.x) {
-        const int32_t v = val(t);
-        if (v >= min_hits) atomicAdd(&hist[v >> 7], 1);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        int32_t total = 0;
-        for (int i = 0; i < 256; ++i) total += hist[i];
-        sh_total = total;
-        sh_thr = -1;  // -1: every survivor is taken
-        sh_take_eq = 0;
-        if (total > top_k) {
-            int32_t above = 0, b = 255;
-            for (; b >= 0; --b) {
-                if (above + hist[b] >= top_k) break;
-                above += hist[b];
-            }
-            sh_thr = b;        // coarse bin holding the threshold
-            sh_take_eq = above; // survivors in higher bins
-        }
-    }
-    __syncthreads();
-    if (sh_thr >= 0) {
-        const int32_t coarse = sh_thr, above_coarse = sh_take_eq;
-        for (int i = tid; i < 128; i += blockDim.x) hist[i] = 0;
+    if (from_list) {
+        const int32_t n = n_cand[q];
+        const int32_t *list = cand + (int64_t)q * CAND_CAP;
+        for (int32_t i = tid; i < n; i += SELECT_THREADS) s_id[i] = list[i];
+        block_bitonic<int32_t>(s_id, n, INT32_MAX);
+        radix_threshold([&](int32_t i) { return val(s_id[i]); }, n, min_hits, top_k, top_shift, hist, sh);
+        const int32_t thr = sh[0], take_eq = top_k - sh[1];
+        if (tid == 0) { sh_run_eq = 0; sh_run_sel = 0; }
         __syncthreads();
-        for (int32_t t = tid; t < num_db; t += blockDim.x) {
-            const int32_t v = val(t);
-            if (v >= min_hits && (v >> 7) == coarse) atomicAdd(&hist[v & 127], 1);
+        for (int32_t base = 0; base < n; base += SELECT_THREADS) {
+            const int32_t i = base + tid;
+            const int32_t t = i < n ? s_id[i] : 0;
+            const int32_t v = i < n ? val(t) : -1;
+            const int32_t is_eq = (i < n && thr >= 0 && v == thr) ? 1 : 0;
+            int32_t eq_rank, eq_tot;
+            BlockScan(scan_tmp).ExclusiveSum(is_eq, eq_rank, eq_tot);
+            __syncthreads();
+            const bool sel = i < n && (thr < 0 || v > thr || (is_eq && sh_run_eq + eq_rank < take_eq));
+            int32_t pos, sel_tot;
+            BlockScan(scan_tmp).ExclusiveSum(sel ? 1 : 0, pos, sel_tot);
+            if (sel) {
+                o_t[sh_run_sel + pos] = t;
+                if (o_s) o_s[sh_run_sel + pos] = v;
+            }
+            __syncthreads();
+            if (tid == 0) { sh_run_eq += eq_tot; sh_run_sel += sel_tot; }
+            __syncthreads();
         }
+    } else {
+        radix_threshold(val, num_db, min_hits, top_k, top_shift, hist, sh);
+        const int32_t thr = sh[0], take_eq = top_k - sh[1];
+        const int warp = tid >> 5, lane = tid & 31;
+        constexpr int NW = SELECT_THREADS / 32;
+        const int32_t chunk = ((num_db + NW - 1) / NW + 31) & ~31;
+        const int32_t b0 = warp * chunk;
+        const int32_t b1 = min(num_db, b0 + chunk);
+        const uint32_t lt = (1u << lane) - 1u;
+        int32_t n_strict = 0, n_eq = 0;
+        for (int32_t base = b0; base < b1; base += 32) {
+            const int32_t t = base + lane;
+            const int32_t v = t < b1 ? val(t) : -1;
+            const bool surv = t < b1 && v >= min_hits;
+            n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v > thr)));
+            n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v == thr));
+        }
+        __shared__ int32_t w_strict[NW], w_eq[NW], w_eq_base[NW], w_out_base[NW];
+        if (lane == 0) { w_strict[warp] = n_strict; w_eq[warp] = n_eq; }
         __syncthreads();
         if (tid == 0) {
-            int32_t above = above_coarse, lo = 127;
-            for (; lo >= 0; --lo) {
-                if (above + hist[lo] >= top_k) break;
-                above += hist[lo];
+            int32_t eq_acc = 0, out_acc = 0;
+            for (int w = 0; w < NW; ++w) {
+                w_eq_base[w] = eq_acc;
+                w_out_base[w] = out_acc;
+                int32_t take = take_eq - eq_acc;
+                take = take < 0 ? 0 : (take > w_eq[w] ? w_eq[w] : take);
+                eq_acc += w_eq[w];
+                out_acc += w_strict[w] + (thr >= 0 ? take : 0);
             }
-            sh_thr = (coarse << 7) | lo;     // exact threshold count
-            sh_take_eq = top_k - above;      // how many of the ties at the threshold
         }
         __syncthreads();
-    }
-    const int32_t thr = sh_thr, take_eq = sh_take_eq;
-    // Ordered compaction.  Warp w owns ids [w * chunk, (w + 1) * chunk), read
-    // 32 at a time (coalesced); a first pass counts its strict survivors
-    // (v > thr) and its ties (v == thr), one prefix over the 32 warps gives
-    // each warp its tie rank base and output base, a second pass writes.
-    // Ties are taken in id order, the first take_eq of them.
-    const int warp = tid >> 5, lane = tid & 31;
-    constexpr int NW = SELECT_THREADS / 32;
-    const int32_t chunk = ((num_db + NW - 1) / NW + 31) & ~31;
-    const int32_t b0 = warp * chunk;
-    const int32_t b1 = min(num_db, b0 + chunk);
-    const uint32_t lt = (1u << lane) - 1u;
-    int32_t n_strict = 0, n_eq = 0;
-    for (int32_t base = b0; base < b1; base += 32) {
-        const int32_t t = base + lane;
-        const int32_t v = t < b1 ? val(t) : -1;
-        const bool surv = t < b1 && v >= min_hits;
-        n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v > thr)));
-        n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v == thr));
-    }
-    __shared__ int32_t w_strict[NW], w_eq[NW], w_eq_base[NW], w_out_base[NW];
-    if (lane == 0) { w_strict[warp] = n_strict; w_eq[warp] = n_eq; }
-    __syncthreads();
-    if (tid == 0) {
-        int32_t eq_acc = 0, out_acc = 0;
-        for (int w = 0; w < NW; ++w) {
-            w_eq_base[w] = eq_acc;
-            w_out_base[w] = out_acc;
-            int32_t take = take_eq - eq_acc;
-            take = take < 0 ? 0 : (take > w_eq[w] ? w_eq[w] : take);
-            eq_acc += w_eq[w];
-            out_acc += w_strict[w] + (thr >= 0 ? take : 0);
+        int32_t eq_seen = w_eq_base[warp], written = w_out_base[warp];
+        for (int32_t base = b0; base < b1; base += 32) {
+            const int32_t t = base + lane;
+            const int32_t v = t < b1 ? val(t) : -1;
+            const bool surv = t < b1 && v >= min_hits;
+            const bool strict = surv && (thr < 0 || v > thr);
+            const bool is_eq = surv && thr >= 0 && v == thr;
+            const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
+            const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
+            const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
+            if (sel) {
+                const int32_t at = written + __popc(sel_b & lt);
+                o_t[at] = t;
+                if (o_s) o_s[at] = v;
+            }
+            eq_seen += __popc(eq_b);
+            written += __popc(sel_b);
         }
     }
+    const int32_t total = sh[2];
+    const int32_t n_out = total < top_k ? total : top_k;
     __syncthreads();
-    int32_t eq_seen = w_eq_base[warp], written = w_out_base[warp];
-    for (int32_t base = b0; base < b1; base += 32) {
-        const int32_t t = base + lane;
-        const int32_t v = t < b1 ? val(t) : -1;
-        const bool surv = t < b1 && v >= min_hits;
-        const bool strict = surv && (thr < 0 || v > thr);
-        const bool is_eq = surv && thr >= 0 && v == thr;
-        const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
-        const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
-        const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
-        if (sel) {
-            const int64_t o = (int64_t)q * top_k + written + __popc(sel_b & lt);
-            out_targets[o] = t;
-            if (out_scores) out_scores[o] = v;
+    // capped: the kept targets in descending value order, ties by id
+    if (total > top_k && top_k <= CAND_CAP) {
+        for (int32_t i = tid; i < n_out; i += SELECT_THREADS) {
+            const int32_t t = o_t[i];
+            s_buf[i] = ((uint64_t)(uint32_t)(0x7fffffff - val(t)) << 32) | (uint32_t)t;
         }
-        eq_seen += __popc(eq_b);
-        written += __popc(sel_b);
+        block_bitonic<uint64_t>(s_buf, n_out, ~0ull);
+        for (int32_t i = tid; i < n_out; i += SELECT_THREADS) {
+            const int32_t t = (int32_t)(s_buf[i] & 0xffffffffu);
+            o_t[i] = t;
+            if (o_s) o_s[i] = 0x7fffffff - (int32_t)(s_buf[i] >> 32);
+        }
     }
-    if (tid == 0) out_n[q] = sh_total < top_k ? sh_total : top_k;
+    if (tid == 0) out_n[q] = n_out;
+}
+
+// ----------------------------------------------------------------- similar k-mers
+// clustkit/kmer_index.py:1187-1291: with k = 5 every 5-mer whose BLOSUM62
+// column sum against a query 5-mer reaches the threshold T adds that sum to
+// each target of its posting list (frequency in (0, freq_thresh]).  Stage 1:
+// one thread per (query position, first two residues) enumerates the rest by
+// branch and bound -- the same pruning bound, max remaining row scores -- and
+// lists (5-mer value, score) per query, in a counting pass and then an
+// emitting pass; stage 2: a warp per listed 5-mer walks its posting list.
+constexpr int32_t NB_PREFIX = 400;
+
+// Work item (q, t): query position p = t / 400, first residues (a0, a1) =
+// (t % 400) / 20, t % 20; items are laid out q * stride + t.  The counting
+// pass writes each item's number of listed 5-mers, the emitting pass writes
+// them from the item's exclusive offset on (same enumeration order).
+template <bool EMIT>
+__global__ void nbr_enum_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len,
+                                const int64_t *__restrict__ qoff, const int32_t *__restrict__ qlen,
+                                const int8_t *__restrict__ sub, int32_t T, const int32_t *__restrict__ kmer_freqs,
+                                int32_t freq_thresh, int64_t stride, int64_t *__restrict__ item,
+                                uint64_t *__restrict__ list, int32_t *err) {
+    __shared__ int32_t S[400];
+    __shared__ int32_t mx[20];
+    for (int i = threadIdx.x; i < 400; i += blockDim.x) S[i] = sub[i];
+    __syncthreads();
+    if (threadIdx.x < 20) {
+        int32_t m = -1000;
+        for (int j = 0; j < 20; ++j) m = max(m, S[threadIdx.x * 20 + j]);
+        mx[threadIdx.x] = m;
+    }
+    __syncthreads();
+    const int32_t q = blockIdx.y;
+    const int32_t L = qlen[q];
+    const int64_t o = qoff[q];
+    const bool bad = L < 0 || o < 0 || o + L > qflat_len;
+    if (bad && threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERRBIT_SEQ_EXTENT);
+    const uint8_t *sq = qflat + (bad ? 0 : o);
+    const int64_t work = bad ? 0 : (int64_t)(L >= 5 ? L - 4 : 0) * NB_PREFIX;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < stride;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t found = 0;
+        int64_t at = EMIT ? item[(int64_t)q * stride + t] : 0;
+        if (t < work) {
+            const int32_t p = (int32_t)(t / NB_PREFIX), pre = (int32_t)(t % NB_PREFIX);
+            const int32_t a0 = pre / 20, a1 = pre % 20;
+            const int32_t q0 = sq[p], q1 = sq[p + 1], q2 = sq[p + 2], q3 = sq[p + 3], q4 = sq[p + 4];
+            if (q0 < 20 && q1 < 20 && q2 < 20 && q3 < 20 && q4 < 20) {
+                const int32_t m4 = mx[q4], m34 = mx[q3] + m4, m234 = mx[q2] + m34;
+                const int32_t s0 = S[q0 * 20 + a0];
+                const int32_t s1 = s0 + S[q1 * 20 + a1];
+                if (s0 + mx[q1] + m234 >= T && s1 + m234 >= T) {
+                    const int32_t v1 = a0 * 160000 + a1 * 8000;
+                    for (int32_t a2 = 0; a2 < 20; ++a2) {
+                        const int32_t s2 = s1 + S[q2 * 20 + a2];
+                        if (s2 + m34 < T) continue;
+                        for (int32_t a3 = 0; a3 < 20; ++a3) {
+                            const int32_t s3 = s2 + S[q3 * 20 + a3];
+                            if (s3 + m4 < T) continue;
+                            const int32_t v3 = v1 + a2 * 400 + a3 * 20;
+                            for (int32_t a4 = 0; a4 < 20; ++a4) {
+                                const int32_t s4 = s3 + S[q4 * 20 + a4];
+                                if (s4 < T) continue;
+                                const int32_t v = v3 + a4;
+                                const int32_t f = kmer_freqs[v];
+                                if (f == 0 || f > freq_thresh) continue;
+                                if (EMIT) list[at++] = ((uint64_t)(uint32_t)s4 << 32) | (uint32_t)v;
+                                else ++found;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (!EMIT) item[(int64_t)q * stride + t] = found;
+    }
+}
+
+// A warp per listed 5-mer: its posting list's targets each gain its score.
+// Query q's entries are list[item[q * stride] .. item[(q + 1) * stride]).
+__global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int64_t *__restrict__ item,
+                                    int64_t stride, const int64_t *__restrict__ kmer_offsets,
+                                    const int64_t *__restrict__ kmer_entries, int32_t num_db,
+                                    int32_t *__restrict__ counts, int32_t min_hits, int32_t *__restrict__ cand,
+                                    int32_t *__restrict__ n_cand, int32_t *err) {
+    const int32_t q = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int64_t e0 = item[(int64_t)q * stride], e1 = item[(int64_t)(q + 1) * stride];
+    int32_t *c = counts + (int64_t)q * num_db;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = e0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); e < e1; e += warps) {
+        const uint64_t x = list[e];
+        const int32_t v = (int32_t)(x & 0xffffffffu), w = (int32_t)(x >> 32);
+        const int64_t b = kmer_offsets[v], en = kmer_offsets[v + 1];
+        for (int64_t h = b + lane; h < en; h += 32) {
+            const int32_t t = (int32_t)(kmer_entries[h] >> 32);
+            if (t < 0 || t >= num_db) { atomicOr(err, ERRBIT_PAIR_INDEX); continue; }
+            const int32_t old = atomicAdd(&c[t], w);
+            if (old < min_hits && old + w >= min_hits) {
+                const int32_t pos = atomicAdd(&n_cand[q], 1);
+                if (pos < CAND_CAP) cand[(int64_t)q * CAND_CAP + pos] = t;
+            }
+        }
+    }
 }
 
 struct PhaseAArgs {
+    const int8_t *sub_host; int32_t score_thresh;  // similar k-mers when sub_host != nullptr
     const uint8_t *qflat; int64_t qflat_len; const int64_t *qoff; const int32_t *qlen; int32_t nq; int32_t max_qlen;
     int32_t k, alpha; const int64_t *kmer_offsets; const int64_t *kmer_entries;
     const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
@@ -440,18 +531,63 @@ static int32_t phase_a_impl(void *pv) {
     CK_CUDA(cudaMemsetAsync(counts, 0, nc * 4, a.st));
     CK_CUDA(cudaMemsetAsync(n_cand, 0, (size_t)a.nq * 4, a.st));
     const int32_t npos = a.max_qlen - a.k + 1;
-    if (npos > 0) {
-        int bx = (npos + 7) / 8;  // 8 warps per block
-        if (bx > 16) bx = 16;
-        dim3 grid((unsigned)bx, (unsigned)a.nq);
-        phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha,
-                                                      a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
-                                                      a.freq_thresh, a.num_db, counts, a.min_hits, cand,
-                                                      n_cand, err);
-        CK_CUDA(cudaGetLastError());
+    int32_t clamp = 32767, top_shift = 8;  // clustkit's int16 hit counters
+    if (!a.sub_host) {
+        if (npos > 0) {
+            int bx = (npos + 7) / 8;  // 8 warps per block
+            if (bx > 16) bx = 16;
+            dim3 grid((unsigned)bx, (unsigned)a.nq);
+            phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha,
+                                                          a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
+                                                          a.freq_thresh, a.num_db, counts, a.min_hits, cand,
+                                                          n_cand, err);
+            CK_CUDA(cudaGetLastError());
+        }
+    } else {
+        clamp = INT32_MAX;  // score-weighted int32 sums
+        top_shift = 24;
+        const int8_t *d_sub = device_sub_matrix(a.sub_host, &status);
+        if (!d_sub) return status;
+        if (npos > 0) {
+            // items: nq x stride, plus one trailing entry that ends the last query's range
+            const int64_t stride = (int64_t)npos * NB_PREFIX;
+            const int64_t n_items = (int64_t)a.nq * stride + 1;
+            int64_t *item = (int64_t *)scratch(SLOT_SEARCH_TMP0, (size_t)n_items * 8, &status);
+            if (!item) return status;
+            int bx = (int)((stride + 255) / 256);
+            if (bx > 64) bx = 64;
+            const dim3 grid((unsigned)bx, (unsigned)a.nq);
+            nbr_enum_kernel<false><<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, d_sub,
+                                                            a.score_thresh, a.kmer_freqs, a.freq_thresh, stride,
+                                                            item, nullptr, err);
+            CK_CUDA(cudaGetLastError());
+            CK_CUDA(cudaMemsetAsync(item + n_items - 1, 0, 8, a.st));
+            size_t tb = 0;
+            CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, item, item, n_items, a.st));
+            void *tmp = scratch(SLOT_SORT_TEMP, tb, &status);
+            if (!tmp) return status;
+            CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, item, item, n_items, a.st));
+            int64_t total = 0;
+            CK_CUDA(cudaMemcpyAsync(&total, item + n_items - 1, 8, cudaMemcpyDeviceToHost, a.st));
+            CK_CUDA(cudaStreamSynchronize(a.st));
+            uint64_t *list = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)(total > 0 ? total : 1) * 8, &status);
+            if (!list) return status;
+            nbr_enum_kernel<true><<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, d_sub,
+                                                           a.score_thresh, a.kmer_freqs, a.freq_thresh, stride,
+                                                           item, list, err);
+            CK_CUDA(cudaGetLastError());
+            int by = (int)((total / (a.nq > 0 ? a.nq : 1) + 7) / 8);
+            if (by > 4 * sm_count()) by = 4 * sm_count();
+            if (by < 1) by = 1;
+            nbr_postings_kernel<<<dim3((unsigned)by, (unsigned)a.nq), 256, 0, a.st>>>(
+                list, item, stride, a.kmer_offsets, a.kmer_entries, a.num_db, counts, a.min_hits, cand, n_cand,
+                err);
+            CK_CUDA(cudaGetLastError());
+        }
     }
-    phase_a_select_kernel<<<a.nq, SELECT_THREADS, 0, a.st>>>(counts, a.num_db, a.min_hits, a.top_k, cand,
-                                                             n_cand, a.out_targets, a.out_scores, a.out_n);
+    phase_a_select_kernel<<<a.nq, SELECT_THREADS, 0, a.st>>>(counts, a.num_db, a.min_hits, a.top_k, clamp,
+                                                             top_shift, cand, n_cand, a.out_targets,
+                                                             a.out_scores, a.out_n);
     CK_CUDA(cudaGetLastError());
     return CK_OK;
 }
@@ -495,8 +631,30 @@ extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat,
         set_error(CK_ERR_INVALID_ARGUMENT, "phase A: bad arguments");
         return CK_ERR_INVALID_ARGUMENT;
     }
-    PhaseAArgs a{d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha, d_kmer_offsets, d_kmer_entries,
+    PhaseAArgs a{nullptr, 0, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha, d_kmer_offsets, d_kmer_entries,
                  d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k, d_out_targets, d_out_scores,
                  d_out_n, (cudaStream_t)stream};
+    return run_in_context(ctx, phase_a_impl, &a);
+}
+
+extern "C" int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
+                                                    const int64_t *d_qoffsets, const int32_t *d_qlengths,
+                                                    int32_t nq, int32_t max_qlen, const int8_t *sub_matrix_host,
+                                                    int32_t kmer_score_thresh, const int64_t *d_kmer_offsets,
+                                                    const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
+                                                    int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
+                                                    int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
+                                                    int32_t *d_out_n, void *stream) {
+    std::lock_guard<std::mutex> lock(library_mutex());
+    reset_thread_status();
+    if (nq < 0 || nq > 65535 || qflat_len < 0 || top_k < 1 || num_db < 0 || !sub_matrix_host ||
+        kmer_score_thresh < 1 || !d_out_targets || !d_out_n || (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) ||
+        !d_kmer_offsets || !d_kmer_freqs) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "similar k-mer phase A: bad arguments");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    PhaseAArgs a{sub_matrix_host, kmer_score_thresh, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, 5,
+                 20, d_kmer_offsets, d_kmer_entries, d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k,
+                 d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream};
     return run_in_context(ctx, phase_a_impl, &a);
 }

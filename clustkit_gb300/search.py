@@ -1,17 +1,20 @@
 """Query-vs-database search on the GPU, batch and continuous-batching serving.
 
 Mirrors the k-mer search of clustkit (clustkit/kmer_index.py:1475-2349) in
-the configuration it takes with ``min_diag_hits <= 1`` and no similar-k-mer
-scoring: k-mer inverted index (k = 5, clustkit's CSR layout,
-kmer_index.py:117-166), Phase-A hit counting with the frequency cap
-(:451-534), at most ``max_cands`` candidates per query (:893-902), banded
-Smith-Waterman with a positive score as pass (:2271-2280, pairwise.py:636-681),
-rank ``0.267 * score - ln(qlen * tlen)`` (:2318-2323) and the top-k hits per
-query (clustkit/search.py:727-800).
+its two k-mer scoring modes with ``min_diag_hits <= 1``: k-mer inverted index
+(k = 5, clustkit's CSR layout, kmer_index.py:117-166); either BLOSUM62
+similar-k-mer scoring (``kmer_score_thresh > 0``, clustkit's default 13:
+every 5-mer scoring >= the threshold against a query 5-mer adds its score,
+:1187-1328) or exact Phase-A hit counting (``kmer_score_thresh = 0``,
+:451-534), both with the frequency cap; at most ``max_cands`` candidates per
+query (:893-902, :1320-1328); banded Smith-Waterman with a positive score as
+pass (:2271-2280, pairwise.py:636-681); rank ``0.267 * score - ln(qlen *
+tlen)`` (:2318-2323) and the top-k hits per query (clustkit/search.py:727-800).
 
 Differences, by design:
-* candidates above the cap are chosen by hit count with ties to the lower
-  target id (clustkit orders them with numpy's unstable quicksort);
+* candidates above the cap are the top ones by score, in score order as
+  clustkit gives them, with ties to the lower target id (clustkit's order
+  among equal scores is numpy's unstable quicksort);
 * the band width is fixed when the database is loaded
   (``max(20, 0.3 * p95(database lengths))``) instead of being recomputed per
   query batch, so a query's result does not depend on which other queries
@@ -237,7 +240,7 @@ class _Slot:
         hl[nq:n_all] = 0
         return nq, lens, tot
 
-    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, min_total_hits: int):
+    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, min_total_hits: int, kmer_score_thresh: int = 0):
         """The device pipeline of a batch of nq queries on this slot's stream:
         H2D, Phase A, pair list, SW, D2H.  No host synchronisation, so it can
         be captured in a CUDA graph."""
@@ -254,11 +257,18 @@ class _Slot:
         qoff_ptr = db.d_offsets.data_ptr() + self.seq0 * 8
         qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
         self._mark(1)
-        _lib.check(lib.ck_search_phase_a_device(
-            self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
-            db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
-            db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
-            self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+        if kmer_score_thresh > 0:  # BLOSUM62 similar k-mers (k = 5), clustkit's default scoring
+            _lib.check(lib.ck_search_phase_a_similar_device(
+                self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen, _SUB.ctypes.data,
+                int(kmer_score_thresh), db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
+                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+        else:
+            _lib.check(lib.ck_search_phase_a_device(
+                self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
+                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
+                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
         self._mark(2)
         # dense pair list: (query, target) or (empty, empty) past a query's candidates
         q = self.d_slotq[:M]
@@ -303,12 +313,14 @@ class _Slot:
         self.graph_min_hits = int(min_total_hits)
         self.stream.synchronize()
 
-    def launch(self, queries: list[np.ndarray], min_total_hits: int):
-        """Enqueue the whole pipeline for a batch on this slot's stream."""
+    def launch(self, queries: list[np.ndarray], min_total_hits: int, kmer_score_thresh: int = 0):
+        """Enqueue the whole pipeline for a batch on this slot's stream.  The
+        similar-k-mer scoring sizes its neighbour list on the host, so it runs
+        call by call; exact k-mer batches replay the captured graphs."""
         torch = _torch()
         db = self.db
         bucket = None
-        if self.graphs and int(min_total_hits) == self.graph_min_hits:
+        if self.graphs and int(min_total_hits) == self.graph_min_hits and kmer_score_thresh <= 0:
             bucket = next((b for b in sorted(self.graphs) if b >= len(queries)), None)
         if bucket is not None:
             nq, lens, tot = self._fill_host(queries, pad_to=bucket)
@@ -318,7 +330,7 @@ class _Slot:
         else:
             nq, lens, tot = self._fill_host(queries)
             with torch.cuda.stream(self.stream):
-                self._enqueue(nq, int(lens.max() if nq else 0), tot, min_total_hits)
+                self._enqueue(nq, int(lens.max() if nq else 0), tot, min_total_hits, kmer_score_thresh)
                 self.event.record(self.stream)
         self.batch = (nq, lens)
 
@@ -357,7 +369,8 @@ class _Slot:
 
 
 def search_batch(db: DeviceDatabase, queries: list[np.ndarray], top_k: int = 10,
-                 max_cands: int = 500, min_total_hits: int = 2, slot: _Slot | None = None):
+                 max_cands: int = 500, min_total_hits: int = 2, slot: _Slot | None = None,
+                 kmer_score_thresh: int = 13):
     """Synchronous search of a list of encoded queries; list of hit lists."""
     own = slot is None
     if own:
@@ -366,7 +379,7 @@ def search_batch(db: DeviceDatabase, queries: list[np.ndarray], top_k: int = 10,
         res = []
         for s in range(0, len(queries), db.arena_queries):
             chunk = queries[s:s + db.arena_queries]
-            slot.launch(chunk, min_total_hits)
+            slot.launch(chunk, min_total_hits, kmer_score_thresh)
             slot.event.synchronize()
             for qi, hits in enumerate(slot.results(top_k)):
                 for h in hits:
@@ -398,12 +411,14 @@ class SearchServer:
     """
 
     def __init__(self, db: DeviceDatabase, top_k: int = 10, max_cands: int = 500,
-                 min_total_hits: int = 2, max_batch: int | None = None, use_graphs: bool = True):
+                 min_total_hits: int = 2, max_batch: int | None = None, use_graphs: bool = True,
+                 kmer_score_thresh: int = 13):
         torch = _torch()
         self.db = db
         self.top_k = top_k
         self.max_cands = max_cands
         self.min_total_hits = min_total_hits
+        self.kmer_score_thresh = int(kmer_score_thresh)
         self.max_batch = min(max_batch or db.arena_queries, db.arena_queries)
         free, _ = torch.cuda.mem_get_info(db.dev)
         # per slot: counts scratch + pair/SW buffers + the SW kernel's window scratch
@@ -421,9 +436,9 @@ class SearchServer:
         # CUDA graphs (one replay per batch), or warm it with one batch
         warm = [np.arange(40, dtype=np.uint8) % 20]
         for s in self.slots:
-            if use_graphs:
+            if use_graphs and self.kmer_score_thresh <= 0:
                 s.capture_graphs(min_total_hits)
-            s.launch(warm, min_total_hits)
+            s.launch(warm, min_total_hits, self.kmer_score_thresh)
             s.event.synchronize()
             s.results(1)
 
@@ -496,7 +511,7 @@ class SearchServer:
             if batch:
                 slot = self.free.pop()
                 try:
-                    slot.launch([r.query for r in batch], self.min_total_hits)
+                    slot.launch([r.query for r in batch], self.min_total_hits, self.kmer_score_thresh)
                     self.busy.append((slot, batch))
                 except Exception as e:
                     for r in batch:

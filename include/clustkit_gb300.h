@@ -260,6 +260,23 @@ int32_t ck_lsh_candidates_device(int32_t ctx, const uint64_t *d_sketches, int64_
                                  const uint64_t *seeds_host, int32_t *d_out_pairs, int64_t capacity,
                                  int64_t *out_count, void *stream);
 
+/* The same with clustkit's BLOSUM62 similar-k-mer scoring (k = 5,
+ * clustkit/kmer_index.py:1187-1328, its default search mode with
+ * kmer_score_thresh = 13): every 5-mer whose column-sum score under
+ * sub_matrix_host (int8 [20][20], row = query residue) against a query 5-mer
+ * is >= kmer_score_thresh adds that score to each target of its posting list
+ * (k-mers with frequency 0 or above freq_thresh skipped); sums are int32, not
+ * saturated; survivors and cap as above.  Blocking (it sizes its neighbour
+ * list on the host). */
+int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
+                                         const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,
+                                         int32_t max_qlen, const int8_t *sub_matrix_host,
+                                         int32_t kmer_score_thresh, const int64_t *d_kmer_offsets,
+                                         const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
+                                         int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
+                                         int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
+                                         int32_t *d_out_n, void *stream);
+
 /* ---------------------------------------------------- graph + components
  * The step after Align.  ck_graph_csr_device: the symmetric similarity graph
  * of clustkit/graph.py:7-39 -- edges (i, j) and (j, i) of every pair with
@@ -287,7 +304,9 @@ int32_t ck_connected_components_device(int32_t ctx, const int32_t *d_pairs, int6
  * their number to d_out_n[q].  Every query's extent is checked against
  * qflat_len on the device (CK_ERR_OUT_OF_RANGE, reported by ck_ctx_status);
  * max_qlen sizes the grid only.  Uses nq * num_db * 4 bytes of context
- * scratch. */
+ * scratch.  When more than top_k survive, the top_k are written in descending
+ * count order (ties: lower id first), as clustkit's argsort(-scores) orders
+ * them; otherwise in id order. */
 int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                  const int64_t *d_qoffsets,
                                  const int32_t *d_qlengths, int32_t nq, int32_t max_qlen, int32_t k,

@@ -8,8 +8,13 @@ project root.
 * ``compute_freq_threshold`` -- clustkit/kmer_index.py:451-463
 * ``phase_a``               -- clustkit/kmer_index.py:470-534 (Phase A only,
   the path taken when min_diag_hits <= 1, :832-850) with the per-query cap of
-  :893-902; ties at the cap go to the lower target id (clustkit's
-  ``np.argsort(-scores)`` leaves tie order to numpy's unstable quicksort)
+  :893-902: above the cap the top targets in score order, ties to the lower
+  target id (clustkit's ``np.argsort(-scores)`` leaves tie order to numpy's
+  unstable quicksort)
+* ``phase_a_similar``       -- the k = 5 BLOSUM62-neighbour scoring of
+  clustkit/kmer_index.py:1187-1291 (every 5-mer whose column-sum score against
+  the query 5-mer is >= the threshold adds that score per posting) with the
+  cap of :1320-1328
 * ``rank_hits``             -- the E-value-style rank of
   clustkit/kmer_index.py:2318-2323 and the top-k collection of
   clustkit/search.py:727-800
@@ -76,11 +81,45 @@ def phase_a(query, k, alpha, kmer_offsets, kmer_entries, kmer_freqs, freq_thresh
     counts = np.minimum(counts, 32767)
     ids = np.nonzero(counts >= min_total_hits)[0]
     sc = counts[ids]
+    return _cap(ids, sc, top_k)
+
+
+def _cap(ids, sc, top_k):
+    """Survivors in id order; above top_k the top_k by score in score order
+    (clustkit's argsort(-scores), kmer_index.py:893-899), ties by id."""
     if len(ids) > top_k:
         order = np.lexsort((ids, -sc))[:top_k]
-        keep = np.sort(ids[order])
-        return keep.astype(np.int32), counts[keep].astype(np.int32)
+        return ids[order].astype(np.int32), sc[order].astype(np.int32)
     return ids.astype(np.int32), sc.astype(np.int32)
+
+
+def neighbours_k5(q5, sub, T):
+    """(values, scores) of every 5-mer with sum_i sub[q_i, a_i] >= T."""
+    S = np.asarray(sub, np.int64)
+    s = (S[q5[0]][:, None, None, None, None] + S[q5[1]][None, :, None, None, None]
+         + S[q5[2]][None, None, :, None, None] + S[q5[3]][None, None, None, :, None]
+         + S[q5[4]][None, None, None, None, :])
+    idx = np.nonzero(s.reshape(-1) >= T)[0]
+    return idx.astype(np.int64), s.reshape(-1)[idx]
+
+
+def phase_a_similar(query, kmer_offsets, kmer_entries, kmer_freqs, freq_thresh, num_db, min_total_hits,
+                    top_k, sub, T):
+    """Survivors (ids, score-weighted counts) of the neighbour scoring, capped as above."""
+    q = np.asarray(query)
+    counts = np.zeros(num_db, np.int64)
+    for p in range(len(q) - 4):
+        q5 = q[p:p + 5].astype(np.int64)
+        if (q5 >= 20).any():
+            continue
+        vals, sc = neighbours_k5(q5, sub, T)
+        f = kmer_freqs[vals]
+        ok = (f > 0) & (f <= freq_thresh)
+        for v, w in zip(vals[ok], sc[ok]):
+            t = (kmer_entries[kmer_offsets[v]:kmer_offsets[v + 1]] >> 32).astype(np.int64)
+            np.add.at(counts, t, int(w))
+    ids = np.nonzero(counts >= min_total_hits)[0]
+    return _cap(ids, counts[ids], top_k)
 
 
 def rank_hits(pairs, sims, scores, q_lengths, t_lengths, nq, top_k):

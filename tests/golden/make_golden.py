@@ -313,6 +313,35 @@ def make_search_golden(rpw):
             ht.append(int(h.target_id[1:]))
             hid.append(h.identity)
             hsc.append(h.score)
+    # BLOSUM62-neighbour scoring (clustkit's default search mode, kmer_score_thresh = 13)
+    # on a subset of the queries: the pure-Python run of the neighbour loops is slow
+    sim_q = [0, 1, 2, 3, 10, 11, 18, 19]
+    sim = {"sim_queries": np.array(sim_q, np.int32)}
+    t0 = time.time()
+    for qi in sim_q:
+        ids, sc = rki._score_query_similar_k5(qs[qi], np.int32(len(qs[qi])), koff, kent, kfreq, np.int32(thr),
+                                              np.int32(db.n), np.int32(2), rpw.BLOSUM62, np.int32(13))
+        sim[f"q{qi}_sim_ids"] = np.asarray(ids, np.int32)
+        sim[f"q{qi}_sim_scores"] = np.asarray(sc, np.int32)
+    print(f"similar-k-mer phase A {time.time()-t0:.1f}s")
+    sq_flat, sq_off, sq_len = pack([qs[i] for i in sim_q])
+    t0 = time.time()
+    res2 = rki.search_kmer_index(idx, _dataset(sq_flat, sq_off, sq_len, "q"), threshold=0.0, top_k=5,
+                                 band_width=None, min_total_hits=2, min_diag_hits=1, max_cands_per_query=100000,
+                                 freq_percentile=95.0, kmer_score_thresh=13, local_alignment=True,
+                                 evalue_normalize=True)
+    print(f"search_kmer_index (similar k-mers) {time.time()-t0:.1f}s, {sum(len(h) for h in res2.hits)} hits")
+    sq, st_, sid, ssc = [], [], [], []
+    for qi, hl in enumerate(res2.hits):
+        for h in hl:
+            sq.append(sim_q[qi])
+            st_.append(int(h.target_id[1:]))
+            sid.append(h.identity)
+            ssc.append(h.score)
+    sim.update(sim_hit_query=np.array(sq, np.int32), sim_hit_target=np.array(st_, np.int32),
+               sim_hit_identity=np.array(sid, np.float64), sim_hit_score=np.array(ssc, np.float64),
+               sim_band_width=np.int32(max(20, int(int(np.percentile(np.concatenate([sq_len, db.lengths]), 95))
+                                                   * 0.3))))
     nz = np.nonzero(kfreq)[0]
     all_len = np.concatenate([qlen, db.lengths])
     np.savez_compressed(HERE / "search_golden.npz", db_flat=db.flat, db_offsets=db.offsets,
@@ -322,7 +351,7 @@ def make_search_golden(rpw):
                         band_width=np.int32(max(20, int(int(np.percentile(all_len, 95)) * 0.3))),
                         hit_query=np.array(hq, np.int32), hit_target=np.array(ht, np.int32),
                         hit_identity=np.array(hid, np.float64), hit_score=np.array(hsc, np.float64),
-                        top_k=np.int32(5), **phase)
+                        top_k=np.int32(5), **phase, **sim)
 
 
 if __name__ == "__main__":

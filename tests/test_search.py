@@ -18,6 +18,10 @@ def _queries(g):
     return [g["q_flat"][o:o + L] for o, L in zip(g["q_offsets"], g["q_lengths"])]
 
 
+def _ref_index(g):
+    return so.build_kmer_index(g["db_flat"], g["db_offsets"], g["db_lengths"], int(g["k"]))
+
+
 def test_oracle_index_and_phase_a_match_reference(golden):
     g = golden("search_golden.npz")
     k = int(g["k"])
@@ -104,7 +108,7 @@ def test_search_batch_matches_reference(ck, golden):
     g = golden("search_golden.npz")
     db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["band_width"]),
                         arena_queries=8, arena_residues=8 * 400)
-    res = search_batch(db, _queries(g), top_k=int(g["top_k"]), max_cands=1000)
+    res = search_batch(db, _queries(g), top_k=int(g["top_k"]), max_cands=1000, kmer_score_thresh=0)
     want = _golden_hits(g)
     for hits, w in zip(res, want):
         assert [h.target for h in hits] == [x[0] for x in w]
@@ -170,8 +174,8 @@ def test_phase_a_cap_and_ties_vs_oracle(ck):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("use_graphs", [True, False])
-def test_server_results_same_alone_and_in_mix(ck, use_graphs):
+@pytest.mark.parametrize("use_graphs,thresh", [(True, 0), (False, 0), (False, 13)])
+def test_server_results_same_alone_and_in_mix(ck, use_graphs, thresh):
     """Each query's hits are identical whether it is searched alone or lands
     in concurrent batches of the continuous-batching server (slots replaying
     captured CUDA graphs, or launching the pipeline call by call)."""
@@ -183,8 +187,8 @@ def test_server_results_same_alone_and_in_mix(ck, use_graphs):
     qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 40, replace=False)]
     bg = synth.random_sequences(20, median=200, lo=40, hi=600, seed=93)
     qs += [bg.seq(i).copy() for i in range(bg.n)]
-    alone = [search_batch(db, [q], top_k=10)[0] for q in qs]
-    server = SearchServer(db, top_k=10, max_batch=7, use_graphs=use_graphs).start()
+    alone = [search_batch(db, [q], top_k=10, kmer_score_thresh=thresh)[0] for q in qs]
+    server = SearchServer(db, top_k=10, max_batch=7, use_graphs=use_graphs, kmer_score_thresh=thresh).start()
     try:
         futs = [server.submit(q) for q in qs]
         mixed = [f.result(timeout=120) for f in futs]
@@ -237,3 +241,72 @@ def test_frozen_context_refuses_to_grow(ck):
         assert np.array_equal(outs[1].cpu().numpy(), ref["scores"])
     finally:
         lib.ck_ctx_destroy(ctx)
+
+
+def test_oracle_similar_phase_a_matches_reference(golden):
+    """The numpy restatement of the BLOSUM62 similar-k-mer scoring against the
+    reference's own _score_query_similar_k5 (golden)."""
+    g = golden("search_golden.npz")
+    off, ent, fr = _ref_index(g)
+    qs = _queries(g)
+    for qi in g["sim_queries"]:
+        ids, sc = so.phase_a_similar(qs[qi], off, ent, fr, int(g["freq_thresh"]), len(g["db_lengths"]), 2,
+                                     10 ** 9, BLOSUM62, 13)
+        assert np.array_equal(ids, g[f"q{qi}_sim_ids"]), qi
+        assert np.array_equal(sc, g[f"q{qi}_sim_scores"]), qi
+
+
+@pytest.mark.gpu
+def test_similar_phase_a_and_search_match_reference(ck, golden):
+    from clustkit_gb300.search import DeviceDatabase, _Slot, search_batch
+    g = golden("search_golden.npz")
+    db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["sim_band_width"]),
+                        arena_queries=16, arena_residues=16 * 400)
+    qs = _queries(g)
+    sq = [qs[i] for i in g["sim_queries"]]
+    slot = _Slot(db, 0, 1000)
+    try:
+        slot.launch(sq, 2, 13)
+        slot.event.synchronize()
+        n = slot.h_n.numpy()[:len(sq)]
+        tg = slot.h_targets.numpy().reshape(-1, 1000)
+        for k, qi in enumerate(g["sim_queries"]):
+            assert np.array_equal(tg[k, :n[k]], g[f"q{qi}_sim_ids"]), qi
+        slot.results(5)
+    finally:
+        slot.close()
+    res = search_batch(db, sq, top_k=int(g["top_k"]), max_cands=1000, kmer_score_thresh=13)
+    got = [(int(g["sim_queries"][q]), h.target, h.identity, h.score) for q, hl in enumerate(res) for h in hl]
+    exp = list(zip(g["sim_hit_query"].tolist(), g["sim_hit_target"].tolist(), g["sim_hit_identity"].tolist(),
+                   g["sim_hit_score"].tolist()))
+    assert len(got) == len(exp)
+    for a, b in zip(got, exp):
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.float32(a[2]) == np.float32(b[2]) and np.float32(a[3]) == np.float32(b[3])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("thresh", [11, 13, 15])
+def test_similar_phase_a_cap_vs_oracle(ck, thresh):
+    """Capped and uncapped outputs of the neighbour scoring against the oracle,
+    on a database large enough that most queries hit the cap."""
+    from clustkit_gb300.search import DeviceDatabase, _Slot
+    db_set = synth.generate_families(200, 8, median=150, lo=40, hi=400, seed=thresh)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=8, arena_residues=8 * 500)
+    off, ent, fr = db.index_arrays()
+    rng = np.random.default_rng(thresh)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 5, replace=False)]
+    qs += [synth.random_sequences(1, median=120, lo=60, hi=200, seed=thresh + 1).seq(0).copy()]
+    for cap in (7, 300, 5000):
+        slot = _Slot(db, 0, cap)
+        try:
+            slot.launch(qs, 2, thresh)
+            slot.event.synchronize()
+            n = slot.h_n.numpy()[:len(qs)]
+            tg = slot.h_targets.numpy().reshape(-1, cap)
+            for qi, q in enumerate(qs):
+                ids, _ = so.phase_a_similar(q, off, ent, fr, db.freq_thresh, db_set.n, 2, cap, BLOSUM62, thresh)
+                assert np.array_equal(tg[qi, :n[qi]], ids), (cap, qi)
+            slot.results(3)
+        finally:
+            slot.close()
