@@ -276,7 +276,7 @@ def test_similar_phase_a_and_search_match_reference(ck, golden):
     finally:
         slot.close()
     res = search_batch(db, sq, top_k=int(g["top_k"]), max_cands=1000, kmer_score_thresh=13)
-    got = [(int(g["sim_queries"][q]), h.target, h.identity, h.score) for q, hl in enumerate(res) for h in hl]
+    got = [(int(g["sim_queries"][q]), h.target, h.identity, h.rank) for q, hl in enumerate(res) for h in hl]
     exp = list(zip(g["sim_hit_query"].tolist(), g["sim_hit_target"].tolist(), g["sim_hit_identity"].tolist(),
                    g["sim_hit_score"].tolist()))
     assert len(got) == len(exp)
