@@ -16,6 +16,7 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <algorithm>
 #include <vector>
 
 #include "ck_common.cuh"
@@ -554,8 +555,10 @@ static int32_t phase_a_impl(void *pv) {
             const int64_t n_items = (int64_t)a.nq * stride + 1;
             int64_t *item = (int64_t *)scratch(SLOT_SEARCH_TMP0, (size_t)n_items * 8, &status);
             if (!item) return status;
+            // enough blocks per query that a small batch still spreads over every SM
             int bx = (int)((stride + 255) / 256);
-            if (bx > 64) bx = 64;
+            const int bx_cap = std::max(64, 8 * sm_count() / std::max(1, (int)a.nq));
+            if (bx > bx_cap) bx = bx_cap;
             const dim3 grid((unsigned)bx, (unsigned)a.nq);
             nbr_enum_kernel<false><<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, d_sub,
                                                             a.score_thresh, a.kmer_freqs, a.freq_thresh, stride,
@@ -577,7 +580,8 @@ static int32_t phase_a_impl(void *pv) {
                                                            item, list, err);
             CK_CUDA(cudaGetLastError());
             int by = (int)((total / (a.nq > 0 ? a.nq : 1) + 7) / 8);
-            if (by > 4 * sm_count()) by = 4 * sm_count();
+            const int by_cap = std::max(4 * sm_count(), 16 * sm_count() / std::max(1, (int)a.nq));
+            if (by > by_cap) by = by_cap;
             if (by < 1) by = 1;
             nbr_postings_kernel<<<dim3((unsigned)by, (unsigned)a.nq), 256, 0, a.st>>>(
                 list, item, stride, a.kmer_offsets, a.kmer_entries, a.num_db, counts, a.min_hits, cand, n_cand,
