@@ -44,3 +44,27 @@ def test_connected_components_identical(ck, golden):
         return connected_components(a + a.T, directed=False)[1]
 
     assert np.array_equal(labels(fp, fs), labels(g["t0p5_pairs"], g["t0p5_sims"]))
+
+
+@pytest.mark.parametrize("t,tag", [(0.5, "0p5"), (0.3, "0p3")])
+def test_whole_chain_on_device_matches_reference(ck, golden, t, tag):
+    """Sketches, LSH, Jaccard pre-filter, SW, similarity graph and connected
+    components, every stage on the GPU from the sequences alone, against the
+    reference pipeline's recorded candidates and passing pairs and the clusters
+    scipy gives for them (clustkit/pipeline.py:600-700's order of stages)."""
+    import oracle.graph_oracle as go
+    from clustkit_gb300 import graph
+    from clustkit_gb300.lsh import lsh_candidates_device
+    g = golden("pipeline_golden.npz")
+    n = len(g["lengths"])
+    sk = sketch_flat(g["flat"], g["offsets"], g["lengths"], 5, 128)
+    cand = lsh_candidates_device(sk, int(g["num_tables"]), int(g["num_bands"]), 42).cpu().numpy()
+    assert np.array_equal(cand, g["candidates"].astype(np.int32))
+    fp, fs = compute_pairwise_alignment(
+        cand, None, g["lengths"], t, band_width=100, device="cpu", sketches=sk,
+        flat_sequences=g["flat"], offsets=g["offsets"], use_sw=True, use_c_sw=True)
+    assert np.array_equal(fp, g[f"t{tag}_pairs"])
+    gr = graph.build_similarity_graph(n, fp, fs)
+    labels = graph.cluster_connected_components(gr)
+    ref = go.cluster_connected_components(go.build_similarity_graph(n, g[f"t{tag}_pairs"], g[f"t{tag}_sims"]))
+    assert np.array_equal(labels, ref)
