@@ -265,6 +265,10 @@ static int32_t read_and_clear_error(cudaStream_t st) {
         set_error(CK_ERR_OUT_OF_RANGE, "sequence extent outside the flat buffer");
         return CK_ERR_OUT_OF_RANGE;
     }
+    if (h & ERRBIT_SCHEDULE) {
+        set_error(CK_ERR_CUDA, "internal: a streamed warp-per-pair strip missed its start step");
+        return CK_ERR_CUDA;
+    }
     return CK_OK;
 }
 
@@ -497,6 +501,7 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     if (key == CK_CFG_WAVE_MIN_ROWS) return sw_set_wave(0, value);
     if (key == CK_CFG_WAVE_ALL_BELOW) return sw_set_wave(1, value);
     if (key == CK_CFG_WAVE_ADAPTIVE) return sw_set_wave(2, value);
+    if (key == CK_CFG_WAVE_STREAM) return sw_set_wave(3, value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -509,6 +514,7 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (key == CK_CFG_WAVE_MIN_ROWS) { *value = sw_wave(0); return CK_OK; }
     if (key == CK_CFG_WAVE_ALL_BELOW) { *value = sw_wave(1); return CK_OK; }
     if (key == CK_CFG_WAVE_ADAPTIVE) { *value = sw_wave(2); return CK_OK; }
+    if (key == CK_CFG_WAVE_STREAM) { *value = sw_wave(3); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

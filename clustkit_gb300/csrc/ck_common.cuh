@@ -31,6 +31,7 @@ int32_t cuda_status(cudaError_t e, const char *what);
 enum : int32_t {
     ERRBIT_PAIR_INDEX = 1,     // pair index outside [0, n_seqs)
     ERRBIT_SEQ_EXTENT = 2,     // offsets[i] + lengths[i] outside [0, flat_len]
+    ERRBIT_SCHEDULE = 4,       // a streamed warp-per-pair strip missed its start step (internal)
 };
 
 // ---------------------------------------------------------------- SW constants
@@ -163,7 +164,7 @@ int32_t sw_set_rows_per_strip(int32_t r);
 int32_t sw_rows_per_strip();
 int32_t sw_set_variant(int32_t v);
 int32_t sw_variant();
-int32_t sw_set_wave(int32_t key, int32_t v);  // key 0: min rows, 1: all-pairs batch limit, 2: adaptive
+int32_t sw_set_wave(int32_t key, int32_t v);  // key 0: min rows, 1: all-pairs batch limit, 2: adaptive, 3: stream
 int32_t sw_wave(int32_t key);
 int32_t sw_run_device(const SwIn &in, const SwOut &out, int64_t M, int32_t engine,
                       const int8_t *sub_host, cudaStream_t st, SwCounters *ctr,

@@ -60,6 +60,9 @@ constexpr int32_t MATCH_MASK = (1 << 13) - 1;
 }  // namespace key
 
 constexpr int STRIP_THREADS = 256;
+// per warp, the streamed warp-per-pair phase's pair slots in shared memory
+constexpr size_t WAVE_SLOT_BYTES = 72;  // sizeof(WaveSlot), checked where it is defined
+constexpr int WAVE_SLOTS_PER_WARP = 16;
 
 // a * one + b with `one` a runtime 1: issued as an integer multiply-add on
 // the FMA pipe, which the recurrence leaves mostly idle, instead of an add on
@@ -440,13 +443,19 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
 // increment table + per-row first-max trackers (16 rows for the warp-per-pair phase)
 template <int R>
 __host__ __device__ constexpr size_t strip_smem() {
-    return INC_SMEM + (size_t)(R > 16 ? R : 16) * STRIP_THREADS * sizeof(int32_t);
+    return INC_SMEM + (size_t)(R > 16 ? R : 16) * STRIP_THREADS * sizeof(int32_t) +
+           (size_t)(STRIP_THREADS / 32) * WAVE_SLOTS_PER_WARP * WAVE_SLOT_BYTES;
 }
 
 __device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &out, int64_t p,
                                                  const char *s_inc, int32_t *s_best, int32_t lane,
                                                  int32_t *fallback, int32_t *fallback_count,
                                                  int32_t *err, int32_t one);
+struct WaveSlot;
+__device__ __noinline__ void wave_stream_any(int32_t rows, const SwIn &in, const SwOut &out, const uint32_t *order,
+                                             int32_t n_wave, int32_t *ticket, const char *s_inc, int32_t *s_best,
+                                             WaveSlot *slots, int32_t lane, int32_t *fallback,
+                                             int32_t *fallback_count, int32_t *err, int32_t one);
 
 // Persistent alignment kernel.  Its warps first take the leading
 // counters[6] sorted pairs one warp per pair (long pairs, or every pair of a
@@ -459,7 +468,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
                 int32_t *__restrict__ wave_ticket, int32_t *__restrict__ fallback,
-                int32_t *__restrict__ fallback_count, int32_t *err, int32_t one) {
+                int32_t *__restrict__ fallback_count, int32_t *err, int32_t one, int32_t wave_rows) {
     extern __shared__ int32_t s_inc[];
     if (counters[0] <= 0) return;
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
@@ -467,14 +476,24 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
     int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
     const int32_t lane = threadIdx.x & 31;
     const int32_t n_wave = counters[6];
-    for (;;) {
-        __syncwarp();
-        int32_t q = 0;
-        if (lane == 0) q = atomicAdd(wave_ticket, 1);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= n_wave) break;
-        align_pair_wave_any(in, out, (int64_t)order[q], (const char *)s_inc, s_best, lane, fallback,
-                            fallback_count, err, one);
+    if (wave_rows > 0) {
+        // slots behind the increment table and the per-row trackers
+        char *slot_base = (char *)(s_inc + INC_ENTRIES * 32 + (R > 16 ? R : 16) * STRIP_THREADS);
+        WaveSlot *slots = (WaveSlot *)(slot_base + (size_t)(threadIdx.x >> 5) * WAVE_SLOTS_PER_WARP *
+                                                       WAVE_SLOT_BYTES);
+        if (n_wave > 0)
+            wave_stream_any(wave_rows, in, out, order, n_wave, wave_ticket, (const char *)s_inc, s_best, slots,
+                            lane, fallback, fallback_count, err, one);
+    } else {
+        for (;;) {
+            __syncwarp();
+            int32_t q = 0;
+            if (lane == 0) q = atomicAdd(wave_ticket, 1);
+            q = __shfl_sync(0xffffffffu, q, 0);
+            if (q >= n_wave) break;
+            align_pair_wave_any(in, out, (int64_t)order[q], (const char *)s_inc, s_best, lane, fallback,
+                                fallback_count, err, one);
+        }
     }
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int2 *win = window + (size_t)gwarp * (size_t)W * 32 + lane;
@@ -646,6 +665,255 @@ __device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &ou
     }
 }
 
+// ----------------------------------------------------------------- streamed warp-per-pair
+// The warp-per-pair phase with the strips of consecutive pairs streamed
+// through one warp, so that lanes freed by one pair's strips take the next
+// pair's instead of idling while the pair's wavefront fills and drains.  All
+// pairs of the call share R (chosen from the band width so every pair can
+// rotate).  Strips carry one global sequence number g; lane g mod 32 runs
+// strip g.  Strip s of a pair starting at T0 runs column j at step
+// T0 + s + j - J0(strip 0), i.e. exactly one step behind its upstream strip
+// s - 1 at every column, so the (H, E) hand-over by shuffle works as in the
+// single-pair schedule.  A pair is issued (one per step, once every strip
+// of the previous one has started) with the smallest T0 at which each of its
+// first 32 strips finds its lane free; its later strips rotate through the
+// same lanes as before.  A lane's strip whose upstream lane belongs to
+// another pair or strip reads the out-of-band boundary instead (overrides
+// below), so a lane never reads a neighbour's unrelated values.
+//
+// Per pair, a slot in shared memory holds its geometry, the running best
+// score (first-maximum trigger) and the best cell as one packed 64-bit value
+// (score, then lower row, then match count), merged by atomicMax at each
+// strip's end; the pair's last strip ends last and writes the result.
+constexpr int WS_SLOTS = 16;
+
+struct WaveSlot {
+    unsigned long long acc;   // score << 27 | (16383 - row) << 13 | matches
+    int64_t a_off, b_off;     // residues of the row and column sequences
+    int64_t p;                // pair index
+    int32_t la, lb, w, h, c0, S, J00, T0;
+    int32_t gs;               // running best score of the pair (first-maximum trigger)
+    int32_t live;
+};
+
+static_assert(sizeof(WaveSlot) == WAVE_SLOT_BYTES, "slot layout");
+static_assert(WS_SLOTS == WAVE_SLOTS_PER_WARP, "slot count");
+
+template <int R>
+__device__ __forceinline__ void strip_bounds(const WaveSlot &sl, int32_t s, int32_t &i0, int32_t &lo,
+                                             int32_t &J0, int32_t &J1, int32_t &alive) {
+    i0 = s * R + 1;
+    lo = s * R + sl.c0;
+    J0 = lo > 1 ? lo : 1;
+    const int32_t hi = lo + R - 1 + 2 * sl.w;
+    J1 = hi < sl.lb ? hi : sl.lb;
+    alive = sl.la - i0 + 1 < R ? sl.la - i0 + 1 : R;
+    if (alive < 0) alive = 0;
+}
+template <int R>
+__device__ __forceinline__ int32_t strip_t0(const WaveSlot &sl, int32_t s) {
+    const int32_t lo = s * R + sl.c0;
+    return sl.T0 + s + (lo > 1 ? lo : 1) - sl.J00;
+}
+template <int R>
+__device__ __forceinline__ int32_t strip_te(const WaveSlot &sl, int32_t s) {
+    const int32_t lo = s * R + sl.c0;
+    const int32_t hi = lo + R - 1 + 2 * sl.w;
+    const int32_t J1 = hi < sl.lb ? hi : sl.lb;
+    const int32_t te = sl.T0 + s + J1 - sl.J00;
+    const int32_t t0 = strip_t0<R>(sl, s);
+    return te > t0 ? te : t0;  // a strip whose band lies left of column 1 ends where it starts
+}
+
+template <int R>
+__device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *order, int32_t n_wave,
+                            int32_t *ticket, const char *s_inc, int32_t *s_best, WaveSlot *slots, int32_t lane,
+                            int32_t *fallback, int32_t *fallback_count, int32_t *err, int32_t one) {
+    using namespace key;
+    constexpr uint32_t FULL = 0xffffffffu;
+    // warp-uniform schedule state
+    int32_t T = 0, T_issue = -1, g_next = 0, seq = 0;
+    bool exhausted = false;
+    for (int i = lane; i < WS_SLOTS; i += 32) slots[i].live = 0;
+    __syncwarp();
+    // per-lane strip state
+    int32_t cur_slot = -1, cur_s = 0, i0 = 0, lo0 = 0, J0 = 1, J1 = 0, alive = 0, te = 0, top = 0;
+    int32_t pend_slot = -1, pend_s = 0, pend_t0 = 0;
+    int32_t F = -1;
+    int32_t hout = 0, eout = NEG_E, hprev = 0;
+    const uint8_t *B = nullptr;
+    StripRegs<R> S;
+    for (;;) {
+        // ---- issue one pair (warp-uniform)
+        if (!exhausted && T > T_issue && !slots[seq % WS_SLOTS].live) {
+            int32_t q = 0;
+            if (lane == 0) q = atomicAdd(ticket, 1);
+            q = __shfl_sync(FULL, q, 0);
+            if (q >= n_wave) {
+                exhausted = true;
+            } else {
+                const int64_t p = (int64_t)order[q];
+                const PairGeom g = pair_geometry(in, p, err);
+                int32_t n_strips = (g.la + R - 1) / R;
+                {
+                    const int64_t lim = (int64_t)g.lb - 1 - g.h + g.w;
+                    const int64_t s_lim = lim < 0 ? 0 : lim / R + 1;
+                    if (s_lim < n_strips) n_strips = (int32_t)s_lim;
+                }
+                if (n_strips <= 0) {
+                    if (lane == 0) write_result(out, in, p, 0, 0, g.la, g.la, g.lb);
+                } else {
+                    WaveSlot &sl = slots[seq % WS_SLOTS];
+                    const int32_t c0 = 1 + g.h - g.w;
+                    const int32_t J00 = c0 > 1 ? c0 : 1;
+                    const int32_t m = (lane - g_next) & 31;
+                    const int32_t first = n_strips < 32 ? n_strips : 32;
+                    int32_t req = T;
+                    if (m < first) {
+                        const int32_t lom = m * R + c0;
+                        const int32_t r = F + 1 - m - ((lom > 1 ? lom : 1) - J00);
+                        req = r > T ? r : T;
+                    }
+                    const int32_t T0p = __reduce_max_sync(FULL, req);
+                    if (lane == 0) {
+                        sl.acc = 0;
+                        sl.a_off = in.offsets[g.a_idx];
+                        sl.b_off = in.offsets[g.b_idx];
+                        sl.p = p;
+                        sl.la = g.la; sl.lb = g.lb; sl.w = g.w; sl.h = g.h; sl.c0 = c0;
+                        sl.S = n_strips; sl.J00 = J00; sl.T0 = T0p; sl.gs = 1; sl.live = 1;
+                    }
+                    __syncwarp();
+                    if (m < first) {
+                        pend_slot = seq % WS_SLOTS;
+                        pend_s = m;
+                        pend_t0 = strip_t0<R>(sl, m);
+                        const int32_t last = m + 32 * ((n_strips - 1 - m) / 32);
+                        F = strip_te<R>(sl, last);
+                    }
+                    T_issue = strip_t0<R>(sl, n_strips - 1);
+                    g_next += n_strips;
+                    ++seq;
+                }
+            }
+        }
+        // ---- start this lane's next strip.  Its start step is never in the past
+        // (the rotation bound on R); were it, the strip starts now and the call
+        // reports an internal error rather than the warp waiting forever.
+        if (pend_slot >= 0 && T >= pend_t0) {
+            if (T > pend_t0) atomicOr(err, ERRBIT_SCHEDULE);
+            const WaveSlot &sl = slots[pend_slot];
+            cur_slot = pend_slot;
+            cur_s = pend_s;
+            pend_slot = -1;
+            strip_bounds<R>(sl, cur_s, i0, lo0, J0, J1, alive);
+            te = strip_te<R>(sl, cur_s);
+            top = cur_s * R + sl.h + sl.w;
+            B = in.flat + sl.b_off;
+            const uint8_t *A = in.flat + sl.a_off;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                S.hc[r] = 0;
+                S.fT[r] = NEG_F;
+                s_best[r * STRIP_THREADS] = 0;
+                const uint32_t code = r < alive ? (uint32_t)A[i0 + r - 1] : 0u;
+                S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
+            }
+        }
+        // ---- one column of this lane's strip
+        int32_t hin = __shfl_sync(FULL, hout, (lane + 31) & 31);
+        int32_t ein = __shfl_sync(FULL, eout, (lane + 31) & 31);
+        int32_t cm = 0;
+        const bool has = cur_slot >= 0;
+        int32_t j = 0;
+        if (has) {
+            const WaveSlot &sl = slots[cur_slot];
+            j = T - sl.T0 - cur_s + sl.J00;
+            const int32_t hdiag = (cur_s == 0 || j - 1 > top || j - 1 < 1) ? 0 : hprev;
+            hprev = hin;
+            if (cur_s == 0 || j > top) { hin = 0; ein = NEG_E; }
+            if (j >= J0 && j <= J1) {
+                const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
+                int32_t hu = hin, eu = ein;
+                strip_cells<R, 0, R, true>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, 2u * (uint32_t)sl.w, alive,
+                                           one);
+                hout = hu;
+                eout = eu;
+                cm = S.hc[0];
+#pragma unroll
+                for (int r = 1; r + 1 < R; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
+                if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
+            } else {
+                hout = 0;
+                eout = NEG_E;
+            }
+        } else {
+            hprev = hin;
+            hout = 0;
+            eout = NEG_E;
+        }
+        // ---- first-maximum trackers: per-pair running best score
+        const bool trig = has && (cm >> 16) >= slots[cur_slot].gs;
+        if (__any_sync(FULL, trig)) {
+            if (has) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int32_t b = s_best[r * STRIP_THREADS];
+                    if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
+                }
+                if (cm > 0) atomicMax(&slots[cur_slot].gs, cm >> 16);
+            }
+        }
+        // ---- strip end: merge its rows into the pair's best; the last strip writes
+        if (has && T == te) {
+            int32_t bk = 0, br = 0;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int32_t b = s_best[r * STRIP_THREADS];
+                if (r < alive && b > (bk | (KU - 1))) { bk = b; br = i0 + r; }
+            }
+            WaveSlot &sl = slots[cur_slot];
+            if (bk > 0)
+                atomicMax(&sl.acc, ((unsigned long long)(uint32_t)(bk >> 16) << 27) |
+                                       ((unsigned long long)(uint32_t)(16383 - br) << 13) |
+                                       (unsigned long long)(uint32_t)(bk & MATCH_MASK));
+            if (cur_s == sl.S - 1) {
+                __threadfence_block();
+                const unsigned long long acc = atomicAdd(&sl.acc, 0ull);
+                const int32_t score = (int32_t)(acc >> 27);
+                if (score >= SCORE_LIMIT) {
+                    const int32_t pos = atomicAdd(fallback_count, 1);
+                    fallback[pos] = (int32_t)sl.p;
+                    atomicAdd(fallback_count + 2, 1);  // re-run counter
+                } else {
+                    write_result(out, in, sl.p, score, score > 0 ? (int32_t)(acc & MATCH_MASK) : 0, sl.la, sl.la,
+                                 sl.lb);
+                }
+                sl.live = 0;
+            } else if (cur_s + 32 < sl.S) {
+                pend_slot = cur_slot;
+                pend_s = cur_s + 32;
+                pend_t0 = strip_t0<R>(sl, pend_s);
+            }
+            cur_slot = -1;
+        }
+        __syncwarp();
+        ++T;
+        if (__all_sync(FULL, exhausted && cur_slot < 0 && pend_slot < 0)) break;
+    }
+}
+
+__device__ __noinline__ void wave_stream_any(int32_t rows, const SwIn &in, const SwOut &out, const uint32_t *order,
+                                             int32_t n_wave, int32_t *ticket, const char *s_inc, int32_t *s_best,
+                                             WaveSlot *slots, int32_t lane, int32_t *fallback,
+                                             int32_t *fallback_count, int32_t *err, int32_t one) {
+    switch (rows) {
+        case 4: wave_stream<4>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
+        case 8: wave_stream<8>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
+        default: wave_stream<16>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
+    }
+}
+
 // ----------------------------------------------------------------- driver
 static int32_t pow2_at_least(int64_t x) {
     int32_t p = 1;
@@ -661,6 +929,19 @@ static int32_t g_variant = 1;
 static int32_t g_wave_all_below = 24576;
 static int32_t g_wave_min_rows = 256;
 static int32_t g_wave_adaptive = 1;
+static int32_t g_wave_stream = 1;  // stream the strips of consecutive pairs through a warp
+
+// Rows per strip shared by every warp-per-pair pair of a call: the smallest
+// that lets a strip of any of them rotate through 32 lanes (half-widths up to
+// max(band width, 50); with a wider band every pair has at most 512 rows, as
+// the routing guarantees, so 16 rows give at most 32 strips).  0: one pair
+// per warp at a time.
+static int32_t wave_rows_for(int32_t wmax) {
+    if (!g_wave_stream) return 0;
+    if (2 * wmax < 31 * 4 + 32) return 4;
+    if (2 * wmax < 31 * 8 + 32) return 8;
+    return 16;
+}
 
 int32_t sw_set_wave(int32_t key, int32_t v) {
     if (v < 0) {
@@ -669,11 +950,12 @@ int32_t sw_set_wave(int32_t key, int32_t v) {
     }
     if (key == 0) g_wave_min_rows = v;
     else if (key == 1) g_wave_all_below = v;
-    else g_wave_adaptive = v ? 1 : 0;
+    else if (key == 2) g_wave_adaptive = v ? 1 : 0;
+    else g_wave_stream = v ? 1 : 0;
     return CK_OK;
 }
 int32_t sw_wave(int32_t key) {
-    return key == 0 ? g_wave_min_rows : key == 1 ? g_wave_all_below : g_wave_adaptive;
+    return key == 0 ? g_wave_min_rows : key == 1 ? g_wave_all_below : key == 2 ? g_wave_adaptive : g_wave_stream;
 }
 
 int32_t sw_set_variant(int32_t v) {
@@ -724,7 +1006,7 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     int2 *window = (int2 *)scratch(SLOT_WINDOW, (size_t)blocks * per_block, &status);
     if (!window) return status;
     kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
-                                              ticket + 5, fallback, fb_count, err, 1);
+                                              ticket + 5, fallback, fb_count, err, 1, wave_rows_for(wmax));
     CK_CUDA(cudaGetLastError());
     if (ctr) ctr->launches += 1;
     return CK_OK;

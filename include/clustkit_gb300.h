@@ -172,12 +172,16 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_WAVE_ADAPTIVE   1 (default): raise that row bound to where a pair's
  *                          one-lane time would pass the call's expected
  *                          kernel time, from the call's cell count; 0:
- *                          use CK_CFG_WAVE_MIN_ROWS as given */
+ *                          use CK_CFG_WAVE_MIN_ROWS as given
+ *   CK_CFG_WAVE_STREAM     1 (default): a warp streams the row strips of
+ *                          consecutive warp-per-pair pairs through its lanes;
+ *                          0: one such pair per warp at a time */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
 #define CK_CFG_WAVE_ALL_BELOW 3
 #define CK_CFG_WAVE_ADAPTIVE 4
+#define CK_CFG_WAVE_STREAM 5
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

@@ -98,13 +98,13 @@ def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
 
 
 @contextlib.contextmanager
-def wave_config(all_below, min_rows, adaptive=0):
+def wave_config(all_below, min_rows, adaptive=0, stream=1):
     """Route pairs between the warp-per-pair and the lane-per-pair kernels."""
-    from clustkit_gb300._lib import (CFG_WAVE_ADAPTIVE, CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, get_config,
-                                     set_config)
-    keys = (CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_ADAPTIVE)
+    from clustkit_gb300._lib import (CFG_WAVE_ADAPTIVE, CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_STREAM,
+                                     get_config, set_config)
+    keys = (CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_ADAPTIVE, CFG_WAVE_STREAM)
     keep = [get_config(k) for k in keys]
-    for k, v in zip(keys, (all_below, min_rows, adaptive)):
+    for k, v in zip(keys, (all_below, min_rows, adaptive, stream)):
         set_config(k, v)
     try:
         yield
@@ -117,10 +117,11 @@ def wave_config(all_below, min_rows, adaptive=0):
 WAVE_ROUTES = [(1 << 30, 0), (0, 64), (0, 1024)]
 
 
+@pytest.mark.parametrize("stream", [1, 0])
 @pytest.mark.parametrize("all_below,min_rows", WAVE_ROUTES)
 @pytest.mark.parametrize("bw", [0, 3, 16, 32, 50, 100, 128, 238, 300])
-def test_wave_kernel_golden_and_random(ck, golden, all_below, min_rows, bw):
-    with wave_config(all_below, min_rows):
+def test_wave_kernel_golden_and_random(ck, golden, all_below, min_rows, bw, stream):
+    with wave_config(all_below, min_rows, stream=stream):
         g = golden("sw_golden.npz")
         if f"bw{bw}_scores" in g.files:
             r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
@@ -138,7 +139,7 @@ def test_wave_kernel_golden_and_random(ck, golden, all_below, min_rows, bw):
 
 
 @pytest.mark.parametrize("bw", [16, 64, 128])
-def test_wave_kernel_heavy_tailed_lengths(ck, bw):
+def test_wave_kernel_heavy_tailed_lengths(ck, bw):  # streamed warp-per-pair phase (the default)
     """Pareto lengths to 8000: long pairs take the warp-per-pair kernel in a
     large call, the rest the strip kernel."""
     s = synth.generate_families(300, 4, median=0, lo=30, hi=8000, seed=bw, length_dist="pareto")
@@ -338,3 +339,16 @@ def test_autotuner_settings_agree(ck):
             _same(call.results(), ref)
     finally:
         tune.apply(keep)
+
+
+@pytest.mark.parametrize("bw", [238, 100, 20])
+def test_streamed_wave_many_small_pairs(ck, bw):
+    """Thousands of short and mixed pairs through the streamed warp-per-pair
+    phase (many pairs in flight per warp, slot reuse), against the oracle."""
+    s = synth.generate_families(300, 6, median=120, lo=5, hi=900, seed=bw)
+    pairs = synth.mixed_pairs(s, 20000, seed=bw + 1)
+    with wave_config(1 << 30, 0):
+        r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
+        c = ck.sw_counters()
+    assert c["wave"] == c["batched"]
+    _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))

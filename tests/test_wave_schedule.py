@@ -162,3 +162,181 @@ def test_wave_schedule_matches_oracle(li, lj, bw, hint):
         res = run_case(rng, li, lj, bw, hint, related)
         assert res is not None
         assert res[0] == res[2] and res[1] == res[3], res
+
+
+# ----------------------------------------------------------------------------
+# The streamed schedule (sw_batched.cu, wave_stream): strips of consecutive
+# pairs flow through one warp's lanes; strip s of a pair starting at T0 runs
+# column j at step T0 + s + j - J0(strip 0); a pair is issued (one per step,
+# after every strip of the previous one has started) at the smallest T0 that
+# finds each of its first 32 strips' lanes free; per-pair slots hold the
+# running best score and the packed best cell.
+NSLOT = 16
+
+def r_call(bw):
+    wmax = max(bw, 50) if bw > 0 else 10**9
+    if 2 * wmax < 31 * 4 + 32: return 4
+    if 2 * wmax < 31 * 8 + 32: return 8
+    return 16
+
+def stream(pairs_geo, R):
+    """pairs_geo: list of (A, B, la, lb, w, h).  Returns list of (score, matches)."""
+    res = [None] * len(pairs_geo)
+    slots = [None] * NSLOT
+    lanes = [dict(cur=None, pend=None, F=-1, hout=0, eout=NEG_E, hprev=0) for _ in range(32)]
+    T = 0; q = 0; g_next = 0; seq = 0; T_issue = -1
+    def strip_geo(sl, s):
+        i0 = s * R + 1; lo = s * R + sl['c0']
+        J0 = max(1, lo); J1 = min(sl['lb'], lo + R - 1 + 2 * sl['w'])
+        alive = max(0, min(R, sl['la'] - i0 + 1))
+        return i0, lo, J0, J1, alive
+    def t0(sl, s):
+        return sl['T0'] + s + strip_geo(sl, s)[2] - sl['J00']
+    def te(sl, s):
+        # a strip whose band lies left of column 1 has no cells: it ends where it starts
+        return max(t0(sl, s), sl['T0'] + s + strip_geo(sl, s)[3] - sl['J00'])
+    while True:
+        # issue
+        if q < len(pairs_geo) and T > T_issue and slots[seq % NSLOT] is None:
+            A, B, la, lb, w, h = pairs_geo[q]
+            c0 = 1 + h - w
+            n_strips = (la + R - 1) // R
+            lim = lb - 1 - h + w
+            s_lim = 0 if lim < 0 else lim // R + 1
+            S = min(n_strips, s_lim)
+            if S == 0:
+                res[q] = (0, 0); q += 1   # written at issue; the next issue waits a step
+            else:
+                sl = dict(p=q, A=A, B=B, la=la, lb=lb, w=w, h=h, c0=c0, S=S, J00=max(1, c0), T0=0, acc=0, gs=1,
+                          seq=seq)
+                req = T
+                for lane in range(32):
+                    m = (lane - g_next) % 32
+                    if m < min(S, 32):
+                        J0m = max(1, m * R + c0)
+                        req = max(req, lanes[lane]['F'] + 1 - m - (J0m - sl['J00']))
+                sl['T0'] = req
+                slots[seq % NSLOT] = sl
+                for lane in range(32):
+                    m = (lane - g_next) % 32
+                    if m < min(S, 32):
+                        assert lanes[lane]['pend'] is None
+                        lanes[lane]['pend'] = (seq % NSLOT, m)
+                        last = m + 32 * ((S - 1 - m) // 32)
+                        lanes[lane]['F'] = te(sl, last)
+                T_issue = t0(sl, S - 1)
+                g_next += S; seq += 1; q += 1
+        # activation
+        for L in lanes:
+            if L['pend'] is not None:
+                slot_i, s = L['pend']
+                sl = slots[slot_i]
+                if T >= t0(sl, s):
+                    assert T == t0(sl, s), 'strip started late'
+                    assert L['cur'] is None
+                    i0, lo, J0, J1, alive = strip_geo(sl, s)
+                    codes = [int(sl['A'][i0 + r - 1]) if r < alive else 0 for r in range(R)]
+                    L['cur'] = dict(slot=slot_i, s=s, i0=i0, lo=lo, J0=J0, J1=J1, alive=alive, codes=codes,
+                                    hc=[0] * R, fT=[NEG_F] * R, best=[0] * R, Te=te(sl, s))
+                    L['pend'] = None
+        hin_all = [lanes[(l + 31) & 31]['hout'] for l in range(32)]
+        ein_all = [lanes[(l + 31) & 31]['eout'] for l in range(32)]
+        cms = [0] * 32
+        for lane, L in enumerate(lanes):
+            hin, ein = hin_all[lane], ein_all[lane]
+            c = L['cur']
+            if c is None:
+                L['hprev'] = hin; L['hout'], L['eout'] = 0, NEG_E; continue
+            sl = slots[c['slot']]; s = c['s']
+            j = T - sl['T0'] - s + sl['J00']
+            top = s * R + sl['h'] + sl['w']
+            hdiag = 0 if (s == 0 or j - 1 > top or j - 1 < 1) else L['hprev']
+            L['hprev'] = hin
+            if s == 0 or j > top: hin, ein = 0, NEG_E
+            assert c['J0'] <= j <= c['J1'] or j > c['J1'] or j < c['J0']
+            if c['J0'] <= j <= c['J1']:
+                bc = int(sl['B'][j - 1]); hu, eu = hin, ein; hc, fT = c['hc'], c['fT']
+                for r in range(R):
+                    if r < c['alive'] and 0 <= j - r - c['lo'] <= 2 * sl['w']:
+                        diagc = max(hdiag + inc(c['codes'][r], bc), ZKEY)
+                        eR = max(hu + OPEN_E, eu + EXT)
+                        fTn = max(fT[r] + EXT, hc[r] + OPEN_F) | TBIT
+                        hn = max(diagc, eR, fTn) & CLEAN
+                        hdiag = hc[r]; hc[r] = hn; fT[r] = fTn; hu = hn; eu = eR | TBIT
+                    else:
+                        hdiag = hc[r]; hc[r] = 0; hu = 0; eu = NEG_E
+                L['hout'], L['eout'] = hu, eu
+                cms[lane] = max(hc)
+            else:
+                L['hout'], L['eout'] = 0, NEG_E
+        # tracking: per-pair gs
+        trig = any(lanes[l]['cur'] is not None and (cms[l] >> 16) >= slots[lanes[l]['cur']['slot']]['gs']
+                   for l in range(32))
+        if trig:
+            for l, L in enumerate(lanes):
+                c = L['cur']
+                if c is None: continue
+                for r in range(R):
+                    if c['hc'][r] > (c['best'][r] | (KU - 1)): c['best'][r] = c['hc'][r]
+                sl = slots[c['slot']]
+                if cms[l] > 0:
+                    sl['gs'] = max(sl['gs'], cms[l] >> 16)
+        # strip ends
+        for l, L in enumerate(lanes):
+            c = L['cur']
+            if c is None or T != c['Te']: continue
+            sl = slots[c['slot']]
+            lb_, lr = 0, INT_MAX
+            for r in range(R):
+                b = c['best'][r]
+                if r < c['alive'] and b > (lb_ | (KU - 1)): lb_, lr = b, c['i0'] + r
+            if lb_ > 0:
+                packed = ((lb_ >> 16) << 27) | ((16383 - lr) << 13) | (lb_ & MATCH)
+                sl['acc'] = max(sl['acc'], packed)
+            L['cur'] = None
+            s = c['s']
+            if s == sl['S'] - 1:
+                acc = sl['acc']
+                res[sl['p']] = (acc >> 27, acc & MATCH) if acc else (0, 0)
+                slots[c['slot']] = None
+            elif s + 32 < sl['S']:
+                L['pend'] = (c['slot'], s + 32)
+        T += 1
+        if q >= len(pairs_geo) and all(L['cur'] is None and L['pend'] is None for L in lanes):
+            break
+    return res, T
+
+def run_stream(seed, n, bw, maxlen=400, hint_frac=0.3):
+    rng = np.random.default_rng(seed)
+    seqs, pg, pairs = [], [], []
+    for k in range(n):
+        li = int(rng.integers(1, maxlen)); lj = int(rng.integers(1, maxlen))
+        a = rng.integers(0, 20, li).astype(np.uint8); b = rng.integers(0, 20, lj).astype(np.uint8)
+        if rng.random() < 0.5:
+            b = a[:lj].copy() if lj <= li else np.concatenate([a, rng.integers(0, 20, lj - li)]).astype(np.uint8)
+            m = rng.random(lj) < 0.3; b[m] = rng.integers(0, 20, m.sum())
+        sh = min(li, lj)
+        hint = int(rng.integers(-sh, sh + 1)) if rng.random() < hint_frac else 0
+        swap, la, lb, w, h = geometry(li, lj, bw, hint)
+        A, B = (a, b) if not swap else (b, a)
+        pg.append((A, B, la, lb, w, h)); seqs.append((a, b, hint))
+    R = r_call(bw)
+    got, T = stream(pg, R)
+    bad = 0
+    for k, (a, b, hint) in enumerate(seqs):
+        flat = np.concatenate([a, b]); offs = np.array([0, len(a)], np.int64); lens = np.array([len(a), len(b)], np.int32)
+        r = oracle.sw_batch(np.array([[0, 1]], np.int32), flat, offs, lens, bw, BLOSUM62, diag_hints=np.array([hint], np.int32))
+        exp = (int(r['scores'][0]), int(r['matches'][0]))
+        if got[k] != exp:
+            bad += 1
+            if bad < 4: print('BAD', k, len(a), len(b), bw, hint, got[k], exp)
+    cells = sum(la * min(2 * w + 1, lb) for (_, _, la, lb, w, h) in pg)
+    return bad
+
+
+
+@pytest.mark.parametrize("seed,n,bw,maxlen", [(1, 12, 238, 300), (2, 20, 100, 200), (3, 8, 16, 700),
+                                              (4, 6, 60, 900), (5, 10, 0, 45), (6, 6, 1, 300),
+                                              (7, 4, 238, 900), (8, 40, 238, 120)])
+def test_streamed_schedule_matches_oracle(seed, n, bw, maxlen):
+    assert run_stream(seed, n, bw, maxlen) == 0
