@@ -808,6 +808,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             pend_slot = -1;
             strip_bounds<R>(sl, cur_s, i0, lo0, J0, J1, alive);
             te = strip_te<R>(sl, cur_s);
+            if (te < T) te = T;  // only after a late start: the strip still ends
             top = cur_s * R + sl.h + sl.w;
             B = in.flat + sl.b_off;
             const uint8_t *A = in.flat + sl.a_off;
