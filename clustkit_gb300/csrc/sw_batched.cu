@@ -468,7 +468,8 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
                 int32_t *__restrict__ wave_ticket, int32_t *__restrict__ fallback,
-                int32_t *__restrict__ fallback_count, int32_t *err, int32_t one, int32_t wave_rows) {
+                int32_t *__restrict__ fallback_count, int32_t *err, int32_t one, int32_t wave_rows,
+                int32_t wave_rows_force) {
     extern __shared__ int32_t s_inc[];
     if (counters[0] <= 0) return;
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
@@ -476,7 +477,11 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
     int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
     const int32_t lane = threadIdx.x & 31;
     const int32_t n_wave = counters[6];
-    if (wave_rows > 0) {
+    // stream the pairs' strips through each warp when there are more pairs than
+    // warps (each warp then sees several); with fewer, one pair per warp at the
+    // rows per strip each pair allows has the shorter wavefronts
+    const int32_t n_warps = (int32_t)((gridDim.x * blockDim.x) >> 5);
+    if (wave_rows > 0 && (wave_rows_force || n_wave > n_warps)) {
         // slots behind the increment table and the per-row trackers
         char *slot_base = (char *)(s_inc + INC_ENTRIES * 32 + (R > 16 ? R : 16) * STRIP_THREADS);
         WaveSlot *slots = (WaveSlot *)(slot_base + (size_t)(threadIdx.x >> 5) * WAVE_SLOTS_PER_WARP *
@@ -930,7 +935,9 @@ static int32_t g_variant = 1;
 static int32_t g_wave_all_below = 24576;
 static int32_t g_wave_min_rows = 256;
 static int32_t g_wave_adaptive = 1;
-static int32_t g_wave_stream = 1;  // stream the strips of consecutive pairs through a warp
+// stream the strips of consecutive pairs through a warp: 1 when the call has
+// more warp-per-pair pairs than warps, 2 always, 0 never
+static int32_t g_wave_stream = 1;
 
 // Rows per strip shared by every warp-per-pair pair of a call: the smallest
 // that lets a strip of any of them rotate through 32 lanes (half-widths up to
@@ -952,7 +959,7 @@ int32_t sw_set_wave(int32_t key, int32_t v) {
     if (key == 0) g_wave_min_rows = v;
     else if (key == 1) g_wave_all_below = v;
     else if (key == 2) g_wave_adaptive = v ? 1 : 0;
-    else g_wave_stream = v ? 1 : 0;
+    else g_wave_stream = v > 2 ? 2 : v;
     return CK_OK;
 }
 int32_t sw_wave(int32_t key) {
@@ -1007,7 +1014,8 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     int2 *window = (int2 *)scratch(SLOT_WINDOW, (size_t)blocks * per_block, &status);
     if (!window) return status;
     kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
-                                              ticket + 5, fallback, fb_count, err, 1, wave_rows_for(wmax));
+                                              ticket + 5, fallback, fb_count, err, 1, wave_rows_for(wmax),
+                                              g_wave_stream == 2 ? 1 : 0);
     CK_CUDA(cudaGetLastError());
     if (ctr) ctr->launches += 1;
     return CK_OK;

@@ -173,9 +173,10 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *                          one-lane time would pass the call's expected
  *                          kernel time, from the call's cell count; 0:
  *                          use CK_CFG_WAVE_MIN_ROWS as given
- *   CK_CFG_WAVE_STREAM     1 (default): a warp streams the row strips of
- *                          consecutive warp-per-pair pairs through its lanes;
- *                          0: one such pair per warp at a time */
+ *   CK_CFG_WAVE_STREAM     1 (default): when a call has more warp-per-pair
+ *                          pairs than the kernel has warps, a warp streams the
+ *                          row strips of consecutive pairs through its lanes;
+ *                          2: always; 0: never (one pair per warp at a time) */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2

@@ -117,7 +117,7 @@ def wave_config(all_below, min_rows, adaptive=0, stream=1):
 WAVE_ROUTES = [(1 << 30, 0), (0, 64), (0, 1024)]
 
 
-@pytest.mark.parametrize("stream", [1, 0])
+@pytest.mark.parametrize("stream", [2, 0])
 @pytest.mark.parametrize("all_below,min_rows", WAVE_ROUTES)
 @pytest.mark.parametrize("bw", [0, 3, 16, 32, 50, 100, 128, 238, 300])
 def test_wave_kernel_golden_and_random(ck, golden, all_below, min_rows, bw, stream):
@@ -145,7 +145,7 @@ def test_wave_kernel_heavy_tailed_lengths(ck, bw):  # streamed warp-per-pair pha
     s = synth.generate_families(300, 4, median=0, lo=30, hi=8000, seed=bw, length_dist="pareto")
     pairs = synth.mixed_pairs(s, 30000, seed=bw, min_ratio=0.5)
     ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
-    with wave_config(0, 512):
+    with wave_config(0, 512, stream=2):
         r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
         c = ck.sw_counters()
     _same(r, ref)
@@ -347,7 +347,7 @@ def test_streamed_wave_many_small_pairs(ck, bw):
     phase (many pairs in flight per warp, slot reuse), against the oracle."""
     s = synth.generate_families(300, 6, median=120, lo=5, hi=900, seed=bw)
     pairs = synth.mixed_pairs(s, 20000, seed=bw + 1)
-    with wave_config(1 << 30, 0):
+    with wave_config(1 << 30, 0, stream=2):
         r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62)
         c = ck.sw_counters()
     assert c["wave"] == c["batched"]
