@@ -173,6 +173,42 @@ def barrier(world: int):
 
 
 # ----------------------------------------------------------------------------- CPU baselines
+def reference_gpu_baseline(s, pairs, d_flat, d_off, d_len, stream, n_sample: int = 150_000):
+    """The reference's CuPy GPU path (its own kernel source, compiled from the
+    reference checkout into oracle/_ref/, with its host batching restated in
+    oracle/cupy_ref.py) on a random sample of the workload's pairs, device-resident
+    inputs, CUDA events around its launches; plus whether its identities and
+    pass/fail equal this engine's under the same (CuPy) pass rule."""
+    import torch
+    from oracle import cupy_ref
+    from clustkit_gb300.blosum import BLOSUM62
+    from clustkit_gb300.pairwise import PASS_CUPY, batch_sw
+    if not cupy_ref.available():
+        return {"unavailable": "oracle/_ref/sw_cupy_ref.cubin is built from the reference checkout, absent here"}
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(len(pairs), size=min(n_sample, len(pairs)), replace=False))
+    sp = pairs[idx]
+    k = cupy_ref.CupyPathKernel()
+    plan = k.prepare(sp, s.lengths, BAND_WIDTH, BLOSUM62)
+    k.launch(plan, d_flat, d_off, d_len, THRESHOLD, stream.cuda_stream)  # warm-up
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    k.launch(plan, d_flat, d_off, d_len, THRESHOLD, stream.cuda_stream)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b)
+    sims, mask = k.results(plan)
+    ours = batch_sw(sp, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, THRESHOLD, pass_rule=PASS_CUPY)
+    cells = int(pair_cells(sp, s.lengths, BAND_WIDTH).sum())
+    return {"value": cells / (ms * 1e-3) / 1e9, "unit": "GCUPS", "pairs_per_s": len(sp) / (ms * 1e-3),
+            "kernel_ms": ms, "sample": f"{len(sp)} random pairs of the workload ({cells} cells)",
+            "threads_per_block": [t for (_, _, _, t) in plan["batches"]], "launches": len(plan["batches"]),
+            "agrees_with_this_engine_pass_cupy": bool(np.array_equal(sims, ours["sims"]) and
+                                                      np.array_equal(mask, ours["mask"])),
+            "source": "clustkit/pairwise.py:1215-1402 kernel + :1480-1547 batching (CuPy not installed)"}
+
+
 def cpu_baseline(s, pairs, target_s: float = 12.0, use_ref: bool = True):
     import oracle
     from clustkit_gb300.blosum import BLOSUM62
@@ -395,6 +431,8 @@ def run_ours(args, world, rank, local):
     gcups_kernel = cells / kernel_s / 1e9
     achieved = gcups_kernel * OPS_PER_CELL  # Gop/s
     cpu = cpu_baseline(s, pairs) if (rank == 0 and not args.no_cpu) else None
+    gpu_ref = (reference_gpu_baseline(s, pairs, d_flat, d_off, d_len, stream)
+               if (rank == 0 and not args.no_cpu) else None)
 
     gcups = world * cells / t_batched * args.steps / 1e9
     line = {
@@ -425,6 +463,7 @@ def run_ours(args, world, rank, local):
                      "probe_gops": {k: v / 1e9 for k, v in rates.items()},
                      "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL)},
         "cpu_baseline": cpu,
+        "reference_cupy_path": gpu_ref,
         "rows_per_strip": _lib.get_config(_lib.CFG_ROWS_PER_STRIP),
         "strip_variant": _lib.get_config(_lib.CFG_STRIP_VARIANT),
         "sweep_gcups": sweep or None,

@@ -11,6 +11,12 @@ legs).  Nothing in the product library links or loads them.
   straight from the reference checkout (read in place, never copied), with the
   reference's own build line (clustkit/csrc/sw_align.c:10) minus
   ``-march=native``.  Built only when the reference checkout exists.
+* ``oracle/_ref/sw_cupy_ref.cubin`` -- the reference's CuPy SW kernel
+  (the ``_SW_ALIGN_KERNEL_CODE`` string, clustkit/pairwise.py:1215-1402, read
+  from the checkout with ``ast``, never imported), compiled by nvcc for
+  sm_103a from a temporary file outside the repository; only the device
+  binary is written.  It is the "reference's CuPy path" baseline timed by
+  bench.py through oracle/cupy_ref.py (CuPy itself is not installed).
 """
 from __future__ import annotations
 
@@ -58,9 +64,38 @@ def build_reference(verbose: bool = False) -> Path | None:
     return out
 
 
+def build_reference_cupy_kernel(verbose: bool = False) -> Path | None:
+    """Compile the reference's CuPy kernel string into oracle/_ref/sw_cupy_ref.cubin."""
+    import ast
+    import tempfile
+    py = REF_SRC.parent.parent / "pairwise.py"
+    if not py.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    out = REF_OUT / "sw_cupy_ref.cubin"
+    if out.exists() and out.stat().st_mtime >= py.stat().st_mtime:
+        return out
+    code = None
+    for node in ast.parse(py.read_text()).body:
+        if isinstance(node, ast.Assign) and any(getattr(t, "id", None) == "_SW_ALIGN_KERNEL_CODE"
+                                                for t in node.targets):
+            code = node.value.value
+    if code is None:
+        return None
+    with tempfile.TemporaryDirectory() as td:
+        src = Path(td) / "sw_cupy_ref.cu"
+        src.write_text(code)
+        cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", str(out), str(src)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    return out
+
+
 def main() -> None:
     print(build_oracle(verbose=True))
     print(build_reference(verbose=True))
+    print(build_reference_cupy_kernel(verbose=True))
 
 
 if __name__ == "__main__":
