@@ -182,6 +182,7 @@ def reference_gpu_baseline(s, pairs, d_flat, d_off, d_len, stream, n_sample: int
     import torch
     from oracle import cupy_ref
     from clustkit_gb300.blosum import BLOSUM62
+    from clustkit_gb300.cells import pair_cells
     from clustkit_gb300.pairwise import PASS_CUPY, batch_sw
     if not cupy_ref.available():
         return {"unavailable": "oracle/_ref/sw_cupy_ref.cubin is built from the reference checkout, absent here"}
