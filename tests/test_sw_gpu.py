@@ -352,3 +352,24 @@ def test_streamed_wave_many_small_pairs(ck, bw):
         c = ck.sw_counters()
     assert c["wave"] == c["batched"]
     _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+
+
+@pytest.mark.parametrize("bw", [50, 100, 128])
+def test_reference_cupy_kernel_agrees(ck, bw):
+    """clustkit's own CuPy SW kernel (built from the reference checkout into
+    oracle/_ref/, launched with its batching by oracle/cupy_ref.py) gives the
+    same identities and pass/fail as this engine under the CuPy pass rule."""
+    import torch
+    from oracle import cupy_ref
+    if not cupy_ref.available():
+        pytest.skip("oracle/_ref/sw_cupy_ref.cubin is built only where the reference checkout exists")
+    s = synth.generate_families(80, 10, median=250, lo=10, hi=1200, seed=bw)
+    pairs = synth.mixed_pairs(s, 30000, seed=bw)
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    k = cupy_ref.CupyPathKernel()
+    plan = k.prepare(pairs, s.lengths, bw, BLOSUM62)
+    k.launch(plan, T(s.flat), T(s.offsets), T(s.lengths), 0.3, torch.cuda.current_stream(dev).cuda_stream)
+    sims, mask = k.results(plan)
+    ours = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, 0.3, pass_rule=PASS_CUPY)
+    assert np.array_equal(sims, ours["sims"]) and np.array_equal(mask, ours["mask"])
