@@ -483,11 +483,14 @@ __global__ void nbr_enum_kernel(const uint8_t *__restrict__ qflat, int64_t qflat
 
 // A warp per listed 5-mer: its posting list's targets each gain its score.
 // Query q's entries are list[item[q * stride] .. item[(q + 1) * stride]).
+__global__ void fill_kernel(int32_t *a, int32_t n, int32_t v) {
+    for (int32_t i = threadIdx.x; i < n; i += blockDim.x) a[i] = v;
+}
+
 __global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int64_t *__restrict__ item,
                                     int64_t stride, const int64_t *__restrict__ kmer_offsets,
                                     const int64_t *__restrict__ kmer_entries, int32_t num_db,
-                                    int32_t *__restrict__ counts, int32_t min_hits, int32_t *__restrict__ cand,
-                                    int32_t *__restrict__ n_cand, int32_t *err) {
+                                    int32_t *__restrict__ counts, int32_t *err) {
     const int32_t q = blockIdx.y;
     const int lane = threadIdx.x & 31;
     const int64_t e0 = item[(int64_t)q * stride], e1 = item[(int64_t)(q + 1) * stride];
@@ -500,11 +503,10 @@ __global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int
         for (int64_t h = b + lane; h < en; h += 32) {
             const int32_t t = (int32_t)(kmer_entries[h] >> 32);
             if (t < 0 || t >= num_db) { atomicOr(err, ERRBIT_PAIR_INDEX); continue; }
-            const int32_t old = atomicAdd(&c[t], w);
-            if (old < min_hits && old + w >= min_hits) {
-                const int32_t pos = atomicAdd(&n_cand[q], 1);
-                if (pos < CAND_CAP) cand[(int64_t)q * CAND_CAP + pos] = t;
-            }
+            // no candidate list here (most of the database crosses min_hits in
+            // this mode; the select scans the row): the add's result is unused,
+            // so it issues as a reduction
+            atomicAdd(&c[t], w);
         }
     }
 }
@@ -584,8 +586,10 @@ static int32_t phase_a_impl(void *pv) {
             if (by > by_cap) by = by_cap;
             if (by < 1) by = 1;
             nbr_postings_kernel<<<dim3((unsigned)by, (unsigned)a.nq), 256, 0, a.st>>>(
-                list, item, stride, a.kmer_offsets, a.kmer_entries, a.num_db, counts, a.min_hits, cand, n_cand,
-                err);
+                list, item, stride, a.kmer_offsets, a.kmer_entries, a.num_db, counts, err);
+            CK_CUDA(cudaGetLastError());
+            // the select scans the whole count row (no candidate list in this mode)
+            fill_kernel<<<1, 256, 0, a.st>>>(n_cand, a.nq, CAND_CAP + 1);
             CK_CUDA(cudaGetLastError());
         }
     }
