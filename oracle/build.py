@@ -11,6 +11,9 @@ legs).  Nothing in the product library links or loads them.
   straight from the reference checkout (read in place, never copied), with the
   reference's own build line (clustkit/csrc/sw_align.c:10) minus
   ``-march=native``.  Built only when the reference checkout exists.
+* ``oracle/_ref/kmer_score_ref.so`` -- ``clustkit/csrc/kmer_score.c``, the
+  reference's C k-mer scorer (Phase A, top-K, Phase B, diagonal hints), for
+  the golden vectors of the search path's candidate stage.
 * ``oracle/_ref/sw_cupy_ref.cubin`` -- the reference's CuPy SW kernel
   (the ``_SW_ALIGN_KERNEL_CODE`` string, clustkit/pairwise.py:1215-1402, read
   from the checkout with ``ast``, never imported), compiled by nvcc for
@@ -64,6 +67,21 @@ def build_reference(verbose: bool = False) -> Path | None:
     return out
 
 
+def build_reference_kmer_scorer(verbose: bool = False) -> Path | None:
+    """Compile the reference's C k-mer scorer (clustkit/csrc/kmer_score.c) into oracle/_ref/."""
+    src = REF_SRC.parent / "kmer_score.c"
+    if not src.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    out = REF_OUT / "kmer_score_ref.so"
+    if _needs(out, src):
+        cmd = ["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-o", str(out), str(src)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    return out
+
+
 def build_reference_cupy_kernel(verbose: bool = False) -> Path | None:
     """Compile the reference's CuPy kernel string into oracle/_ref/sw_cupy_ref.cubin."""
     import ast
@@ -96,6 +114,7 @@ def main() -> None:
     print(build_oracle(verbose=True))
     print(build_reference(verbose=True))
     print(build_reference_cupy_kernel(verbose=True))
+    print(build_reference_kmer_scorer(verbose=True))
 
 
 if __name__ == "__main__":

@@ -15,6 +15,13 @@ project root.
   clustkit/kmer_index.py:1187-1291 (every 5-mer whose column-sum score against
   the query 5-mer is >= the threshold adds that score per posting) with the
   cap of :1320-1328
+* ``kmer_candidates``       -- the C scorer's per-query candidates
+  (clustkit/csrc/kmer_score.c:195-415, ``score_query_full``): Phase A, the
+  top ``phase_a_topk`` by (count desc, id asc), Phase B -- per target the
+  longest run of hits on one diagonal bin ``(tpos - qpos + qlen) //
+  diag_bin_width``, first bin on ties -- kept at >= ``min_diag_hits``, the
+  diagonal hint ``bin * width - qlen + width // 2``, and the ``max_cands``
+  cap by (score desc, id asc)
 * ``rank_hits``             -- the E-value-style rank of
   clustkit/kmer_index.py:2318-2323 and the top-k collection of
   clustkit/search.py:727-800
@@ -140,3 +147,59 @@ def rank_hits(pairs, sims, scores, q_lengths, t_lengths, nq, top_k):
         if len(hits[q]) < top_k:
             hits[q].append((int(pairs[idx, 1]), float(sims[idx]), float(rank[idx])))
     return hits
+
+
+def _top_by_score(ids, sc, k):
+    """kmer_score.c:148-193: all in the given order when n <= k, else the top k by
+    (score desc, id asc) in that order."""
+    if len(ids) <= k:
+        return np.arange(len(ids))
+    return np.lexsort((ids, -sc))[:k]
+
+
+def kmer_candidates(query, k, alpha, kmer_offsets, kmer_entries, kmer_freqs, freq_thresh, num_db,
+                    min_total_hits, min_diag_hits, diag_bin_width, max_cands, phase_a_topk):
+    """(ids, scores, diags); diags are 0 when min_diag_hits <= 1 (the C scorer leaves them unset)."""
+    q = np.asarray(query)
+    v, ok = kmer_values(q, k, alpha)
+    counts = np.zeros(num_db, np.int64)
+    post = []  # (qpos, entries) of the valid, frequency-capped k-mers
+    for p in np.nonzero(ok)[0]:
+        val = v[p]
+        if kmer_freqs[val] > freq_thresh:
+            continue
+        e = kmer_entries[kmer_offsets[val]:kmer_offsets[val + 1]]
+        np.add.at(counts, (e >> 32).astype(np.int64), 1)
+        post.append((int(p), e))
+    counts = np.minimum(counts, 32767)
+    ids = np.nonzero(counts >= min_total_hits)[0]
+    sc = counts[ids]
+    empty = np.empty(0, np.int32)
+    if len(ids) == 0:
+        return empty, empty, empty
+    if min_diag_hits <= 1:
+        o = _top_by_score(ids, sc, max_cands)
+        return ids[o].astype(np.int32), sc[o].astype(np.int32), np.zeros(len(o), np.int32)
+    sel = ids[_top_by_score(ids, sc, phase_a_topk)]
+    in_sel = np.zeros(num_db, bool)
+    in_sel[sel] = True
+    qlen = len(q)
+    runs = {}
+    for p, e in post:
+        t = (e >> 32).astype(np.int64)
+        m = in_sel[t]
+        tpos = (e[m] & 0xFFFFFFFF).astype(np.int64)
+        for tid, b in zip(t[m], (tpos - p + qlen) // diag_bin_width):
+            runs[(int(tid), int(b))] = runs.get((int(tid), int(b)), 0) + 1
+    best = {}
+    for (tid, b) in sorted(runs):
+        c = runs[(tid, b)]
+        if tid not in best or c > best[tid][0]:
+            best[tid] = (c, b)
+    fid = np.array([t for t in sorted(best) if best[t][0] >= min_diag_hits], np.int64)
+    if len(fid) == 0:
+        return empty, empty, empty
+    fsc = np.array([best[t][0] for t in fid], np.int64)
+    fdg = np.array([best[t][1] * diag_bin_width - qlen + diag_bin_width // 2 for t in fid], np.int64)
+    o = _top_by_score(fid, fsc, max_cands)
+    return fid[o].astype(np.int32), fsc[o].astype(np.int32), fdg[o].astype(np.int32)

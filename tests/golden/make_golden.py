@@ -18,6 +18,7 @@ Outputs (all small, compressed):
   blosum62_ref.npy      the reference's BLOSUM62 table
   sketch_golden.npz     sequences + reference sketches for several (k, s, alphabet)
   jaccard_golden.npz    sketch pairs + reference _batch_jaccard values
+  kmer_scorer_golden.npz  the reference's C k-mer scorer (Phase A/B, caps, hints)
   sw_golden.npz         sequences, pairs, band widths + reference C SW outputs,
                         a diagonal-hint case, and a Numba-twin cross-check subset
   lsh_golden.npz        reference lsh_candidates on the sketches
@@ -352,6 +353,71 @@ def make_search_golden(rpw):
                         hit_query=np.array(hq, np.int32), hit_target=np.array(ht, np.int32),
                         hit_identity=np.array(hid, np.float64), hit_score=np.array(hsc, np.float64),
                         top_k=np.int32(5), **phase, **sim)
+
+
+def make_kmer_scorer_golden(rpw):
+    """clustkit's C k-mer scorer (csrc/kmer_score.c, batch_score_queries_c --
+    Phase A, top-K, Phase B diagonal scoring, diagonal hints) compiled from the
+    checkout into oracle/_ref/, on a family database large enough for every cap
+    to bind; plus the Numba two-stage scorer (kmer_index.py:654-829) where no
+    cap binds."""
+    import ctypes
+    import clustkit.kmer_index as rki
+    sys.path.insert(0, str(REPO))
+    import oracle.build as obuild
+    from clustkit_gb300 import synth
+    lib = ctypes.CDLL(str(obuild.build_reference_kmer_scorer()))
+    db = synth.generate_families(600, 8, median=150, lo=30, hi=400, seed=707)
+    rng = np.random.default_rng(708)
+    qs = []
+    for i in rng.choice(db.n, 8, replace=False):
+        q = db.seq(int(i)).copy()
+        m = rng.random(len(q)) < rng.uniform(0.05, 0.4)
+        q[m] = rng.integers(0, 20, int(m.sum()))
+        qs.append(q.astype(np.uint8))
+    bg = synth.random_sequences(4, median=200, lo=60, hi=400, seed=709)
+    qs += [bg.seq(i).copy() for i in range(bg.n)]
+    qs.append(np.concatenate([db.seq(3)[:60], np.full(3, 20, np.uint8), db.seq(3)[60:]]).astype(np.uint8))
+    qs.append(np.array([5, 6, 7], np.uint8))
+    qflat, qoff, qlen = pack(qs)
+    k = 5
+    koff, kent, kfreq = rki.build_kmer_index(db.flat, db.offsets, db.lengths, k, "protein")
+    thr = int(rki.compute_freq_threshold(kfreq, db.n, 95.0))
+    # (min_total_hits, min_diag_hits, diag_bin_width, max_cands, phase_a_topk)
+    configs = [(2, 1, 10, 100000, 10000), (2, 1, 10, 17, 10000), (2, 2, 10, 100000, 10000),
+               (2, 2, 10, 11, 40), (1, 3, 7, 25, 200), (3, 2, 16, 6, 9)]
+    P, I32 = ctypes.c_void_p, ctypes.c_int32
+    lib.batch_score_queries_c.restype = None
+    lib.batch_score_queries_c.argtypes = [P, P, P, I32, I32, I32, P, P, P, P, I32, I32, I32, I32, I32, I32, I32,
+                                          P, P, P, P]
+    out = {}
+    nq = len(qs)
+    qoff64 = qoff.astype(np.int64)
+    qlen32 = qlen.astype(np.int32)
+    for ci, (mth, mdh, dbw, mc, topk) in enumerate(configs):
+        tg = np.full((nq, mc), -1, np.int32)
+        cnt = np.zeros(nq, np.int32)
+        sc = np.zeros((nq, mc), np.int32)
+        dg = np.zeros((nq, mc), np.int32)
+        lib.batch_score_queries_c(qflat.ctypes.data, qoff64.ctypes.data, qlen32.ctypes.data, nq, k, 20,
+                                  koff.ctypes.data, kent.ctypes.data, None, kfreq.ctypes.data, thr, db.n, mth, mdh,
+                                  dbw, mc, topk, tg.ctypes.data, cnt.ctypes.data, sc.ctypes.data, dg.ctypes.data)
+        for qi in range(nq):
+            n = int(cnt[qi])
+            out[f"c{ci}_q{qi}_targets"] = tg[qi, :n].copy()
+            out[f"c{ci}_q{qi}_scores"] = sc[qi, :n].copy()
+            out[f"c{ci}_q{qi}_diags"] = dg[qi, :n].copy()
+    for qi in range(nq):  # Numba two-stage, config 2 (no cap binds)
+        ids, sc = rki._score_query_two_stage(qs[qi], np.int32(len(qs[qi])), np.int32(k), np.int32(20), koff, kent,
+                                             kfreq, np.int32(thr), np.int32(db.n), np.int32(2), np.int32(2),
+                                             np.int32(10), np.int32(10000))
+        out[f"numba_q{qi}_ids"] = np.asarray(ids, np.int32)
+        out[f"numba_q{qi}_scores"] = np.asarray(sc, np.int32)
+    np.savez_compressed(HERE / "kmer_scorer_golden.npz", db_flat=db.flat, db_offsets=db.offsets,
+                        db_lengths=db.lengths, q_flat=qflat, q_offsets=qoff, q_lengths=qlen,
+                        configs=np.array(configs, np.int32), freq_thresh=np.int32(thr), **out)
+    print("kmer scorer golden:", {f"c{ci}": int(sum(len(out[f'c{ci}_q{q}_targets']) for q in range(nq)))
+                                  for ci in range(len(configs))})
 
 
 if __name__ == "__main__":

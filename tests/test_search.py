@@ -310,3 +310,24 @@ def test_similar_phase_a_cap_vs_oracle(ck, thresh):
             slot.results(3)
         finally:
             slot.close()
+
+
+def test_oracle_kmer_candidates_match_reference_c_scorer(golden):
+    """The numpy restatement of clustkit's C k-mer scorer (Phase A, top-K,
+    Phase B, diagonal hints, caps) against the compiled reference scorer, and
+    the reference's Numba two-stage scorer where no cap binds."""
+    g = golden("kmer_scorer_golden.npz")
+    off, ent, fr = so.build_kmer_index(g["db_flat"], g["db_offsets"], g["db_lengths"], 5)
+    qs = _queries(g)
+    nd = len(g["db_lengths"])
+    for ci, (mth, mdh, dbw, mc, topk) in enumerate(g["configs"]):
+        for qi, q in enumerate(qs):
+            ids, sc, dg = so.kmer_candidates(q, 5, 20, off, ent, fr, int(g["freq_thresh"]), nd, int(mth), int(mdh),
+                                             int(dbw), int(mc), int(topk))
+            assert np.array_equal(ids, g[f"c{ci}_q{qi}_targets"]), (ci, qi)
+            assert np.array_equal(sc, g[f"c{ci}_q{qi}_scores"]), (ci, qi)
+            if mdh >= 2:
+                assert np.array_equal(dg, g[f"c{ci}_q{qi}_diags"]), (ci, qi)
+    for qi in range(len(qs)):
+        assert np.array_equal(g[f"numba_q{qi}_ids"], g[f"c2_q{qi}_targets"])
+        assert np.array_equal(g[f"numba_q{qi}_scores"], g[f"c2_q{qi}_scores"])
