@@ -207,6 +207,7 @@ enum ScratchSlot {
     SLOT_MAXLEN,
     SLOT_SEARCH_COUNTS,
     SLOT_SEARCH_CAND,
+    SLOT_SEARCH_IDX,
     SLOT_SEARCH_TMP0,
     SLOT_SEARCH_TMP1,
     SLOT_SEARCH_TMP2,

@@ -15,6 +15,7 @@
 #include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <cub/device/device_segmented_sort.cuh>
 
 #include <algorithm>
 #include <vector>
@@ -292,7 +293,8 @@ __global__ void __launch_bounds__(SELECT_THREADS)
 phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t top_k,
                       int32_t clamp, int32_t top_shift, const int32_t *__restrict__ cand,
                       const int32_t *__restrict__ n_cand, int32_t *__restrict__ out_targets,
-                      int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n) {
+                      int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n,
+                      int32_t *__restrict__ capped_n) {
     using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
     __shared__ typename BlockScan::TempStorage scan_tmp;
     __shared__ uint64_t s_buf[CAND_CAP];  // sorted candidate ids, later the capped output's sort keys
@@ -402,7 +404,37 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
             if (o_s) o_s[i] = 0x7fffffff - (int32_t)(s_buf[i] >> 32);
         }
     }
-    if (tid == 0) out_n[q] = n_out;
+    if (tid == 0) {
+        out_n[q] = n_out;
+        if (capped_n) capped_n[q] = (total > top_k && top_k > CAND_CAP) ? n_out : 0;
+    }
+}
+
+// Rows capped at more than CAND_CAP targets leave the select in id order; a
+// segmented sort of (score desc, id asc) keys puts them in the order the
+// shorter capped rows get in shared memory.  Rows that were not capped are
+// empty segments.
+__global__ void cap_keys_kernel(const int32_t *__restrict__ t, const int32_t *__restrict__ sc,
+                                const int32_t *__restrict__ capped_n, int32_t top_k, uint64_t *__restrict__ keys,
+                                int32_t *__restrict__ beg, int32_t *__restrict__ end) {
+    const int32_t q = blockIdx.y;
+    const int32_t n = capped_n[q];
+    const int64_t row = (int64_t)q * top_k;
+    if (blockIdx.x == 0 && threadIdx.x == 0) { beg[q] = (int32_t)row; end[q] = (int32_t)(row + n); }
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        keys[row + j] = ((uint64_t)(uint32_t)(0x7fffffff - sc[row + j]) << 32) | (uint32_t)t[row + j];
+}
+
+__global__ void cap_unpack_kernel(const uint64_t *__restrict__ keys, const int32_t *__restrict__ capped_n,
+                                  int32_t top_k, int32_t *__restrict__ t, int32_t *__restrict__ sc) {
+    const int32_t q = blockIdx.y;
+    const int32_t n = capped_n[q];
+    const int64_t row = (int64_t)q * top_k;
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[row + j];
+        t[row + j] = (int32_t)(k & 0xffffffffu);
+        sc[row + j] = 0x7fffffff - (int32_t)(k >> 32);
+    }
 }
 
 // ----------------------------------------------------------------- similar k-mers
@@ -511,6 +543,115 @@ __global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int
     }
 }
 
+// ----------------------------------------------------------------- Phase B
+// clustkit's C scorer (csrc/kmer_score.c:195-415): after Phase A the top
+// phase_a_topk targets by (count desc, id asc) are rescored by their hits'
+// diagonals -- per target the longest run of hits in one diagonal bin
+// (tpos - qpos + qlen) / diag_bin_width, the first such bin on ties -- and
+// kept when that run reaches min_diag_hits, with the diagonal hint
+// bin * width - qlen + width / 2.  Here every selected target owns a dense
+// row of bin counters (its bins: (qlen + tlen) / width + 1), found through a
+// per-query target -> selection-index row.
+__global__ void pb_mark_kernel(const int32_t *__restrict__ sel, const int32_t *__restrict__ sel_n, int32_t topk,
+                               const int32_t *__restrict__ db_len, const int32_t *__restrict__ qlen, int32_t width,
+                               int32_t num_db, int32_t *__restrict__ idx_row, int64_t *__restrict__ nbins) {
+    const int32_t q = blockIdx.y;
+    const int32_t n = sel_n[q];
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < topk; i += gridDim.x * blockDim.x) {
+        int64_t nb = 0;
+        if (i < n) {
+            const int32_t t = sel[(int64_t)q * topk + i];
+            idx_row[(int64_t)q * num_db + t] = i;
+            nb = (int64_t)(qlen[q] + db_len[t]) / width + 1;
+        }
+        nbins[(int64_t)q * topk + i] = nb;
+    }
+}
+
+__global__ void pb_bin_count_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len,
+                                    const int64_t *__restrict__ qoff, const int32_t *__restrict__ qlen, int32_t k,
+                                    int32_t alpha, const int64_t *__restrict__ kmer_offsets,
+                                    const int64_t *__restrict__ kmer_entries, const int32_t *__restrict__ kmer_freqs,
+                                    int32_t freq_thresh, int32_t num_db, const int32_t *__restrict__ idx_row,
+                                    int32_t topk, const int64_t *__restrict__ base, int32_t width,
+                                    int32_t *__restrict__ bins, int32_t *err) {
+    const int32_t q = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int32_t L = qlen[q];
+    const int64_t o = qoff[q];
+    if (L < 0 || o < 0 || o + L > qflat_len) {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERRBIT_SEQ_EXTENT);
+        return;
+    }
+    const uint8_t *s = qflat + o;
+    const int32_t *ix = idx_row + (int64_t)q * num_db;
+    const int64_t *bq = base + (int64_t)q * topk;
+    const int32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p <= L - k; p += warps) {
+        uint32_t v = 0;
+        bool ok = true;
+        for (int32_t m = 0; m < k; ++m) {
+            const uint32_t r = s[p + m];
+            ok &= r < (uint32_t)alpha;
+            v = v * (uint32_t)alpha + r;
+        }
+        if (!ok || kmer_freqs[v] > freq_thresh) continue;
+        const int64_t b = kmer_offsets[v], e = kmer_offsets[v + 1];
+        for (int64_t h = b + lane; h < e; h += 32) {
+            const int64_t entry = kmer_entries[h];
+            const int32_t t = (int32_t)(entry >> 32);
+            if (t < 0 || t >= num_db) { atomicOr(err, ERRBIT_PAIR_INDEX); continue; }
+            const int32_t i = ix[t];
+            if (i < 0) continue;
+            const int64_t dbin = ((int64_t)(int32_t)(entry & 0xffffffff) - p + L) / width;
+            const int64_t at = bq[i] + dbin;
+            if (dbin < 0 || at >= bq[i + 1]) { atomicOr(err, ERRBIT_SEQ_EXTENT); continue; }
+            atomicAdd(&bins[at], 1);
+        }
+    }
+}
+
+// A warp per selected target: its longest run (first bin on ties); kept ones
+// are written into the (cleared) count row and listed for the final selection.
+__global__ void pb_best_kernel(const int32_t *__restrict__ sel, const int32_t *__restrict__ sel_n, int32_t topk,
+                               const int64_t *__restrict__ base, const int32_t *__restrict__ bins,
+                               const int32_t *__restrict__ qlen, int32_t width, int32_t min_diag_hits,
+                               int32_t num_db, int32_t *__restrict__ counts, int32_t *__restrict__ hint_sel,
+                               int32_t *__restrict__ cand, int32_t *__restrict__ n_cand) {
+    const int32_t q = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int32_t n = sel_n[q];
+    const int32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const int64_t b0 = base[(int64_t)q * topk + i], b1 = base[(int64_t)q * topk + i + 1];
+        int32_t best = 0, first = INT32_MAX;
+        for (int64_t x = b0 + lane; x < b1; x += 32) {
+            const int32_t c = bins[x];
+            if (c > best) { best = c; first = (int32_t)(x - b0); }
+        }
+        const int32_t m = __reduce_max_sync(0xffffffffu, best);
+        const int32_t fb = __reduce_min_sync(0xffffffffu, (best == m && m > 0) ? first : INT32_MAX);
+        if (lane == 0 && m >= min_diag_hits && m > 0) {
+            const int32_t t = sel[(int64_t)q * topk + i];
+            counts[(int64_t)q * num_db + t] = m;
+            hint_sel[(int64_t)q * topk + i] = fb * width - qlen[q] + width / 2;
+            const int32_t at = atomicAdd(&n_cand[q], 1);
+            if (at < CAND_CAP) cand[(int64_t)q * CAND_CAP + at] = t;
+        }
+    }
+}
+
+__global__ void pb_hints_kernel(const int32_t *__restrict__ out_t, const int32_t *__restrict__ out_n, int32_t mc,
+                                const int32_t *__restrict__ idx_row, int32_t num_db,
+                                const int32_t *__restrict__ hint_sel, int32_t topk, int32_t *__restrict__ out_d) {
+    const int32_t q = blockIdx.y;
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < out_n[q]; j += gridDim.x * blockDim.x) {
+        const int32_t t = out_t[(int64_t)q * mc + j];
+        const int32_t i = idx_row[(int64_t)q * num_db + t];
+        out_d[(int64_t)q * mc + j] = i >= 0 ? hint_sel[(int64_t)q * topk + i] : 0;
+    }
+}
+
 struct PhaseAArgs {
     const int8_t *sub_host; int32_t score_thresh;  // similar k-mers when sub_host != nullptr
     const uint8_t *qflat; int64_t qflat_len; const int64_t *qoff; const int32_t *qlen; int32_t nq; int32_t max_qlen;
@@ -518,6 +659,44 @@ struct PhaseAArgs {
     const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
     int32_t *out_targets; int32_t *out_scores; int32_t *out_n; cudaStream_t st;
 };
+
+// The select, then the order of rows capped above CAND_CAP (when scores are
+// written; without them only the set matters).
+static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, int32_t min_hits, int32_t top_k,
+                           int32_t clamp, int32_t top_shift, const int32_t *cand, const int32_t *n_cand,
+                           int32_t *out_t, int32_t *out_s, int32_t *out_n, cudaStream_t st) {
+    int32_t status = CK_OK;
+    const bool sort = top_k > CAND_CAP && out_s;
+    int32_t *aux = nullptr;
+    if (sort) {
+        if ((int64_t)nq * top_k >= INT32_MAX) {
+            set_error(CK_ERR_UNSUPPORTED, "search select: nq * top_k must stay below 2^31");
+            return CK_ERR_UNSUPPORTED;
+        }
+        aux = (int32_t *)scratch(SLOT_SEARCH_TMP3, (size_t)nq * 12, &status);
+        if (!aux) return status;
+    }
+    phase_a_select_kernel<<<nq, SELECT_THREADS, 0, st>>>(counts, num_db, min_hits, top_k, clamp, top_shift, cand,
+                                                         n_cand, out_t, out_s, out_n, aux);
+    CK_CUDA(cudaGetLastError());
+    if (!sort) return CK_OK;
+    const size_t items = (size_t)nq * top_k;
+    uint64_t *k0 = (uint64_t *)scratch(SLOT_SORT_KEYS, items * 8, &status);
+    uint64_t *k1 = (uint64_t *)scratch(SLOT_SORT_KEYS_ALT, items * 8, &status);
+    if (!k0 || !k1) return status;
+    int32_t *beg = aux + nq, *end = aux + 2 * (size_t)nq;
+    const dim3 g((unsigned)std::min(64, (top_k + 255) / 256), (unsigned)nq);
+    cap_keys_kernel<<<g, 256, 0, st>>>(out_t, out_s, aux, top_k, k0, beg, end);
+    CK_CUDA(cudaGetLastError());
+    size_t tb = 0;
+    CK_CUDA(cub::DeviceSegmentedSort::SortKeys(nullptr, tb, k0, k1, (int)items, nq, beg, end, st));
+    void *tmp = scratch(SLOT_SORT_TEMP, tb, &status);
+    if (!tmp) return status;
+    CK_CUDA(cub::DeviceSegmentedSort::SortKeys(tmp, tb, k0, k1, (int)items, nq, beg, end, st));
+    cap_unpack_kernel<<<g, 256, 0, st>>>(k1, aux, top_k, out_t, out_s);
+    CK_CUDA(cudaGetLastError());
+    return CK_OK;
+}
 
 static int32_t phase_a_impl(void *pv) {
     PhaseAArgs &a = *(PhaseAArgs *)pv;
@@ -593,11 +772,8 @@ static int32_t phase_a_impl(void *pv) {
             CK_CUDA(cudaGetLastError());
         }
     }
-    phase_a_select_kernel<<<a.nq, SELECT_THREADS, 0, a.st>>>(counts, a.num_db, a.min_hits, a.top_k, clamp,
-                                                             top_shift, cand, n_cand, a.out_targets,
-                                                             a.out_scores, a.out_n);
-    CK_CUDA(cudaGetLastError());
-    return CK_OK;
+    return select_rows(counts, a.nq, a.num_db, a.min_hits, a.top_k, clamp, top_shift, cand, n_cand,
+                       a.out_targets, a.out_scores, a.out_n, a.st);
 }
 
 }  // namespace ck
@@ -665,4 +841,113 @@ extern "C" int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *
                  20, d_kmer_offsets, d_kmer_entries, d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k,
                  d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream};
     return run_in_context(ctx, phase_a_impl, &a);
+}
+
+namespace ck {
+
+struct CandArgs {
+    PhaseAArgs a;  // Phase A part (sub_host null); top_k there = max_cands
+    const int32_t *db_len; int32_t min_diag_hits, width, phase_a_topk; int32_t *out_diags;
+};
+
+static int32_t candidates_impl(void *pv) {
+    CandArgs &c = *(CandArgs *)pv;
+    PhaseAArgs &a = c.a;
+    int32_t status = CK_OK;
+    const size_t nq = (size_t)a.nq;
+    if (c.min_diag_hits <= 1) {  // Phase A and the cap, hints zero
+        CK_TRY(phase_a_impl(&a));
+        if (c.out_diags && a.nq > 0) CK_CUDA(cudaMemsetAsync(c.out_diags, 0, nq * a.top_k * 4, a.st));
+        return CK_OK;
+    }
+    int32_t *err = device_error_word(&status);
+    if (!err) return status;
+    if (a.nq == 0) return CK_OK;
+    const int32_t topk = c.phase_a_topk;
+    // Phase A with the Phase-B top-K as its cap, into the selection buffers
+    int32_t *sel = (int32_t *)scratch(SLOT_SEARCH_TMP2, nq * topk * 4 + nq * 4, &status);
+    int64_t *base = (int64_t *)scratch(SLOT_SEARCH_TMP4, (nq * topk + 1) * 8, &status);
+    int32_t *hint_sel = (int32_t *)scratch(SLOT_SEARCH_TMP0, nq * topk * 4, &status);
+    int32_t *idx_row = (int32_t *)scratch(SLOT_SEARCH_IDX, nq * (size_t)a.num_db * 4 + 4, &status);
+    if (!sel || !base || !hint_sel || !idx_row) return status;
+    int32_t *sel_n = sel + nq * topk;
+    PhaseAArgs a1 = a;
+    a1.top_k = topk;
+    a1.out_targets = sel;
+    a1.out_scores = nullptr;
+    a1.out_n = sel_n;
+    CK_TRY(phase_a_impl(&a1));
+    int32_t *counts = (int32_t *)scratch(SLOT_SEARCH_COUNTS, nq * (size_t)a.num_db * 4 + 4, &status);
+    if (!counts) return status;
+    CK_CUDA(cudaMemsetAsync(idx_row, 0xff, nq * (size_t)a.num_db * 4, a.st));
+    const dim3 g1((unsigned)std::min(64, (topk + 255) / 256), (unsigned)a.nq);
+    pb_mark_kernel<<<g1, 256, 0, a.st>>>(sel, sel_n, topk, c.db_len, a.qlen, c.width, a.num_db, idx_row, base);
+    CK_CUDA(cudaGetLastError());
+    // bin offsets: one exclusive scan over every (query, selected target); the
+    // trailing entry is the total
+    CK_CUDA(cudaMemsetAsync(base + nq * topk, 0, 8, a.st));
+    size_t tb = 0;
+    CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, base, base, (int64_t)(nq * topk + 1), a.st));
+    void *tmp = scratch(SLOT_SORT_TEMP, tb, &status);
+    if (!tmp) return status;
+    CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, base, base, (int64_t)(nq * topk + 1), a.st));
+    int64_t total = 0;
+    CK_CUDA(cudaMemcpyAsync(&total, base + nq * topk, 8, cudaMemcpyDeviceToHost, a.st));
+    CK_CUDA(cudaStreamSynchronize(a.st));
+    int32_t *bins = (int32_t *)scratch(SLOT_SEARCH_TMP1, (size_t)(total > 0 ? total : 1) * 4, &status);
+    if (!bins) return status;
+    if (total > 0) CK_CUDA(cudaMemsetAsync(bins, 0, (size_t)total * 4, a.st));
+    const int32_t npos = a.max_qlen - a.k + 1;
+    if (npos > 0) {
+        int bx = (npos + 7) / 8;
+        if (bx > 16) bx = 16;
+        pb_bin_count_kernel<<<dim3((unsigned)bx, (unsigned)a.nq), 256, 0, a.st>>>(
+            a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha, a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
+            a.freq_thresh, a.num_db, idx_row, topk, base, c.width, bins, err);
+        CK_CUDA(cudaGetLastError());
+    }
+    // final cap over the kept targets: from their list, or a scan of the row
+    // when more than CAND_CAP were kept; runs are not clamped (int32 select)
+    int32_t *cand = (int32_t *)scratch(SLOT_SEARCH_CAND, nq * (CAND_CAP + 1) * 4, &status);
+    if (!cand) return status;
+    int32_t *n_cand = cand + nq * CAND_CAP;
+    CK_CUDA(cudaMemsetAsync(n_cand, 0, nq * 4, a.st));
+    CK_CUDA(cudaMemsetAsync(counts, 0, nq * (size_t)a.num_db * 4, a.st));
+    const dim3 g2((unsigned)std::min(64, (topk + 7) / 8), (unsigned)a.nq);
+    pb_best_kernel<<<g2, 256, 0, a.st>>>(sel, sel_n, topk, base, bins, a.qlen, c.width, c.min_diag_hits, a.num_db,
+                                         counts, hint_sel, cand, n_cand);
+    CK_CUDA(cudaGetLastError());
+    CK_TRY(select_rows(counts, a.nq, a.num_db, c.min_diag_hits, a.top_k, INT32_MAX, 24, cand, n_cand,
+                       a.out_targets, a.out_scores, a.out_n, a.st));
+    if (c.out_diags) {
+        const dim3 g3((unsigned)std::min(64, (a.top_k + 255) / 256), (unsigned)a.nq);
+        pb_hints_kernel<<<g3, 256, 0, a.st>>>(a.out_targets, a.out_n, a.top_k, idx_row, a.num_db, hint_sel, topk,
+                                              c.out_diags);
+        CK_CUDA(cudaGetLastError());
+    }
+    return CK_OK;
+}
+
+}  // namespace ck
+
+extern "C" int32_t ck_search_kmer_candidates_device(
+    int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len, const int64_t *d_qoffsets, const int32_t *d_qlengths,
+    int32_t nq, int32_t max_qlen, int32_t k, int32_t alpha, const int64_t *d_kmer_offsets,
+    const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+    const int32_t *d_db_lengths, int32_t min_total_hits, int32_t min_diag_hits, int32_t diag_bin_width,
+    int32_t max_cands, int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores, int32_t *d_out_diags,
+    int32_t *d_out_n, void *stream) {
+    std::lock_guard<std::mutex> lock(library_mutex());
+    reset_thread_status();
+    if (nq < 0 || nq > 65535 || qflat_len < 0 || max_cands < 1 || k < 1 || alpha < 1 || num_db < 0 ||
+        !d_out_targets || !d_out_n || (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets ||
+        !d_kmer_freqs || (min_diag_hits >= 2 && (!d_db_lengths || diag_bin_width < 1 || phase_a_topk < 1))) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "k-mer candidates: bad arguments");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    CandArgs c{PhaseAArgs{nullptr, 0, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha,
+                          d_kmer_offsets, d_kmer_entries, d_kmer_freqs, freq_thresh, num_db, min_total_hits, max_cands,
+                          d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream},
+               d_db_lengths, min_diag_hits, diag_bin_width, phase_a_topk, d_out_diags};
+    return run_in_context(ctx, candidates_impl, &c);
 }

@@ -11,6 +11,15 @@ query (:893-902, :1320-1328); banded Smith-Waterman with a positive score as
 pass (:2271-2280, pairwise.py:636-681); rank ``0.267 * score - ln(qlen *
 tlen)`` (:2318-2323) and the top-k hits per query (clustkit/search.py:727-800).
 
+With ``min_diag_hits >= 2`` (exact k-mers) or ``use_c_scoring`` the
+candidates come from the device twin of clustkit's C k-mer scorer
+(clustkit/csrc/kmer_score.c:195-470; its Numba two-stage scorer,
+kmer_index.py:262-410, selects the same targets): Phase A, the top
+``phase_a_topk`` by hits, Phase B's longest diagonal-bin run per target and
+its diagonal hint.  ``use_c_sw`` aligns with clustkit's C SW settings
+(kmer_index.py:2230-2266): band ``c_sw_band_width`` and, with
+``use_c_scoring``, the Phase-B hints as band centres.
+
 Differences, by design:
 * candidates above the cap are the top ones by score, in score order as
   clustkit gives them, with ties to the lower target id (clustkit's order
@@ -51,6 +60,39 @@ def compute_freq_threshold(kmer_freqs, num_sequences: int, percentile: float = 9
         return int(num_sequences)
     pctl = int(np.percentile(nonzero, percentile))
     return int(max(pctl, max(100, num_sequences // 200)))
+
+
+@dataclass(frozen=True)
+class Scoring:
+    """k-mer scoring and alignment settings of a search, with the meaning of
+    clustkit's search_kmer_index keywords (clustkit/kmer_index.py:1475-1501)."""
+    min_total_hits: int = 2
+    kmer_score_thresh: int = 0
+    min_diag_hits: int = 1
+    diag_bin_width: int = 10
+    phase_a_topk: int = 10000
+    use_c_scoring: bool = False
+    use_c_sw: bool = False
+    c_sw_band_width: int = 50
+
+    @property
+    def similar(self) -> bool:
+        return self.kmer_score_thresh > 0
+
+    @property
+    def diagonal(self) -> bool:
+        """Candidates from the C-scorer twin (Phase B when min_diag_hits >= 2)."""
+        return not self.similar and (self.min_diag_hits >= 2 or self.use_c_scoring)
+
+    @property
+    def hints(self) -> bool:
+        """Phase-B diagonal hints centre the alignment bands."""
+        return self.use_c_sw and self.use_c_scoring and not self.similar
+
+    @property
+    def graphable(self) -> bool:
+        """No host synchronisation in the pipeline: exact Phase A, the database band."""
+        return not self.similar and not self.diagonal and not self.use_c_sw
 
 
 def _torch():
@@ -162,6 +204,7 @@ class _Slot:
         dev = db.dev
         self.d_targets = torch.empty(Q * K, dtype=torch.int32, device=dev)
         self.d_counts = torch.empty(Q * K, dtype=torch.int32, device=dev)
+        self.d_diags = torch.zeros(Q * K, dtype=torch.int32, device=dev)
         self.d_n = torch.empty(Q, dtype=torch.int32, device=dev)
         self.d_pairs = torch.empty((Q * K, 2), dtype=torch.int32, device=dev)
         self.d_sims = torch.empty(Q * K, dtype=torch.float32, device=dev)
@@ -240,10 +283,11 @@ class _Slot:
         hl[nq:n_all] = 0
         return nq, lens, tot
 
-    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, min_total_hits: int, kmer_score_thresh: int = 0):
+    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, sc: Scoring):
         """The device pipeline of a batch of nq queries on this slot's stream:
-        H2D, Phase A, pair list, SW, D2H.  No host synchronisation, so it can
-        be captured in a CUDA graph."""
+        H2D, k-mer scoring, pair list, SW, D2H.  For exact Phase A with the
+        database band there is no host synchronisation, so it can be captured
+        in a CUDA graph."""
         torch = _torch()
         db = self.db
         K = self.max_cands
@@ -257,17 +301,26 @@ class _Slot:
         qoff_ptr = db.d_offsets.data_ptr() + self.seq0 * 8
         qlen_ptr = db.d_lengths.data_ptr() + self.seq0 * 4
         self._mark(1)
-        if kmer_score_thresh > 0:  # BLOSUM62 similar k-mers (k = 5), clustkit's default scoring
+        min_total_hits = int(sc.min_total_hits)
+        if sc.similar:  # BLOSUM62 similar k-mers (k = 5), clustkit's default scoring
             _lib.check(lib.ck_search_phase_a_similar_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen, _SUB.ctypes.data,
-                int(kmer_score_thresh), db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
-                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
+                int(sc.kmer_score_thresh), db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+        elif sc.diagonal:  # the C scorer's Phase A + Phase B, with diagonal hints
+            _lib.check(lib.ck_search_kmer_candidates_device(
+                self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
+                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, db.d_lengths.data_ptr(), min_total_hits,
+                int(sc.min_diag_hits), int(sc.diag_bin_width), K, int(sc.phase_a_topk),
+                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_diags.data_ptr(),
+                self.d_n.data_ptr(), st))
         else:
             _lib.check(lib.ck_search_phase_a_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
                 db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
-                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, int(min_total_hits), K,
+                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
         self._mark(2)
         # dense pair list: (query, target) or (empty, empty) past a query's candidates
@@ -277,8 +330,9 @@ class _Slot:
         self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M], torch.full_like(q, db.empty_idx))
         _lib.check(lib.ck_sw_batch_device_ctx(
             self.ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
-            db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, db.band_width,
-            _SUB.ctypes.data, 0.0, None, PASS_SCORE, ENGINE_BATCHED,
+            db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all,
+            int(sc.c_sw_band_width) if sc.use_c_sw else db.band_width,
+            _SUB.ctypes.data, 0.0, self.d_diags.data_ptr() if sc.hints else None, PASS_SCORE, ENGINE_BATCHED,
             self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(), st))
         self._mark(3)
         self.h_n[:nq].copy_(self.d_n[:nq], non_blocking=True)
@@ -300,27 +354,30 @@ class _Slot:
         buckets = sorted({b for b in buckets if b <= db.arena_queries} | {db.arena_queries})
         self.stage_events = None
         self._fill_host([], pad_to=buckets[-1])  # every query slot an empty query
+        sc = Scoring(int(min_total_hits), 0)
         with torch.cuda.stream(self.stream):
-            self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, min_total_hits)
+            self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, sc)
         self.stream.synchronize()
         _lib.check(db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream))
         _lib.check(db.lib.ck_ctx_freeze(self.ctx, 1))
         for b in buckets:
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-                self._enqueue(b, db.arena_residues, db.arena_residues, min_total_hits)
+                self._enqueue(b, db.arena_residues, db.arena_residues, sc)
             self.graphs[b] = g
         self.graph_min_hits = int(min_total_hits)
         self.stream.synchronize()
 
-    def launch(self, queries: list[np.ndarray], min_total_hits: int, kmer_score_thresh: int = 0):
-        """Enqueue the whole pipeline for a batch on this slot's stream.  The
-        similar-k-mer scoring sizes its neighbour list on the host, so it runs
-        call by call; exact k-mer batches replay the captured graphs."""
+    def launch(self, queries: list[np.ndarray], min_total_hits: int, kmer_score_thresh: int = 0, **scoring):
+        """Enqueue the whole pipeline for a batch on this slot's stream
+        (``scoring``: the other fields of Scoring).  The similar-k-mer scoring
+        and Phase B size buffers on the host, so they run call by call; exact
+        Phase-A batches replay the captured graphs."""
         torch = _torch()
         db = self.db
+        sc = Scoring(int(min_total_hits), int(kmer_score_thresh), **scoring)
         bucket = None
-        if self.graphs and int(min_total_hits) == self.graph_min_hits and kmer_score_thresh <= 0:
+        if self.graphs and sc.graphable and sc.min_total_hits == self.graph_min_hits:
             bucket = next((b for b in sorted(self.graphs) if b >= len(queries)), None)
         if bucket is not None:
             nq, lens, tot = self._fill_host(queries, pad_to=bucket)
@@ -330,7 +387,7 @@ class _Slot:
         else:
             nq, lens, tot = self._fill_host(queries)
             with torch.cuda.stream(self.stream):
-                self._enqueue(nq, int(lens.max() if nq else 0), tot, min_total_hits, kmer_score_thresh)
+                self._enqueue(nq, int(lens.max() if nq else 0), tot, sc)
                 self.event.record(self.stream)
         self.batch = (nq, lens)
 
@@ -370,8 +427,10 @@ class _Slot:
 
 def search_batch(db: DeviceDatabase, queries: list[np.ndarray], top_k: int = 10,
                  max_cands: int = 500, min_total_hits: int = 2, slot: _Slot | None = None,
-                 kmer_score_thresh: int = 13):
-    """Synchronous search of a list of encoded queries; list of hit lists."""
+                 kmer_score_thresh: int = 13, **scoring):
+    """Synchronous search of a list of encoded queries; list of hit lists.
+    ``scoring``: min_diag_hits, diag_bin_width, phase_a_topk, use_c_scoring,
+    use_c_sw, c_sw_band_width (Scoring)."""
     own = slot is None
     if own:
         slot = _Slot(db, 0, max_cands)
@@ -379,7 +438,7 @@ def search_batch(db: DeviceDatabase, queries: list[np.ndarray], top_k: int = 10,
         res = []
         for s in range(0, len(queries), db.arena_queries):
             chunk = queries[s:s + db.arena_queries]
-            slot.launch(chunk, min_total_hits, kmer_score_thresh)
+            slot.launch(chunk, min_total_hits, kmer_score_thresh, **scoring)
             slot.event.synchronize()
             for qi, hits in enumerate(slot.results(top_k)):
                 for h in hits:
@@ -412,17 +471,21 @@ class SearchServer:
 
     def __init__(self, db: DeviceDatabase, top_k: int = 10, max_cands: int = 500,
                  min_total_hits: int = 2, max_batch: int | None = None, use_graphs: bool = True,
-                 kmer_score_thresh: int = 13):
+                 kmer_score_thresh: int = 13, **scoring):
         torch = _torch()
         self.db = db
         self.top_k = top_k
         self.max_cands = max_cands
         self.min_total_hits = min_total_hits
         self.kmer_score_thresh = int(kmer_score_thresh)
+        self.scoring = dict(scoring)
         self.max_batch = min(max_batch or db.arena_queries, db.arena_queries)
         free, _ = torch.cuda.mem_get_info(db.dev)
         # per slot: counts scratch + pair/SW buffers + the SW kernel's window scratch
         per_slot = (db.arena_queries * db.n * 4 + db.arena_queries * max_cands * 64 + (256 << 20))
+        sc = Scoring(int(min_total_hits), self.kmer_score_thresh, **scoring)
+        if sc.diagonal:  # Phase B: target -> selection row, selection and bin offsets
+            per_slot += db.arena_queries * (db.n * 4 + min(sc.phase_a_topk, db.n) * 16)
         n_slots = int(max(1, min(db.slots, (free // 2) // max(per_slot, 1))))
         self.slots = [_Slot(db, i, max_cands) for i in range(n_slots)]
         self.free = list(self.slots)
@@ -436,9 +499,9 @@ class SearchServer:
         # CUDA graphs (one replay per batch), or warm it with one batch
         warm = [np.arange(40, dtype=np.uint8) % 20]
         for s in self.slots:
-            if use_graphs and self.kmer_score_thresh <= 0:
+            if use_graphs and sc.graphable:
                 s.capture_graphs(min_total_hits)
-            s.launch(warm, min_total_hits, self.kmer_score_thresh)
+            s.launch(warm, min_total_hits, self.kmer_score_thresh, **self.scoring)
             s.event.synchronize()
             s.results(1)
 
@@ -511,7 +574,8 @@ class SearchServer:
             if batch:
                 slot = self.free.pop()
                 try:
-                    slot.launch([r.query for r in batch], self.min_total_hits, self.kmer_score_thresh)
+                    slot.launch([r.query for r in batch], self.min_total_hits, self.kmer_score_thresh,
+                                **self.scoring)
                     self.busy.append((slot, batch))
                 except Exception as e:
                     for r in batch:

@@ -282,6 +282,35 @@ int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, in
                                          int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
                                          int32_t *d_out_n, void *stream);
 
+/* The k-mer scorer of clustkit's C/OpenMP search path (batch_score_queries_c,
+ * clustkit/csrc/kmer_score.c:420-470, bound at clustkit/kmer_index.py:
+ * 1600-1656), on the device.  Phase A as ck_search_phase_a_device (hits from
+ * the query's valid k-mers with frequency <= freq_thresh, saturating at
+ * 32767, survivors with >= min_total_hits).  min_diag_hits <= 1: the survivors
+ * capped at max_cands (kmer_score.c:244-262), d_out_diags zeroed (the C scorer
+ * leaves them unset there).  Otherwise Phase B (kmer_score.c:264-415): the top
+ * phase_a_topk survivors by (hits desc, id asc) are rescored by their hits'
+ * diagonal bins (tpos - qpos + qlen) / diag_bin_width -- per target its
+ * longest bin, the first on ties -- those with a bin of >= min_diag_hits hits
+ * kept with that count as score and the hint bin * diag_bin_width - qlen +
+ * diag_bin_width / 2 in d_out_diags (may be NULL), capped at max_cands.
+ * Output rows [nq x max_cands]: targets id ascending when not capped, else the
+ * max_cands best by (score desc, id asc) in that order; d_out_n [nq].
+ * d_db_lengths int32 [num_db] (the target lengths size each target's bins; the
+ * C scorer sorts its hits instead) is needed only for Phase B.  The k-mer
+ * entries are the full (target << 32 | position) ones; the C scorer's
+ * optional compact Phase-A entries are a host memory layout and not taken.
+ * Blocking (it sizes the bins on the host). */
+int32_t ck_search_kmer_candidates_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
+                                         const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,
+                                         int32_t max_qlen, int32_t k, int32_t alpha,
+                                         const int64_t *d_kmer_offsets, const int64_t *d_kmer_entries,
+                                         const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+                                         const int32_t *d_db_lengths, int32_t min_total_hits,
+                                         int32_t min_diag_hits, int32_t diag_bin_width, int32_t max_cands,
+                                         int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores,
+                                         int32_t *d_out_diags, int32_t *d_out_n, void *stream);
+
 /* ---------------------------------------------------- graph + components
  * The step after Align.  ck_graph_csr_device: the symmetric similarity graph
  * of clustkit/graph.py:7-39 -- edges (i, j) and (j, i) of every pair with

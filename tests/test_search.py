@@ -173,12 +173,17 @@ def test_phase_a_cap_and_ties_vs_oracle(ck):
             slot.close()
 
 
+_C_PATH = {"min_diag_hits": 2, "use_c_scoring": True, "use_c_sw": True}
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("use_graphs,thresh", [(True, 0), (False, 0), (False, 13)])
-def test_server_results_same_alone_and_in_mix(ck, use_graphs, thresh):
+@pytest.mark.parametrize("use_graphs,thresh,scoring", [(True, 0, {}), (False, 0, {}), (False, 13, {}),
+                                                       (True, 0, _C_PATH)])
+def test_server_results_same_alone_and_in_mix(ck, use_graphs, thresh, scoring):
     """Each query's hits are identical whether it is searched alone or lands
     in concurrent batches of the continuous-batching server (slots replaying
-    captured CUDA graphs, or launching the pipeline call by call)."""
+    captured CUDA graphs, or launching the pipeline call by call; exact,
+    similar-k-mer and Phase-B + hinted-SW scoring)."""
     from clustkit_gb300.search import DeviceDatabase, SearchServer, search_batch
     db_set = synth.generate_families(400, 10, median=200, lo=40, hi=600, seed=92)
     db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_slots=3, arena_queries=16,
@@ -187,8 +192,9 @@ def test_server_results_same_alone_and_in_mix(ck, use_graphs, thresh):
     qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 40, replace=False)]
     bg = synth.random_sequences(20, median=200, lo=40, hi=600, seed=93)
     qs += [bg.seq(i).copy() for i in range(bg.n)]
-    alone = [search_batch(db, [q], top_k=10, kmer_score_thresh=thresh)[0] for q in qs]
-    server = SearchServer(db, top_k=10, max_batch=7, use_graphs=use_graphs, kmer_score_thresh=thresh).start()
+    alone = [search_batch(db, [q], top_k=10, kmer_score_thresh=thresh, **scoring)[0] for q in qs]
+    server = SearchServer(db, top_k=10, max_batch=7, use_graphs=use_graphs, kmer_score_thresh=thresh,
+                          **scoring).start()
     try:
         futs = [server.submit(q) for q in qs]
         mixed = [f.result(timeout=120) for f in futs]
