@@ -708,34 +708,40 @@ def run_search(args, n_db_fam=50000):
     # clustkit's default scoring (BLOSUM62 similar 5-mers, threshold 13): far
     # more k-mer work per query, so the rates follow its measured batch rate
     similar = _measure_search_mode(db, qs[3000:], 13, None, n_plain=30, n_stage=10, n_batch=2)
+    # clustkit's C path: exact 5-mers with Phase B (min_diag_hits 2, bin 10,
+    # Phase-A top 10,000), SW at band 50 centred on the diagonal hints
+    c_path = _measure_search_mode(db, qs[1500:], 0, None, n_plain=100, n_stage=20, n_batch=3,
+                                  scoring={"min_diag_hits": 2, "diag_bin_width": 10, "phase_a_topk": 10000,
+                                           "use_c_scoring": True, "use_c_sw": True, "c_sw_band_width": 50})
     return {"db_sequences": int(s.n), "db_residues": int(s.flat.size), "index_entries": db.n_entries,
             "band_width": db.band_width, "max_cands": 500, "top_k": 10, "slots": exact.pop("slots"),
             "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)", **exact,
-            "similar_kmers_thresh13": similar}
+            "similar_kmers_thresh13": similar, "c_path_phase_b_hinted_sw": c_path}
 
 
-def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch):
+def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scoring=None):
     from clustkit_gb300.search import SearchServer, _Slot, search_batch
+    scoring = scoring or {}
     slot = _Slot(db, 0, 500)
     for q in qs[:min(20, n_plain)]:
-        search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh)
+        search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
     lat = []
     tp0 = time.perf_counter()
     for q in qs[:n_plain]:
         a = time.perf_counter()
-        search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh)
+        search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
         lat.append(time.perf_counter() - a)
     plain_qps = n_plain / (time.perf_counter() - tp0)
     # device time per stage of a one-query batch (separate pass: events add syncs)
     slot.enable_stage_timing()
     stages, cells1 = [], []
     for q in qs[:n_stage]:
-        search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh)
+        search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
         stages.append(slot.stage_ms())
         cells1.append(slot.last_cells())
     full, cells64 = [], []
     for r in range(n_batch):
-        search_batch(db, qs[64 * r:64 * (r + 1)], top_k=10, slot=slot, kmer_score_thresh=thresh)
+        search_batch(db, qs[64 * r:64 * (r + 1)], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
         full.append(slot.stage_ms())
         cells64.append(slot.last_cells())
     sw1 = np.array([x[2] for x in stages])
@@ -755,7 +761,7 @@ def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch):
     if rates is None:
         batch_qps = 64.0 / (float(np.sum(full_med)) * 1e-3)
         rates = tuple(int(max(10, round(batch_qps * f, -1))) for f in (0.1, 0.3, 0.6, 0.9))
-    server = SearchServer(db, top_k=10, max_cands=500, kmer_score_thresh=thresh).start()
+    server = SearchServer(db, top_k=10, max_cands=500, kmer_score_thresh=thresh, **scoring).start()
     sweep = []
     rng = np.random.default_rng(3)
     qi = 0
@@ -779,7 +785,7 @@ def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch):
             p = server.latency_percentiles()
             sweep.append({"offered_qps": rate, "achieved_qps": n / (t_end - t_start), "queries": n,
                           "p50_ms": p["p50_ms"], "p99_ms": p["p99_ms"]})
-            log(f"search (kmer_score_thresh {thresh}) rate {rate}/s: {sweep[-1]}")
+            log(f"search (kmer_score_thresh {thresh}{', C path' if scoring else ''}) rate {rate}/s: {sweep[-1]}")
     finally:
         server.stop()
     return {"plain_loop": plain, "continuous_batching": sweep, "slots": len(server.slots)}

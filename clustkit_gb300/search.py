@@ -1,7 +1,7 @@
 """Query-vs-database search on the GPU, batch and continuous-batching serving.
 
-Mirrors the k-mer search of clustkit (clustkit/kmer_index.py:1475-2349) in
-its two k-mer scoring modes with ``min_diag_hits <= 1``: k-mer inverted index
+Mirrors the k-mer search of clustkit (clustkit/kmer_index.py:1475-2349).
+With ``min_diag_hits <= 1``: k-mer inverted index
 (k = 5, clustkit's CSR layout, kmer_index.py:117-166); either BLOSUM62
 similar-k-mer scoring (``kmer_score_thresh > 0``, clustkit's default 13:
 every 5-mer scoring >= the threshold against a query 5-mer adds its score,
@@ -227,6 +227,7 @@ class _Slot:
         self.stage_events = None
         self.graphs: dict = {}  # batch-size bucket -> captured pipeline
         self.graph_min_hits = None
+        self.last_band = db.band_width  # band of the last enqueued batch
 
     def close(self):
         self.graphs.clear()
@@ -250,7 +251,7 @@ class _Slot:
         ql = lens[qi].astype(np.int64)
         tl = self.db.lengths_host[tg[qi, ci]].astype(np.int64)
         la, lb = np.minimum(ql, tl), np.maximum(ql, tl)
-        return int(band_cells(la, lb, effective_band(la, lb, self.db.band_width)).sum())
+        return int(band_cells(la, lb, effective_band(la, lb, self.last_band)).sum())
 
     def stage_ms(self):
         """(h2d, phase_a, sw, d2h) milliseconds of the last batch (after its event)."""
@@ -323,6 +324,7 @@ class _Slot:
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
         self._mark(2)
+        self.last_band = int(sc.c_sw_band_width) if sc.use_c_sw else db.band_width
         # dense pair list: (query, target) or (empty, empty) past a query's candidates
         q = self.d_slotq[:M]
         valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
@@ -330,8 +332,7 @@ class _Slot:
         self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M], torch.full_like(q, db.empty_idx))
         _lib.check(lib.ck_sw_batch_device_ctx(
             self.ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
-            db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all,
-            int(sc.c_sw_band_width) if sc.use_c_sw else db.band_width,
+            db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, self.last_band,
             _SUB.ctypes.data, 0.0, self.d_diags.data_ptr() if sc.hints else None, PASS_SCORE, ENGINE_BATCHED,
             self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(), st))
         self._mark(3)
