@@ -219,12 +219,12 @@ def cpu_baseline(s, pairs, target_s: float = 12.0, use_ref: bool = True):
     rng = np.random.default_rng(0)
     sample = pairs[rng.permutation(len(pairs))]
 
-    def run(p):
+    def run(p, nt=threads):
         t = time.perf_counter()
         if kind == "reference":
-            oracle.ref_sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=threads)
+            oracle.ref_sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=nt)
         else:
-            oracle.set_num_threads(threads)
+            oracle.set_num_threads(nt)
             oracle.sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
         return time.perf_counter() - t
 
@@ -234,9 +234,17 @@ def cpu_baseline(s, pairs, target_s: float = 12.0, use_ref: bool = True):
     p = sample[:n]
     dt = run(p)
     cells = int(pair_cells(p, s.lengths, BAND_WIDTH).sum())
+    # one thread, on a ~3 s slice of the same sample
+    n1 = max(50, int(n * 3.0 / max(dt * threads, 1e-3)))
+    p1 = sample[:n1]
+    dt1 = run(p1, 1)
+    cells1 = int(pair_cells(p1, s.lengths, BAND_WIDTH).sum())
+    oracle.set_num_threads(threads)
     return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
             "pairs_per_s": n / dt,
-            "sample": f"{n} random pairs of the workload ({cells} cells), {threads} threads, {dt:.1f}s"}
+            "sample": f"{n} random pairs of the workload ({cells} cells), {threads} threads, {dt:.1f}s",
+            "single_thread": {"value": cells1 / dt1 / 1e9, "unit": "GCUPS", "pairs_per_s": n1 / dt1,
+                              "sample": f"{n1} pairs ({cells1} cells), 1 thread, {dt1:.1f}s"}}
 
 
 # ----------------------------------------------------------------------------- arms
@@ -713,10 +721,61 @@ def run_search(args, n_db_fam=50000):
     c_path = _measure_search_mode(db, qs[1500:], 0, None, n_plain=100, n_stage=20, n_batch=3,
                                   scoring={"min_diag_hits": 2, "diag_bin_width": 10, "phase_a_topk": 10000,
                                            "use_c_scoring": True, "use_c_sw": True, "c_sw_band_width": 50})
+    if not args.no_cpu:
+        c_path["cpu_baseline"] = search_cpu_baseline(db, s, qs[1500:])
+        log(f"search C path on the host cores: {c_path['cpu_baseline']}")
     return {"db_sequences": int(s.n), "db_residues": int(s.flat.size), "index_entries": db.n_entries,
             "band_width": db.band_width, "max_cands": 500, "top_k": 10, "slots": exact.pop("slots"),
             "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)", **exact,
             "similar_kmers_thresh13": similar, "c_path_phase_b_hinted_sw": c_path}
+
+
+def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
+    """clustkit's C search path on the host cores, as C restatements (the port):
+    the C k-mer scorer (kmer_score.c, Phase A + Phase B + hints, OpenMP over
+    queries), the C SW at band 50 centred on the hints (sw_align.c, OpenMP over
+    pairs) and the rank, on a sample of the same queries; queries/s of the
+    whole chain with the index resident in host memory."""
+    import oracle
+    from oracle import search_oracle as so
+    from clustkit_gb300.blosum import BLOSUM62
+    threads = os.cpu_count() or 1
+    oracle.set_num_threads(threads)
+    off, ent, fr = db.index_arrays()
+    mc, topk = 500, 10000
+
+    def run(sample):
+        lens = np.array([len(q) for q in sample], np.int32)
+        q_off = np.zeros(len(sample), np.int64)
+        q_off[1:] = np.cumsum(lens[:-1])
+        q_flat = np.concatenate(sample).astype(np.uint8)
+        flat = np.concatenate([s.flat, q_flat])
+        offs = np.concatenate([s.offsets, q_off + len(s.flat)])
+        all_lens = np.concatenate([s.lengths, lens])
+        t0 = time.perf_counter()
+        cands = oracle.kmer_candidates_batch(q_flat, q_off, lens, 5, 20, off, ent, fr, db.freq_thresh, s.n,
+                                             2, 2, 10, mc, topk)
+        t1 = time.perf_counter()
+        qi = np.concatenate([np.full(len(c[0]), i, np.int32) for i, c in enumerate(cands)])
+        tg = np.concatenate([c[0] for c in cands]).astype(np.int32)
+        hints = np.concatenate([c[2] for c in cands]).astype(np.int32)
+        pairs = np.stack([qi + s.n, tg], axis=1)
+        r = oracle.sw_batch(pairs, flat, offs, all_lens, 50, BLOSUM62, diag_hints=hints)
+        t2 = time.perf_counter()
+        keep = r["scores"] > 0
+        so.rank_hits(np.stack([qi, tg], axis=1)[keep], r["sims"][keep], r["scores"][keep], lens, s.lengths,
+                     len(sample), 10)
+        t3 = time.perf_counter()
+        return t3 - t0, t1 - t0, t2 - t1, t3 - t2, len(pairs)
+
+    n = 32
+    dt = run(qs[:n])[0]
+    n = int(min(len(qs), max(n, n * target_s / max(dt, 1e-3))))
+    tot, ts, tsw, trank, npairs = run(qs[:n])
+    return {"value": n / tot, "unit": "queries/s", "cores": threads, "kind": "port",
+            "stage_s": {"kmer_scorer": ts, "sw": tsw, "rank": trank},
+            "sample": f"{n} queries of the stream, {npairs} candidate pairs, {threads} threads, {tot:.1f}s",
+            "source": "restatements of clustkit/csrc/kmer_score.c:195-470 and sw_align.c:25-266"}
 
 
 def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scoring=None):

@@ -10,7 +10,10 @@ function (reference paths relative to the clustkit project root):
 * ``sw_batch``  -- clustkit/csrc/sw_align.c:25-266 (banded Smith-Waterman,
   BLOSUM62, gaps -11/-1, match-count provenance, first-max tie rule);
 * ``sketches``  -- clustkit/sketch.py:17-109 (fmix64 bottom-s MinHash);
-* ``jaccard``   -- clustkit/pairwise.py:1564-1612 (merge-walk Jaccard).
+* ``jaccard``   -- clustkit/pairwise.py:1564-1612 (merge-walk Jaccard);
+* ``kmer_candidates_batch`` -- clustkit/csrc/kmer_score.c:195-470 (the C
+  k-mer scorer: Phase A, top-K, Phase B diagonal runs and hints), from
+  ``oracle/kmer_oracle.c``.
 
 ``ref_sw_batch`` calls the reference's own sw_align.c, compiled from source
 into ``oracle/_ref/`` by ``oracle/build.py`` (only where the reference
@@ -45,6 +48,10 @@ def _load():
                                   ctypes.c_int32, ctypes.c_uint64, _P]
         lib.or_jaccard.restype = None
         lib.or_jaccard.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, _P]
+        lib.or_kmer_candidates.restype = None
+        lib.or_kmer_candidates.argtypes = [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
+                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P, _P]
         lib.or_set_num_threads.restype = None
         lib.or_set_num_threads.argtypes = [ctypes.c_int32]
         lib.or_max_threads.restype = ctypes.c_int32
@@ -89,6 +96,28 @@ def sw_batch(pairs, flat, offsets, lengths, band_width, sub_matrix, diag_hints=N
                     out["sims"].ctypes.data, out["scores"].ctypes.data, out["matches"].ctypes.data,
                     out["shorter"].ctypes.data, out["mask"].ctypes.data)
     return out
+
+
+def kmer_candidates_batch(q_flat, q_offsets, q_lengths, k, alpha, kmer_offsets, kmer_entries, kmer_freqs,
+                          freq_thresh, num_db, min_total_hits, min_diag_hits, diag_bin_width, max_cands,
+                          phase_a_topk):
+    """Per query (ids, scores, diags) of the C k-mer scorer's restatement,
+    all queries in one OpenMP call."""
+    lib = _load()
+    q_flat = _c(q_flat if len(q_flat) else np.zeros(1, np.uint8), np.uint8)
+    q_offsets, q_lengths = _c(q_offsets, np.int64), _c(q_lengths, np.int32)
+    off, ent, fr = _c(kmer_offsets, np.int64), _c(kmer_entries, np.int64), _c(kmer_freqs, np.int32)
+    nq = len(q_lengths)
+    mc = int(max_cands)
+    t = np.zeros((max(nq, 1), mc), np.int32)
+    s = np.zeros_like(t)
+    d = np.zeros_like(t)
+    n = np.zeros(max(nq, 1), np.int32)
+    lib.or_kmer_candidates(q_flat.ctypes.data, q_offsets.ctypes.data, q_lengths.ctypes.data, nq, int(k), int(alpha),
+                           off.ctypes.data, ent.ctypes.data, fr.ctypes.data, int(freq_thresh), int(num_db),
+                           int(min_total_hits), int(min_diag_hits), int(diag_bin_width), mc, int(phase_a_topk),
+                           t.ctypes.data, s.ctypes.data, d.ctypes.data, n.ctypes.data)
+    return [(t[i, :n[i]].copy(), s[i, :n[i]].copy(), d[i, :n[i]].copy()) for i in range(nq)]
 
 
 def sketches(flat, offsets, lengths, k, s, alphabet=20, seed=42):

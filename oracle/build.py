@@ -5,8 +5,9 @@ TEST INFRASTRUCTURE ONLY: the libraries built here are checkers for the CUDA
 path (tests/, __graft_entry__.smoke(), bench.py's cpu_baseline and reference
 legs).  Nothing in the product library links or loads them.
 
-* ``oracle/_build/liboracle.so`` -- ``oracle/oracle.c`` (this project's own
-  restatement), ``gcc -O3 -fopenmp``.
+* ``oracle/_build/liboracle.so`` -- ``oracle/oracle.c`` and
+  ``oracle/kmer_oracle.c`` (this project's own restatements), ``gcc -O3
+  -fopenmp``.
 * ``oracle/_ref/sw_align_ref.so`` -- ``clustkit/csrc/sw_align.c`` compiled
   straight from the reference checkout (read in place, never copied), with the
   reference's own build line (clustkit/csrc/sw_align.c:10) minus
@@ -43,10 +44,10 @@ def _needs(out: Path, src: Path) -> bool:
 
 def build_oracle(verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    src = HERE / "oracle.c"
+    srcs = [HERE / "oracle.c", HERE / "kmer_oracle.c"]
     out = BUILD / "liboracle.so"
-    if _needs(out, src):
-        cmd = ["gcc", *CFLAGS, "-o", str(out), str(src)]
+    if any(_needs(out, src) for src in srcs):
+        cmd = ["gcc", *CFLAGS, "-o", str(out), *map(str, srcs)]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         subprocess.run(cmd, check=True)

@@ -337,3 +337,35 @@ def test_oracle_kmer_candidates_match_reference_c_scorer(golden):
     for qi in range(len(qs)):
         assert np.array_equal(g[f"numba_q{qi}_ids"], g[f"c2_q{qi}_targets"])
         assert np.array_equal(g[f"numba_q{qi}_scores"], g[f"c2_q{qi}_scores"])
+
+
+def test_c_oracle_kmer_candidates_match_reference_and_numpy(golden):
+    """The C restatement of the k-mer scorer (the search path's CPU baseline)
+    against the reference scorer's golden vectors and the numpy restatement."""
+    g = golden("kmer_scorer_golden.npz")
+    off, ent, fr = so.build_kmer_index(g["db_flat"], g["db_offsets"], g["db_lengths"], 5)
+    nd = len(g["db_lengths"])
+    for ci, (mth, mdh, dbw, mc, topk) in enumerate(g["configs"]):
+        got = oracle.kmer_candidates_batch(g["q_flat"], g["q_offsets"], g["q_lengths"], 5, 20, off, ent, fr,
+                                           int(g["freq_thresh"]), nd, int(mth), int(mdh), int(dbw), int(mc),
+                                           int(topk))
+        for qi, (ids, sc, dg) in enumerate(got):
+            assert np.array_equal(ids, g[f"c{ci}_q{qi}_targets"]), (ci, qi)
+            assert np.array_equal(sc, g[f"c{ci}_q{qi}_scores"]), (ci, qi)
+            if mdh >= 2:
+                assert np.array_equal(dg, g[f"c{ci}_q{qi}_diags"]), (ci, qi)
+    db_set = synth.generate_families(300, 8, median=200, lo=40, hi=700, seed=33)
+    off, ent, fr = so.build_kmer_index(db_set.flat, db_set.offsets, db_set.lengths, 5)
+    thr = so.compute_freq_threshold(fr, db_set.n, 95.0)
+    rng = np.random.default_rng(2)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 10, replace=False)]
+    qs += [np.zeros(0, np.uint8), np.array([1, 2], np.uint8), np.full(50, 20, np.uint8)]
+    lens = np.array([len(q) for q in qs], np.int32)
+    offs = np.concatenate([[0], np.cumsum(lens[:-1])]).astype(np.int64)
+    flat = np.concatenate(qs).astype(np.uint8)
+    for cfg in [(2, 2, 10, 2000, 10000), (1, 3, 1, 9, 40), (2, 1, 10, 5, 100), (0, 2, 30, 50, 200)]:
+        got = oracle.kmer_candidates_batch(flat, offs, lens, 5, 20, off, ent, fr, thr, db_set.n, *cfg)
+        for qi, q in enumerate(qs):
+            want = so.kmer_candidates(q, 5, 20, off, ent, fr, thr, db_set.n, *cfg)
+            for a, b in zip(got[qi], want):
+                assert np.array_equal(a, b), (cfg, qi)
