@@ -261,7 +261,17 @@ template <int V> struct StripVariant {
     static constexpr int UNROLL = (V & 2) ? 4 : 2;
 };
 
-// Cells of rows [RB, RE) at column j, top to bottom.  (hu, eu) enter as
+// Rows of a strip inside their band at a column, as a bit mask: row r
+// (0 <= r < alive) of the strip whose first row's band starts at column lo0
+// covers column j when 0 <= j - r - lo0 <= w2, i.e. r in
+// [d - w2, d] with d = j - lo0.
+__device__ __forceinline__ uint32_t band_rows(int32_t d, uint32_t w2, int32_t alive) {
+    const int32_t lo = d - (int32_t)w2 > 0 ? d - (int32_t)w2 : 0;
+    const int32_t hi = d < alive - 1 ? d : alive - 1;
+    return hi < lo ? 0u : (2u << hi) - (1u << lo);  // here 0 <= lo <= hi < alive <= 24
+}
+
+// Cells of rows [RB, RE) at one column, top to bottom.  (hu, eu) enter as
 // H and E of row RB - 1 at column j, hdiag as H of row RB - 1 at column
 // j - 1; they leave as the values of row RE - 1.  Stored keys: H clean
 // (score * 2^16 + matches), E and F with the tie bit set.
@@ -270,17 +280,17 @@ template <int V> struct StripVariant {
 //     F    = max(F_left - 2^16, H_left + OPEN_F) | tie
 //     H    = max(diag, E, F) & CLEAN
 template <int R, int RB, int RE, bool MASKED>
-__device__ __forceinline__ void strip_cells(int32_t j, uint32_t bcol, int32_t &hu, int32_t &eu,
-                                            int32_t hdiag, StripRegs<R> &S, const char *s_inc,
-                                            int32_t lo0, uint32_t w2, int32_t alive, int32_t one) {
+__device__ __forceinline__ void strip_cells(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t hdiag,
+                                            StripRegs<R> &S, const char *s_inc, uint32_t rmask, int32_t one) {
     using namespace key;
 #pragma unroll
     for (int r = RB; r < RE; ++r) {
-        // Ramp and clipped columns skip rows outside their band: a row that
-        // has not reached its band keeps H = 0, F = -inf; a row that has left
-        // it hands the out-of-band boundary (H = 0, E = -inf) to the row
-        // below and its last H as that row's diagonal input.
-        if (!MASKED || ((r < alive) && ((uint32_t)(j - r - lo0) <= w2))) {
+        // Ramp and clipped columns skip rows outside their band (bit r of
+        // rmask clear): a row that has not reached its band keeps H = 0,
+        // F = -inf; a row that has left it hands the out-of-band boundary
+        // (H = 0, E = -inf) to the row below and its last H as that row's
+        // diagonal input.
+        if (!MASKED || ((rmask >> r) & 1u)) {
             const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
             const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
             // E's extension term comes from E of the row above, known before
@@ -349,7 +359,8 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R>
     int32_t hu = bnd.x, eu = bnd.y;
     const int32_t hdiag = S.hd0;
     S.hd0 = hu;
-    strip_cells<R, 0, R, MASKED>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive, one);
+    strip_cells<R, 0, R, MASKED>(bcol, hu, eu, hdiag, S, s_inc, MASKED ? band_rows(j - lo0, w2, alive) : ~0u,
+                                 one);
     *slot = make_int2(hu, eu);
     strip_track<R>(S, gthr, s_best);
 }
@@ -619,7 +630,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             if (j >= J0 && j <= J1) {
                 const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
                 int32_t hu = hin, eu = ein;
-                strip_cells<R, 0, R, true>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, w2, alive, one);
+                strip_cells<R, 0, R, true>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2, alive), one);
                 hout = hu;
                 eout = eu;
                 cm = S.hc[0];
@@ -743,6 +754,8 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
     __syncwarp();
     // per-lane strip state
     int32_t cur_slot = -1, cur_s = 0, i0 = 0, lo0 = 0, J0 = 1, J1 = 0, alive = 0, te = 0, top = 0;
+    int32_t jb = 0;    // j = T + jb for the strip held
+    uint32_t w2s = 0;  // 2w of its pair
     int32_t pend_slot = -1, pend_s = 0, pend_t0 = 0;
     int32_t F = -1;
     int32_t hout = 0, eout = NEG_E, hprev = 0;
@@ -815,6 +828,8 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             te = strip_te<R>(sl, cur_s);
             if (te < T) te = T;  // only after a late start: the strip still ends
             top = cur_s * R + sl.h + sl.w;
+            jb = sl.J00 - sl.T0 - cur_s;
+            w2s = 2u * (uint32_t)sl.w;
             B = in.flat + sl.b_off;
             const uint8_t *A = in.flat + sl.a_off;
 #pragma unroll
@@ -833,16 +848,14 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
         const bool has = cur_slot >= 0;
         int32_t j = 0;
         if (has) {
-            const WaveSlot &sl = slots[cur_slot];
-            j = T - sl.T0 - cur_s + sl.J00;
+            j = T + jb;
             const int32_t hdiag = (cur_s == 0 || j - 1 > top || j - 1 < 1) ? 0 : hprev;
             hprev = hin;
             if (cur_s == 0 || j > top) { hin = 0; ein = NEG_E; }
             if (j >= J0 && j <= J1) {
                 const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
                 int32_t hu = hin, eu = ein;
-                strip_cells<R, 0, R, true>(j, bcol, hu, eu, hdiag, S, s_inc, lo0, 2u * (uint32_t)sl.w, alive,
-                                           one);
+                strip_cells<R, 0, R, true>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2s, alive), one);
                 hout = hu;
                 eout = eu;
                 cm = S.hc[0];
@@ -938,6 +951,9 @@ static int32_t g_wave_adaptive = 1;
 // stream the strips of consecutive pairs through a warp: 1 when the call has
 // more warp-per-pair pairs than warps, 2 always, 0 never
 static int32_t g_wave_stream = 1;
+// rows per strip of the streamed schedule: 0 = the smallest that rotates,
+// else 4, 8 or 16 when at least that (taller strips rotate a fortiori)
+static int32_t g_wave_rows = 0;
 
 // Rows per strip shared by every warp-per-pair pair of a call: the smallest
 // that lets a strip of any of them rotate through 32 lanes (half-widths up to
@@ -946,9 +962,8 @@ static int32_t g_wave_stream = 1;
 // per warp at a time.
 static int32_t wave_rows_for(int32_t wmax) {
     if (!g_wave_stream) return 0;
-    if (2 * wmax < 31 * 4 + 32) return 4;
-    if (2 * wmax < 31 * 8 + 32) return 8;
-    return 16;
+    const int32_t r = 2 * wmax < 31 * 4 + 32 ? 4 : 2 * wmax < 31 * 8 + 32 ? 8 : 16;
+    return g_wave_rows > r ? g_wave_rows : r;
 }
 
 int32_t sw_set_wave(int32_t key, int32_t v) {
@@ -956,14 +971,20 @@ int32_t sw_set_wave(int32_t key, int32_t v) {
         set_error(CK_ERR_INVALID_ARGUMENT, "warp-per-pair settings must be >= 0");
         return CK_ERR_INVALID_ARGUMENT;
     }
+    if (key == 4 && v != 0 && v != 4 && v != 8 && v != 16) {
+        set_error(CK_ERR_UNSUPPORTED, "streamed strip rows must be 0 (smallest rotating), 4, 8 or 16");
+        return CK_ERR_UNSUPPORTED;
+    }
     if (key == 0) g_wave_min_rows = v;
     else if (key == 1) g_wave_all_below = v;
     else if (key == 2) g_wave_adaptive = v ? 1 : 0;
-    else g_wave_stream = v > 2 ? 2 : v;
+    else if (key == 3) g_wave_stream = v > 2 ? 2 : v;
+    else g_wave_rows = v;
     return CK_OK;
 }
 int32_t sw_wave(int32_t key) {
-    return key == 0 ? g_wave_min_rows : key == 1 ? g_wave_all_below : key == 2 ? g_wave_adaptive : g_wave_stream;
+    return key == 0 ? g_wave_min_rows : key == 1 ? g_wave_all_below : key == 2 ? g_wave_adaptive
+         : key == 3 ? g_wave_stream : g_wave_rows;
 }
 
 int32_t sw_set_variant(int32_t v) {

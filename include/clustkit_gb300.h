@@ -176,13 +176,18 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_WAVE_STREAM     1 (default): when a call has more warp-per-pair
  *                          pairs than the kernel has warps, a warp streams the
  *                          row strips of consecutive pairs through its lanes;
- *                          2: always; 0: never (one pair per warp at a time) */
+ *                          2: always; 0: never (one pair per warp at a time)
+ *   CK_CFG_WAVE_ROWS       rows per strip of that streamed schedule: 0
+ *                          (default) the smallest of 4/8/16 whose strips can
+ *                          rotate through the lanes at the call's band width;
+ *                          4, 8 or 16: at least that many */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
 #define CK_CFG_WAVE_ALL_BELOW 3
 #define CK_CFG_WAVE_ADAPTIVE 4
 #define CK_CFG_WAVE_STREAM 5
+#define CK_CFG_WAVE_ROWS 6
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

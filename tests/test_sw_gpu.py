@@ -98,13 +98,13 @@ def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
 
 
 @contextlib.contextmanager
-def wave_config(all_below, min_rows, adaptive=0, stream=1):
+def wave_config(all_below, min_rows, adaptive=0, stream=1, rows=0):
     """Route pairs between the warp-per-pair and the lane-per-pair kernels."""
-    from clustkit_gb300._lib import (CFG_WAVE_ADAPTIVE, CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_STREAM,
-                                     get_config, set_config)
-    keys = (CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_ADAPTIVE, CFG_WAVE_STREAM)
+    from clustkit_gb300._lib import (CFG_WAVE_ADAPTIVE, CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_ROWS,
+                                     CFG_WAVE_STREAM, get_config, set_config)
+    keys = (CFG_WAVE_ALL_BELOW, CFG_WAVE_MIN_ROWS, CFG_WAVE_ADAPTIVE, CFG_WAVE_STREAM, CFG_WAVE_ROWS)
     keep = [get_config(k) for k in keys]
-    for k, v in zip(keys, (all_below, min_rows, adaptive, stream)):
+    for k, v in zip(keys, (all_below, min_rows, adaptive, stream, rows)):
         set_config(k, v)
     try:
         yield
@@ -352,6 +352,32 @@ def test_streamed_wave_many_small_pairs(ck, bw):
         c = ck.sw_counters()
     assert c["wave"] == c["batched"]
     _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
+
+
+@pytest.mark.parametrize("rows", [8, 16])
+@pytest.mark.parametrize("bw", [0, 1, 3, 16, 50, 100])
+def test_streamed_wave_taller_strips(ck, golden, bw, rows):
+    """The streamed schedule with strips taller than the smallest rotating
+    height (CK_CFG_WAVE_ROWS), every pair one warp per pair: golden vectors
+    and mixed pairs with hints against the oracle."""
+    with wave_config(1 << 30, 0, stream=2, rows=rows):
+        g = golden("sw_golden.npz")
+        if f"bw{bw}_scores" in g.files:
+            r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
+            assert np.array_equal(r["scores"], g[f"bw{bw}_scores"])
+            assert np.array_equal(r["sims"], g[f"bw{bw}_sims"])
+        # full-band pairs (bw 0) rotate only up to 512 rows
+        s = synth.generate_families(60, 8, median=300, lo=5, hi=500 if bw == 0 else 1500, seed=bw + 40)
+        pairs = synth.mixed_pairs(s, 6000, seed=bw + 1)
+        rng = np.random.default_rng(bw + 5)
+        L = s.lengths
+        sh = np.minimum(L[pairs[:, 0]], L[pairs[:, 1]])
+        hints = (rng.integers(-1000, 1000, len(pairs)) % (2 * sh + 7) - sh - 3).astype(np.int32)
+        hints[rng.random(len(pairs)) < 0.5] = 0
+        r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, diag_hints=hints)
+        c = ck.sw_counters()
+    assert c["wave"] == c["batched"]
+    _same(r, oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, diag_hints=hints))
 
 
 @pytest.mark.parametrize("bw", [50, 100, 128])

@@ -306,7 +306,7 @@ def stream(pairs_geo, R):
             break
     return res, T
 
-def run_stream(seed, n, bw, maxlen=400, hint_frac=0.3):
+def run_stream(seed, n, bw, maxlen=400, hint_frac=0.3, rows=None):
     rng = np.random.default_rng(seed)
     seqs, pg, pairs = [], [], []
     for k in range(n):
@@ -320,7 +320,7 @@ def run_stream(seed, n, bw, maxlen=400, hint_frac=0.3):
         swap, la, lb, w, h = geometry(li, lj, bw, hint)
         A, B = (a, b) if not swap else (b, a)
         pg.append((A, B, la, lb, w, h)); seqs.append((a, b, hint))
-    R = r_call(bw)
+    R = max(r_call(bw), rows or 0)
     got, T = stream(pg, R)
     bad = 0
     for k, (a, b, hint) in enumerate(seqs):
@@ -340,3 +340,12 @@ def run_stream(seed, n, bw, maxlen=400, hint_frac=0.3):
                                               (7, 4, 238, 900), (8, 40, 238, 120)])
 def test_streamed_schedule_matches_oracle(seed, n, bw, maxlen):
     assert run_stream(seed, n, bw, maxlen) == 0
+
+
+@pytest.mark.parametrize("seed,n,bw,maxlen,rows", [(11, 12, 50, 400, 16), (12, 10, 16, 700, 16),
+                                                   (13, 10, 100, 300, 16), (14, 16, 50, 300, 8),
+                                                   (15, 6, 1, 300, 16), (16, 30, 0, 45, 16)])
+def test_streamed_schedule_with_taller_strips(seed, n, bw, maxlen, rows):
+    """Strips taller than the smallest rotating height (a call-wide setting):
+    the rotation bound holds a fortiori, results are unchanged."""
+    assert run_stream(seed, n, bw, maxlen, rows=rows) == 0
