@@ -24,6 +24,7 @@ host cores, on a bounded sample of the same pairs.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -705,29 +706,36 @@ def run_search(args, n_db_fam=50000):
     t0 = time.time()
     s = synth.generate_families(n_db_fam, 10, median=350, lo=30, hi=2000, seed=7)
     t1 = time.time()
-    db = DeviceDatabase(s.flat, s.offsets, s.lengths, arena_slots=4, arena_queries=64,
-                        arena_residues=64 * 2000)
+    B = int(args.search_batch)
+    db = DeviceDatabase(s.flat, s.offsets, s.lengths, arena_slots=4, arena_queries=B,
+                        arena_residues=B * 2000)
     t2 = time.time()
     log(f"search db: {s.n} seqs gen {t1 - t0:.1f}s, index+sketch {t2 - t1:.1f}s, "
         f"{db.n_entries} index entries, band {db.band_width}, freq cap {db.freq_thresh}")
     qs = make_queries(s, 6000)
-    exact = _measure_search_mode(db, qs, 0, (100, 1000, 3000, 10000, 20000), n_plain=300, n_stage=50,
-                                 n_batch=5)
-    # clustkit's default scoring (BLOSUM62 similar 5-mers, threshold 13): far
-    # more k-mer work per query, so the rates follow its measured batch rate
-    similar = _measure_search_mode(db, qs[3000:], 13, None, n_plain=30, n_stage=10, n_batch=2)
-    # clustkit's C path: exact 5-mers with Phase B (min_diag_hits 2, bin 10,
-    # Phase-A top 10,000), SW at band 50 centred on the diagonal hints
-    c_path = _measure_search_mode(db, qs[1500:], 0, None, n_plain=100, n_stage=20, n_batch=3,
-                                  scoring={"min_diag_hits": 2, "diag_bin_width": 10, "phase_a_topk": 10000,
-                                           "use_c_scoring": True, "use_c_sw": True, "c_sw_band_width": 50})
-    if not args.no_cpu:
-        c_path["cpu_baseline"] = search_cpu_baseline(db, s, qs[1500:])
-        log(f"search C path on the host cores: {c_path['cpu_baseline']}")
-    return {"db_sequences": int(s.n), "db_residues": int(s.flat.size), "index_entries": db.n_entries,
-            "band_width": db.band_width, "max_cands": 500, "top_k": 10, "slots": exact.pop("slots"),
-            "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)", **exact,
-            "similar_kmers_thresh13": similar, "c_path_phase_b_hinted_sw": c_path}
+    modes = set(args.search_modes.split(","))
+    out = {"db_sequences": int(s.n), "db_residues": int(s.flat.size), "index_entries": db.n_entries,
+           "band_width": db.band_width, "max_cands": 500, "top_k": 10}
+    if "exact" in modes:
+        exact = _measure_search_mode(db, qs, 0, (100, 1000, 3000, 10000, 20000), n_plain=300, n_stage=50,
+                                     n_batch=5)
+        out.update({"slots": exact.pop("slots"), "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)", **exact})
+    if "similar" in modes:
+        # clustkit's default scoring (BLOSUM62 similar 5-mers, threshold 13):
+        # far more k-mer work per query, so the rates follow its batch rate
+        out["similar_kmers_thresh13"] = _measure_search_mode(db, qs[3000:], 13, None, n_plain=30, n_stage=10,
+                                                             n_batch=2)
+    if "c_path" in modes:
+        # clustkit's C path: exact 5-mers with Phase B (min_diag_hits 2, bin
+        # 10, Phase-A top 10,000), SW at band 50 centred on the diagonal hints
+        c_path = _measure_search_mode(db, qs[1500:], 0, None, n_plain=100, n_stage=20, n_batch=3,
+                                      scoring={"min_diag_hits": 2, "diag_bin_width": 10, "phase_a_topk": 10000,
+                                               "use_c_scoring": True, "use_c_sw": True, "c_sw_band_width": 50})
+        if not args.no_cpu:
+            c_path["cpu_baseline"] = search_cpu_baseline(db, s, qs[1500:])
+            log(f"search C path on the host cores: {c_path['cpu_baseline']}")
+        out["c_path_phase_b_hinted_sw"] = c_path
+    return out
 
 
 def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
@@ -781,6 +789,7 @@ def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
 def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scoring=None):
     from clustkit_gb300.search import SearchServer, _Slot, search_batch
     scoring = scoring or {}
+    B = db.arena_queries
     slot = _Slot(db, 0, 500)
     for q in qs[:min(20, n_plain)]:
         search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
@@ -798,13 +807,13 @@ def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scori
         search_batch(db, [q], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
         stages.append(slot.stage_ms())
         cells1.append(slot.last_cells())
-    full, cells64 = [], []
+    full, cells_b = [], []
     for r in range(n_batch):
-        search_batch(db, qs[64 * r:64 * (r + 1)], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
+        search_batch(db, qs[B * r:B * (r + 1)], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
         full.append(slot.stage_ms())
-        cells64.append(slot.last_cells())
+        cells_b.append(slot.last_cells())
     sw1 = np.array([x[2] for x in stages])
-    sw64 = np.array([x[2] for x in full])
+    sw_b = np.array([x[2] for x in full])
     slot.close()
     full_med = np.median(np.array(full), axis=0)
     st_med = np.median(np.array(stages), axis=0)
@@ -812,15 +821,21 @@ def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scori
              "p99_ms": float(np.percentile(lat, 99) * 1e3), "queries": n_plain,
              "device_stage_ms_median": {"h2d": float(st_med[0]), "phase_a": float(st_med[1]),
                                         "sw": float(st_med[2]), "d2h": float(st_med[3])},
-             "device_stage_ms_median_batch64": {"h2d": float(full_med[0]), "phase_a": float(full_med[1]),
+             "batch_queries": B,
+             "device_stage_ms_median_batch": {"h2d": float(full_med[0]), "phase_a": float(full_med[1]),
                                                 "sw": float(full_med[2]), "d2h": float(full_med[3])},
              "sw_gcups_one_query": float(np.sum(cells1) / np.sum(sw1) / 1e6),
-             "sw_gcups_batch64": float(np.sum(cells64) / np.sum(sw64) / 1e6),
+             "sw_gcups_batch": float(np.sum(cells_b) / np.sum(sw_b) / 1e6),
              "cells_per_query": float(np.mean(cells1))}
     if rates is None:
-        batch_qps = 64.0 / (float(np.sum(full_med)) * 1e-3)
+        batch_qps = B / (float(np.sum(full_med)) * 1e-3)
         rates = tuple(int(max(10, round(batch_qps * f, -1))) for f in (0.1, 0.3, 0.6, 0.9))
     server = SearchServer(db, top_k=10, max_cands=500, kmer_score_thresh=thresh, **scoring).start()
+    # a serving process keeps its start-up objects (database arrays, query
+    # set) out of the cyclic collector, whose full passes over them would
+    # pause the scheduler thread for tens of milliseconds
+    gc.collect()
+    gc.freeze()
     sweep = []
     rng = np.random.default_rng(3)
     qi = 0
@@ -847,6 +862,7 @@ def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scori
             log(f"search (kmer_score_thresh {thresh}{', C path' if scoring else ''}) rate {rate}/s: {sweep[-1]}")
     finally:
         server.stop()
+        gc.unfreeze()
     return {"plain_loop": plain, "continuous_batching": sweep, "slots": len(server.slots)}
 
 
@@ -858,6 +874,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="10x smaller workload (smoke-testing the bench)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--search-batch", type=int, default=64,
+                    help="most queries per search batch (the server's slot size)")
+    ap.add_argument("--search-modes", default="exact,similar,c_path",
+                    help="search leg scoring modes: exact, similar, c_path (comma list)")
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24); 0 = library default")
     ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default")
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")

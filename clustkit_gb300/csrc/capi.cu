@@ -127,13 +127,16 @@ void *scratch(int slot, size_t bytes, int32_t *status) {
             *status = CK_ERR_UNSUPPORTED;
             return nullptr;
         }
+        // grow by at least half again, so that a growing workload reallocates
+        // (and, through cudaFree, synchronises the device) only a few times
+        const size_t old = s->cap[slot];
         if (s->buf[slot]) {
             cudaError_t e = cudaFree(s->buf[slot]);  // synchronises with work still using it
             s->buf[slot] = nullptr;
             s->cap[slot] = 0;
             if (e != cudaSuccess) { *status = cuda_status(e, "cudaFree(scratch)"); return nullptr; }
         }
-        size_t want = std::max(bytes, s->cap[slot] + s->cap[slot] / 4);
+        size_t want = std::max(bytes, old + old / 2);
         want = (want + 255) & ~(size_t)255;
         cudaError_t e = cudaMalloc(&s->buf[slot], want);
         if (e != cudaSuccess) {

@@ -50,7 +50,7 @@ from .pairwise import ENGINE_BATCHED, PASS_SCORE
 
 LAMBDA = np.float32(0.267)
 _SUB = np.ascontiguousarray(BLOSUM62, np.int8)
-GRAPH_BUCKETS = (1, 2, 4, 8, 16, 32, 64)
+GRAPH_BUCKETS = (1, 2, 4, 8, 16, 32, 64, 128, 256)
 
 
 def compute_freq_threshold(kmer_freqs, num_sequences: int, percentile: float = 99.5) -> int:
@@ -366,6 +366,11 @@ class _Slot:
             with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
                 self._enqueue(b, db.arena_residues, db.arena_residues, sc)
             self.graphs[b] = g
+        # one replay of each (empty queries) so no graph's first upload falls
+        # on a request
+        with torch.cuda.stream(self.stream):
+            for b in buckets:
+                self.graphs[b].replay()
         self.graph_min_hits = int(min_total_hits)
         self.stream.synchronize()
 
@@ -403,18 +408,30 @@ class _Slot:
         sims = self.h_sims.numpy()[: nq * K].reshape(nq, K)
         scores = self.h_scores.numpy()[: nq * K].reshape(nq, K)
         mask = self.h_mask.numpy()[: nq * K].reshape(nq, K)
-        # one vectorised pass over the batch: candidates that passed, their
-        # rank, then a stable sort by (query, -rank) -- per query this is the
-        # stable descending-rank order
+        # one vectorised pass over the batch: candidates that passed and their
+        # rank; per query only those ranked at least its top_k-th best can be
+        # hits (ties included); then a stable sort by (query, -rank) -- per
+        # query the stable descending-rank order.  The sort key packs the query
+        # above the order-preserving integer image of -rank (one int64 argsort
+        # instead of a two-key lexsort; the same order, ties to the earlier
+        # candidate).
         col = np.arange(K)[None, :]
         keep = (col < n[:, None]) & mask.astype(bool)
         qi, ci = np.nonzero(keep)
         t = tg[qi, ci]
+        rank = LAMBDA * scores[qi, ci].astype(np.float32) - np.log(
+            lens[qi].astype(np.float32) * db.lengths_host[t].astype(np.float32))
+        if top_k < K and len(qi):
+            r2 = np.full((nq, K), -np.inf, np.float32)
+            r2[qi, ci] = rank
+            kth = np.partition(r2, K - top_k, axis=1)[:, K - top_k]  # each query's top_k-th largest
+            near = rank >= kth[qi]
+            qi, ci, t, rank = qi[near], ci[near], t[near], rank[near]
         sc = scores[qi, ci]
         si = sims[qi, ci]
-        rank = LAMBDA * sc.astype(np.float32) - np.log(
-            lens[qi].astype(np.float32) * db.lengths_host[t].astype(np.float32))
-        order = np.lexsort((-rank, qi))
+        neg = (-rank + np.float32(0)).view(np.int32)  # + 0 folds -0.0 into +0.0
+        ordered = np.where(neg < 0, neg ^ np.int32(0x7FFFFFFF), neg).astype(np.int64) + (1 << 31)
+        order = np.argsort((qi.astype(np.int64) << 32) | ordered, kind="stable")
         qs = qi[order]
         first = np.searchsorted(qs, np.arange(nq + 1))
         out = []
@@ -497,8 +514,12 @@ class SearchServer:
         self.latencies: list[float] = []
         self.thread = None
         # allocate every slot's scratch before serving: capture its pipeline in
-        # CUDA graphs (one replay per batch), or warm it with one batch
-        warm = [np.arange(40, dtype=np.uint8) % 20]
+        # CUDA graphs (one replay per batch), or warm it with a full batch of
+        # typical queries (random residues, 400 long) so that serving rarely
+        # grows a buffer (a growth synchronises the device)
+        rng = np.random.default_rng(0)
+        wl = max(1, min(400, db.arena_residues // self.max_batch))
+        warm = [rng.integers(0, 20, wl).astype(np.uint8) for _ in range(self.max_batch)]
         for s in self.slots:
             if use_graphs and sc.graphable:
                 s.capture_graphs(min_total_hits)
