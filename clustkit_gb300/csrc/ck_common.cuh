@@ -208,6 +208,7 @@ enum ScratchSlot {
     SLOT_SEARCH_COUNTS,
     SLOT_SEARCH_CAND,
     SLOT_SEARCH_IDX,
+    SLOT_SEARCH_SCORES,
     SLOT_SEARCH_TMP0,
     SLOT_SEARCH_TMP1,
     SLOT_SEARCH_TMP2,

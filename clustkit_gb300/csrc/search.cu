@@ -658,15 +658,18 @@ struct PhaseAArgs {
     int32_t k, alpha; const int64_t *kmer_offsets; const int64_t *kmer_entries;
     const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
     int32_t *out_targets; int32_t *out_scores; int32_t *out_n; cudaStream_t st;
+    bool ordered = true;  // capped rows in (score desc, id asc) order, not only the set
 };
 
-// The select, then the order of rows capped above CAND_CAP (when scores are
-// written; without them only the set matters).
+// The select, then the order of rows capped above CAND_CAP.  `ordered`:
+// the rows are a call's output (without it only the set matters, as for the
+// Phase-B selection); their scores go to a scratch row when the caller
+// takes none.
 static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, int32_t min_hits, int32_t top_k,
                            int32_t clamp, int32_t top_shift, const int32_t *cand, const int32_t *n_cand,
-                           int32_t *out_t, int32_t *out_s, int32_t *out_n, cudaStream_t st) {
+                           int32_t *out_t, int32_t *out_s, int32_t *out_n, bool ordered, cudaStream_t st) {
     int32_t status = CK_OK;
-    const bool sort = top_k > CAND_CAP && out_s;
+    const bool sort = top_k > CAND_CAP && ordered;
     int32_t *aux = nullptr;
     if (sort) {
         if ((int64_t)nq * top_k >= INT32_MAX) {
@@ -675,6 +678,10 @@ static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, in
         }
         aux = (int32_t *)scratch(SLOT_SEARCH_TMP3, (size_t)nq * 12, &status);
         if (!aux) return status;
+        if (!out_s) {
+            out_s = (int32_t *)scratch(SLOT_SEARCH_SCORES, (size_t)nq * top_k * 4, &status);
+            if (!out_s) return status;
+        }
     }
     phase_a_select_kernel<<<nq, SELECT_THREADS, 0, st>>>(counts, num_db, min_hits, top_k, clamp, top_shift, cand,
                                                          n_cand, out_t, out_s, out_n, aux);
@@ -773,7 +780,7 @@ static int32_t phase_a_impl(void *pv) {
         }
     }
     return select_rows(counts, a.nq, a.num_db, a.min_hits, a.top_k, clamp, top_shift, cand, n_cand,
-                       a.out_targets, a.out_scores, a.out_n, a.st);
+                       a.out_targets, a.out_scores, a.out_n, a.ordered, a.st);
 }
 
 }  // namespace ck
@@ -876,6 +883,7 @@ static int32_t candidates_impl(void *pv) {
     a1.out_targets = sel;
     a1.out_scores = nullptr;
     a1.out_n = sel_n;
+    a1.ordered = false;  // only the selected set matters
     CK_TRY(phase_a_impl(&a1));
     int32_t *counts = (int32_t *)scratch(SLOT_SEARCH_COUNTS, nq * (size_t)a.num_db * 4 + 4, &status);
     if (!counts) return status;
@@ -918,7 +926,7 @@ static int32_t candidates_impl(void *pv) {
                                          counts, hint_sel, cand, n_cand);
     CK_CUDA(cudaGetLastError());
     CK_TRY(select_rows(counts, a.nq, a.num_db, c.min_diag_hits, a.top_k, INT32_MAX, 24, cand, n_cand,
-                       a.out_targets, a.out_scores, a.out_n, a.st));
+                       a.out_targets, a.out_scores, a.out_n, true, a.st));
     if (c.out_diags) {
         const dim3 g3((unsigned)std::min(64, (a.top_k + 255) / 256), (unsigned)a.nq);
         pb_hints_kernel<<<g3, 256, 0, a.st>>>(a.out_targets, a.out_n, a.top_k, idx_row, a.num_db, hint_sel, topk,

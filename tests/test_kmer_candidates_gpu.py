@@ -17,7 +17,7 @@ def _queries(g):
     return [g["q_flat"][o:o + L] for o, L in zip(g["q_offsets"], g["q_lengths"])]
 
 
-def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True):
+def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_scores=True):
     """Per query (ids, scores, diags) from one call of the C-ABI entry point."""
     import torch
     from clustkit_gb300 import _lib
@@ -42,7 +42,8 @@ def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True):
             int(lens.max()) if nq else 0, db.k, db.alpha, db.d_kmer_offsets.data_ptr(),
             db.d_kmer_entries.data_ptr(), db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n,
             db.d_lengths.data_ptr(), int(mth), int(mdh), int(width), int(mc), int(topk), out_t.data_ptr(),
-            out_s.data_ptr(), out_d.data_ptr() if with_diags else None, out_n.data_ptr(), st))
+            out_s.data_ptr() if with_scores else None, out_d.data_ptr() if with_diags else None,
+            out_n.data_ptr(), st))
         _lib.check(lib.ck_ctx_status(ctx, st))
     finally:
         lib.ck_ctx_destroy(ctx)
@@ -108,6 +109,12 @@ def test_device_kmer_candidates_vs_oracle_edges(ck):
                 capped_big += len(full) > mc
     assert over >= 2  # the long background queries at one bin per target
     assert capped_big >= 2  # rows capped above 4,096 (the segmented sort)
+    # the same order when the caller takes no scores (nor hints)
+    for mth, mdh, width, mc, topk in [(1, 2, 100000, 5000, 10 ** 6), (1, 1, 10, 6000, 10000)]:
+        a = _device_candidates(db, qs, mth, mdh, width, mc, topk)
+        b = _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=False, with_scores=False)
+        for qi in range(len(qs)):
+            assert np.array_equal(a[qi][0], b[qi][0]), (mth, mdh, width, mc, topk, qi)
 
 
 def _oracle_search(db_set, qs, top_k, mth, mdh, width, mc, topk, band, hints):
