@@ -583,6 +583,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
         if (rotate && T_first >= lane * D) s = lane + 32 * ((T_first - lane * D) / (32 * D));
         int32_t next_switch = rotate ? (s + 32) * D : INT32_MAX;
         int32_t i0 = 0, lo0 = 0, J0 = 0, J1 = -1, alive = 0;
+        uint32_t bcol_n = 0;  // residue offset of the strip's next column, loaded a step ahead
         StripRegs<R> S;
         auto setup = [&]() {
             i0 = s * R + 1;
@@ -590,6 +591,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             J0 = lo0 > 1 ? lo0 : 1;
             J1 = i0 + R - 1 + h + w < lb ? i0 + R - 1 + h + w : lb;
             if (s >= n_strips) { J0 = 1; J1 = 0; }
+            bcol_n = J0 <= J1 ? (uint32_t)__ldg(B + J0 - 1) * 128u : 0u;
             alive = la - i0 + 1 < R ? la - i0 + 1 : R;
             if (alive < 0) alive = 0;
 #pragma unroll
@@ -628,7 +630,8 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             if (s == 0 || j > top) { hin = 0; ein = NEG_E; }
             int32_t cm = 0;
             if (j >= J0 && j <= J1) {
-                const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
+                const uint32_t bcol = bcol_n;
+                if (j < J1) bcol_n = (uint32_t)__ldg(B + j) * 128u;  // column j + 1
                 int32_t hu = hin, eu = ein;
                 strip_cells<R, 0, R, true>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2, alive), one);
                 hout = hu;
@@ -756,6 +759,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
     int32_t cur_slot = -1, cur_s = 0, i0 = 0, lo0 = 0, J0 = 1, J1 = 0, alive = 0, te = 0, top = 0;
     int32_t jb = 0;    // j = T + jb for the strip held
     uint32_t w2s = 0;  // 2w of its pair
+    uint32_t bcol_n = 0;  // residue offset of its next column, loaded a step ahead
     int32_t pend_slot = -1, pend_s = 0, pend_t0 = 0;
     int32_t F = -1;
     int32_t hout = 0, eout = NEG_E, hprev = 0;
@@ -831,6 +835,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             jb = sl.J00 - sl.T0 - cur_s;
             w2s = 2u * (uint32_t)sl.w;
             B = in.flat + sl.b_off;
+            bcol_n = J0 <= J1 ? (uint32_t)__ldg(B + J0 - 1) * 128u : 0u;
             const uint8_t *A = in.flat + sl.a_off;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -853,7 +858,8 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             hprev = hin;
             if (cur_s == 0 || j > top) { hin = 0; ein = NEG_E; }
             if (j >= J0 && j <= J1) {
-                const uint32_t bcol = (uint32_t)__ldg(B + j - 1) * 128u;
+                const uint32_t bcol = bcol_n;
+                if (j < J1) bcol_n = (uint32_t)__ldg(B + j) * 128u;  // column j + 1
                 int32_t hu = hin, eu = ein;
                 strip_cells<R, 0, R, true>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2s, alive), one);
                 hout = hu;
