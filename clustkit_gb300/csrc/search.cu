@@ -167,11 +167,26 @@ constexpr int32_t CAND_CAP = 4096;
 
 // Grid (blocks, nq): the warps of a query's blocks take its k-mer positions
 // in turn; a warp walks one posting list, lanes adding hits in parallel.
+// Target of posting entry h: from the compact int32 copy when there is one
+// (clustkit's kmer_entries_compact, clustkit/database.py:128-135: half the
+// bytes per posting for the Phase-A walks), else the full entry's high half.
+__device__ __forceinline__ int32_t entry_target(const int64_t *__restrict__ entries,
+                                                const int32_t *__restrict__ targets, int64_t h) {
+    return targets ? __ldg(targets + h) : (int32_t)(entries[h] >> 32);
+}
+
+__global__ void compact_targets_kernel(const int64_t *__restrict__ entries, int64_t n,
+                                       int32_t *__restrict__ targets) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        targets[i] = (int32_t)(entries[i] >> 32);
+}
+
 __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len,
                                      const int64_t *__restrict__ qoff,
                                      const int32_t *__restrict__ qlen, int32_t k, int32_t alpha,
                                      const int64_t *__restrict__ kmer_offsets,
                                      const int64_t *__restrict__ kmer_entries,
+                                     const int32_t *__restrict__ kmer_targets,
                                      const int32_t *__restrict__ kmer_freqs, int32_t freq_thresh,
                                      int32_t num_db, int32_t *__restrict__ counts, int32_t min_hits,
                                      int32_t *__restrict__ cand, int32_t *__restrict__ n_cand,
@@ -198,7 +213,7 @@ __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t 
         if (!ok || kmer_freqs[v] > freq_thresh) continue;
         const int64_t b = kmer_offsets[v], e = kmer_offsets[v + 1];
         for (int64_t h = b + lane; h < e; h += 32) {
-            const int32_t t = (int32_t)(kmer_entries[h] >> 32);
+            const int32_t t = entry_target(kmer_entries, kmer_targets, h);
             if (t >= 0 && t < num_db) {
                 // the hit that lifts a target to min_hits lists it (once: counts only grow)
                 if (atomicAdd(&c[t], 1) == min_hits - 1) {
@@ -444,7 +459,8 @@ __global__ void cap_unpack_kernel(const uint64_t *__restrict__ keys, const int32
 // one thread per (query position, first two residues) enumerates the rest by
 // branch and bound -- the same pruning bound, max remaining row scores -- and
 // lists (5-mer value, score) per query, in a counting pass and then an
-// emitting pass; stage 2: a warp per listed 5-mer walks its posting list.
+// emitting pass; stage 2: a warp takes 32 listed 5-mers at a time and walks
+// their posting lists as one stream.
 constexpr int32_t NB_PREFIX = 400;
 
 // Work item (q, t): query position p = t / 400, first residues (a0, a1) =
@@ -519,26 +535,68 @@ __global__ void fill_kernel(int32_t *a, int32_t n, int32_t v) {
     for (int32_t i = threadIdx.x; i < n; i += blockDim.x) a[i] = v;
 }
 
+// A warp takes 32 listed 5-mers at once: each lane loads one (value, score)
+// and its posting-list bounds -- 32 independent loads instead of 32 chains
+// -- then the warp walks the concatenated lists, lane k of each round taking
+// entry k of the stream (its list found by a binary search over the lanes'
+// exclusive prefix sums of list lengths) and adding the 5-mer's score to
+// the entry's target.
 __global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int64_t *__restrict__ item,
                                     int64_t stride, const int64_t *__restrict__ kmer_offsets,
-                                    const int64_t *__restrict__ kmer_entries, int32_t num_db,
+                                    const int64_t *__restrict__ kmer_entries,
+                                    const int32_t *__restrict__ kmer_targets, int32_t num_db,
                                     int32_t *__restrict__ counts, int32_t *err) {
+    constexpr uint32_t FULL = 0xffffffffu;
     const int32_t q = blockIdx.y;
     const int lane = threadIdx.x & 31;
     const int64_t e0 = item[(int64_t)q * stride], e1 = item[(int64_t)(q + 1) * stride];
     int32_t *c = counts + (int64_t)q * num_db;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t e = e0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); e < e1; e += warps) {
-        const uint64_t x = list[e];
-        const int32_t v = (int32_t)(x & 0xffffffffu), w = (int32_t)(x >> 32);
-        const int64_t b = kmer_offsets[v], en = kmer_offsets[v + 1];
-        for (int64_t h = b + lane; h < en; h += 32) {
-            const int32_t t = (int32_t)(kmer_entries[h] >> 32);
-            if (t < 0 || t >= num_db) { atomicOr(err, ERRBIT_PAIR_INDEX); continue; }
-            // no candidate list here (most of the database crosses min_hits in
-            // this mode; the select scans the row): the add's result is unused,
-            // so it issues as a reduction
-            atomicAdd(&c[t], w);
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int64_t base = e0 + wid * 32; base < e1; base += warps * 32) {
+        const int64_t e = base + lane;
+        int64_t b = 0;
+        int32_t len = 0, w = 0;
+        if (e < e1) {
+            const uint64_t x = list[e];
+            const int32_t v = (int32_t)(x & 0xffffffffu);
+            w = (int32_t)(x >> 32);
+            b = kmer_offsets[v];
+            len = (int32_t)(kmer_offsets[v + 1] - b);
+        }
+        int32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int32_t excl = incl - len;
+        const int32_t total = __shfl_sync(FULL, incl, 31);
+        // rounds are warp-uniform so that every shuffle reads a live lane
+        for (int32_t k0 = 0; k0 < total; k0 += 32) {
+            const int32_t k = k0 + lane;
+            // the stream's entry k belongs to the last lane whose list starts
+            // at or before k (lanes with empty lists share their successor's
+            // start and lose to it)
+            int32_t o = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const int32_t cand = o + step;
+                if (__shfl_sync(FULL, excl, cand) <= k) o = cand;
+            }
+            const int64_t h = __shfl_sync(FULL, b, o) + (k - __shfl_sync(FULL, excl, o));
+            const int32_t wo = __shfl_sync(FULL, w, o);
+            if (k < total) {
+                const int32_t t = entry_target(kmer_entries, kmer_targets, h);
+                if (t < 0 || t >= num_db) {
+                    atomicOr(err, ERRBIT_PAIR_INDEX);
+                } else {
+                    // no candidate list here (most of the database crosses
+                    // min_hits in this mode; the select scans the row): the
+                    // add's result is unused
+                    atomicAdd(&c[t], wo);
+                }
+            }
         }
     }
 }
@@ -655,7 +713,7 @@ __global__ void pb_hints_kernel(const int32_t *__restrict__ out_t, const int32_t
 struct PhaseAArgs {
     const int8_t *sub_host; int32_t score_thresh;  // similar k-mers when sub_host != nullptr
     const uint8_t *qflat; int64_t qflat_len; const int64_t *qoff; const int32_t *qlen; int32_t nq; int32_t max_qlen;
-    int32_t k, alpha; const int64_t *kmer_offsets; const int64_t *kmer_entries;
+    int32_t k, alpha; const int64_t *kmer_offsets; const int64_t *kmer_entries; const int32_t *kmer_targets;
     const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
     int32_t *out_targets; int32_t *out_scores; int32_t *out_n; cudaStream_t st;
     bool ordered = true;  // capped rows in (score desc, id asc) order, not only the set
@@ -727,7 +785,8 @@ static int32_t phase_a_impl(void *pv) {
             if (bx > 16) bx = 16;
             dim3 grid((unsigned)bx, (unsigned)a.nq);
             phase_a_count_kernel<<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha,
-                                                          a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
+                                                          a.kmer_offsets, a.kmer_entries, a.kmer_targets,
+                                                          a.kmer_freqs,
                                                           a.freq_thresh, a.num_db, counts, a.min_hits, cand,
                                                           n_cand, err);
             CK_CUDA(cudaGetLastError());
@@ -767,12 +826,12 @@ static int32_t phase_a_impl(void *pv) {
                                                            a.score_thresh, a.kmer_freqs, a.freq_thresh, stride,
                                                            item, list, err);
             CK_CUDA(cudaGetLastError());
-            int by = (int)((total / (a.nq > 0 ? a.nq : 1) + 7) / 8);
+            int by = (int)((total / (a.nq > 0 ? a.nq : 1) + 255) / 256);  // 8 warps x 32 5-mers
             const int by_cap = std::max(4 * sm_count(), 16 * sm_count() / std::max(1, (int)a.nq));
             if (by > by_cap) by = by_cap;
             if (by < 1) by = 1;
             nbr_postings_kernel<<<dim3((unsigned)by, (unsigned)a.nq), 256, 0, a.st>>>(
-                list, item, stride, a.kmer_offsets, a.kmer_entries, a.num_db, counts, err);
+                list, item, stride, a.kmer_offsets, a.kmer_entries, a.kmer_targets, a.num_db, counts, err);
             CK_CUDA(cudaGetLastError());
             // the select scans the whole count row (no candidate list in this mode)
             fill_kernel<<<1, 256, 0, a.st>>>(n_cand, a.nq, CAND_CAP + 1);
@@ -807,23 +866,43 @@ extern "C" int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat
     return run_in_context(ctx, index_build_impl, &a);
 }
 
+extern "C" int32_t ck_kmer_targets_device(int32_t ctx, const int64_t *d_kmer_entries, int64_t n_entries,
+                                          int32_t *d_kmer_targets, void *stream) {
+    std::lock_guard<std::mutex> lock(library_mutex());
+    reset_thread_status();
+    if (n_entries < 0 || (n_entries > 0 && (!d_kmer_entries || !d_kmer_targets))) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "kmer targets: bad arguments");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    struct Args { const int64_t *e; int64_t n; int32_t *t; cudaStream_t st; } a{d_kmer_entries, n_entries,
+                                                                                 d_kmer_targets, (cudaStream_t)stream};
+    return run_in_context(ctx, [](void *pv) -> int32_t {
+        const Args &a = *(const Args *)pv;
+        if (a.n == 0) return CK_OK;
+        compact_targets_kernel<<<grid_for(a.n, 256), 256, 0, a.st>>>(a.e, a.n, a.t);
+        CK_CUDA(cudaGetLastError());
+        return CK_OK;
+    }, &a);
+}
+
 extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                             const int64_t *d_qoffsets,
                                             const int32_t *d_qlengths, int32_t nq, int32_t max_qlen,
                                             int32_t k, int32_t alpha, const int64_t *d_kmer_offsets,
-                                            const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
-                                            int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
-                                            int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
-                                            int32_t *d_out_n, void *stream) {
+                                            const int64_t *d_kmer_entries, const int32_t *d_kmer_targets,
+                                            const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+                                            int32_t min_total_hits, int32_t top_k, int32_t *d_out_targets,
+                                            int32_t *d_out_scores, int32_t *d_out_n, void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
     if (nq < 0 || nq > 65535 || qflat_len < 0 || top_k < 1 || k < 1 || alpha < 1 || num_db < 0 || !d_out_targets || !d_out_n ||
-        (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets || !d_kmer_freqs) {
+        (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets || !d_kmer_freqs ||
+        (!d_kmer_entries && !d_kmer_targets)) {
         set_error(CK_ERR_INVALID_ARGUMENT, "phase A: bad arguments");
         return CK_ERR_INVALID_ARGUMENT;
     }
     PhaseAArgs a{nullptr, 0, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha, d_kmer_offsets, d_kmer_entries,
-                 d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k, d_out_targets, d_out_scores,
+                 d_kmer_targets, d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k, d_out_targets, d_out_scores,
                  d_out_n, (cudaStream_t)stream};
     return run_in_context(ctx, phase_a_impl, &a);
 }
@@ -832,21 +911,21 @@ extern "C" int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *
                                                     const int64_t *d_qoffsets, const int32_t *d_qlengths,
                                                     int32_t nq, int32_t max_qlen, const int8_t *sub_matrix_host,
                                                     int32_t kmer_score_thresh, const int64_t *d_kmer_offsets,
-                                                    const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
-                                                    int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
-                                                    int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
-                                                    int32_t *d_out_n, void *stream) {
+                                                    const int64_t *d_kmer_entries, const int32_t *d_kmer_targets,
+                                                    const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+                                                    int32_t min_total_hits, int32_t top_k, int32_t *d_out_targets,
+                                                    int32_t *d_out_scores, int32_t *d_out_n, void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
     if (nq < 0 || nq > 65535 || qflat_len < 0 || top_k < 1 || num_db < 0 || !sub_matrix_host ||
         kmer_score_thresh < 1 || !d_out_targets || !d_out_n || (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) ||
-        !d_kmer_offsets || !d_kmer_freqs) {
+        !d_kmer_offsets || !d_kmer_freqs || (!d_kmer_entries && !d_kmer_targets)) {
         set_error(CK_ERR_INVALID_ARGUMENT, "similar k-mer phase A: bad arguments");
         return CK_ERR_INVALID_ARGUMENT;
     }
     PhaseAArgs a{sub_matrix_host, kmer_score_thresh, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, 5,
-                 20, d_kmer_offsets, d_kmer_entries, d_kmer_freqs, freq_thresh, num_db, min_total_hits, top_k,
-                 d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream};
+                 20, d_kmer_offsets, d_kmer_entries, d_kmer_targets, d_kmer_freqs, freq_thresh, num_db,
+                 min_total_hits, top_k, d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream};
     return run_in_context(ctx, phase_a_impl, &a);
 }
 
@@ -941,21 +1020,22 @@ static int32_t candidates_impl(void *pv) {
 extern "C" int32_t ck_search_kmer_candidates_device(
     int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len, const int64_t *d_qoffsets, const int32_t *d_qlengths,
     int32_t nq, int32_t max_qlen, int32_t k, int32_t alpha, const int64_t *d_kmer_offsets,
-    const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
-    const int32_t *d_db_lengths, int32_t min_total_hits, int32_t min_diag_hits, int32_t diag_bin_width,
-    int32_t max_cands, int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores, int32_t *d_out_diags,
-    int32_t *d_out_n, void *stream) {
+    const int64_t *d_kmer_entries, const int32_t *d_kmer_targets, const int32_t *d_kmer_freqs, int32_t freq_thresh,
+    int32_t num_db, const int32_t *d_db_lengths, int32_t min_total_hits, int32_t min_diag_hits,
+    int32_t diag_bin_width, int32_t max_cands, int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores,
+    int32_t *d_out_diags, int32_t *d_out_n, void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
     if (nq < 0 || nq > 65535 || qflat_len < 0 || max_cands < 1 || k < 1 || alpha < 1 || num_db < 0 ||
         !d_out_targets || !d_out_n || (nq > 0 && (!d_qflat || !d_qoffsets || !d_qlengths)) || !d_kmer_offsets ||
-        !d_kmer_freqs || (min_diag_hits >= 2 && (!d_db_lengths || diag_bin_width < 1 || phase_a_topk < 1))) {
+        !d_kmer_freqs || (!d_kmer_entries && !d_kmer_targets) ||
+        (min_diag_hits >= 2 && (!d_kmer_entries || !d_db_lengths || diag_bin_width < 1 || phase_a_topk < 1))) {
         set_error(CK_ERR_INVALID_ARGUMENT, "k-mer candidates: bad arguments");
         return CK_ERR_INVALID_ARGUMENT;
     }
     CandArgs c{PhaseAArgs{nullptr, 0, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha,
-                          d_kmer_offsets, d_kmer_entries, d_kmer_freqs, freq_thresh, num_db, min_total_hits, max_cands,
-                          d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream},
+                          d_kmer_offsets, d_kmer_entries, d_kmer_targets, d_kmer_freqs, freq_thresh, num_db,
+                          min_total_hits, max_cands, d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream},
                d_db_lengths, min_diag_hits, diag_bin_width, phase_a_topk, d_out_diags};
     return run_in_context(ctx, candidates_impl, &c);
 }

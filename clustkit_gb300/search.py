@@ -119,7 +119,7 @@ class DeviceDatabase:
     def __init__(self, flat, offsets, lengths, k: int = 5, freq_percentile: float = 95.0,
                  band_width: int | None = None, arena_slots: int = 1, arena_queries: int = 64,
                  arena_residues: int = 64 * 2000, sketch_size: int = 128, sketch_k: int = 5,
-                 device: str = "cuda:0"):
+                 device: str = "cuda:0", compact_index: bool = True):
         torch = _torch()
         self.lib = _lib.load()
         _lib.require_gpu()
@@ -165,6 +165,13 @@ class DeviceDatabase:
             self.d_kmer_entries.data_ptr(), positions, self.d_kmer_freqs.data_ptr(),
             total.ctypes.data, stream))
         self.n_entries = int(total[0])
+        # the compact Phase-A index (target ids only), read by the Phase-A walks
+        self.d_kmer_targets = None
+        if compact_index:
+            self.d_kmer_targets = torch.empty(max(self.n_entries, 1), dtype=torch.int32, device=self.dev)
+            _lib.check(self.lib.ck_kmer_targets_device(0, self.d_kmer_entries.data_ptr(), self.n_entries,
+                                                       self.d_kmer_targets.data_ptr(), stream))
+        self.kmer_targets_ptr = self.d_kmer_targets.data_ptr() if self.d_kmer_targets is not None else None
         freqs = self.d_kmer_freqs.cpu().numpy()
         self.freq_thresh = compute_freq_threshold(freqs, self.n, freq_percentile)
         if band_width is None:
@@ -307,12 +314,12 @@ class _Slot:
             _lib.check(lib.ck_search_phase_a_similar_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen, _SUB.ctypes.data,
                 int(sc.kmer_score_thresh), db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
-                db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
+                db.kmer_targets_ptr, db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
         elif sc.diagonal:  # the C scorer's Phase A + Phase B, with diagonal hints
             _lib.check(lib.ck_search_kmer_candidates_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
-                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr,
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, db.d_lengths.data_ptr(), min_total_hits,
                 int(sc.min_diag_hits), int(sc.diag_bin_width), K, int(sc.phase_a_topk),
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_diags.data_ptr(),
@@ -320,7 +327,7 @@ class _Slot:
         else:
             _lib.check(lib.ck_search_phase_a_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
-                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
+                db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr,
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
         self._mark(2)

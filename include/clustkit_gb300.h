@@ -254,6 +254,14 @@ int32_t ck_kmer_index_build_device(int32_t ctx, const uint8_t *d_flat, int64_t f
                                    int64_t *d_kmer_entries, int64_t entries_capacity,
                                    int32_t *d_kmer_freqs, int64_t *out_total, void *stream);
 
+/* The compact Phase-A index (clustkit's kmer_entries_compact,
+ * clustkit/database.py:128-135): d_kmer_targets int32[n_entries] = the
+ * sequence ids of d_kmer_entries.  The Phase-A walks below read it instead of
+ * the full entries when given (half the bytes per posting); the entries stay
+ * needed for Phase B. */
+int32_t ck_kmer_targets_device(int32_t ctx, const int64_t *d_kmer_entries, int64_t n_entries,
+                               int32_t *d_kmer_targets, void *stream);
+
 /* LSH candidate pairs on the device (clustkit/lsh.py:20-178): d_sketches is
  * uint64 [n][s]; band_idx_host int32 [num_tables][num_bands] and seeds_host
  * uint64 [num_tables] are the per-table band positions and seeds (clustkit
@@ -276,16 +284,17 @@ int32_t ck_lsh_candidates_device(int32_t ctx, const uint64_t *d_sketches, int64_
  * sub_matrix_host (int8 [20][20], row = query residue) against a query 5-mer
  * is >= kmer_score_thresh adds that score to each target of its posting list
  * (k-mers with frequency 0 or above freq_thresh skipped); sums are int32, not
- * saturated; survivors and cap as above.  Blocking (it sizes its neighbour
- * list on the host). */
+ * saturated; survivors and cap as above.  d_kmer_targets (may be NULL) as
+ * in ck_search_phase_a_device.  Blocking (it sizes its neighbour list on the
+ * host). */
 int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                          const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,
                                          int32_t max_qlen, const int8_t *sub_matrix_host,
                                          int32_t kmer_score_thresh, const int64_t *d_kmer_offsets,
-                                         const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
-                                         int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
-                                         int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
-                                         int32_t *d_out_n, void *stream);
+                                         const int64_t *d_kmer_entries, const int32_t *d_kmer_targets,
+                                         const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+                                         int32_t min_total_hits, int32_t top_k, int32_t *d_out_targets,
+                                         int32_t *d_out_scores, int32_t *d_out_n, void *stream);
 
 /* The k-mer scorer of clustkit's C/OpenMP search path (batch_score_queries_c,
  * clustkit/csrc/kmer_score.c:420-470, bound at clustkit/kmer_index.py:
@@ -303,14 +312,16 @@ int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, in
  * max_cands best by (score desc, id asc) in that order; d_out_n [nq].
  * d_db_lengths int32 [num_db] (the target lengths size each target's bins; the
  * C scorer sorts its hits instead) is needed only for Phase B.  The k-mer
- * entries are the full (target << 32 | position) ones; the C scorer's
- * optional compact Phase-A entries are a host memory layout and not taken.
- * Blocking (it sizes the bins on the host). */
+ * entries are the full (target << 32 | position) ones (needed for Phase B);
+ * d_kmer_targets (may be NULL) is the compact Phase-A index, which Phase A
+ * then reads, as the C scorer reads its compact_entries.  Blocking (it sizes
+ * the bins on the host). */
 int32_t ck_search_kmer_candidates_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                          const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,
                                          int32_t max_qlen, int32_t k, int32_t alpha,
                                          const int64_t *d_kmer_offsets, const int64_t *d_kmer_entries,
-                                         const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+                                         const int32_t *d_kmer_targets, const int32_t *d_kmer_freqs,
+                                         int32_t freq_thresh, int32_t num_db,
                                          const int32_t *d_db_lengths, int32_t min_total_hits,
                                          int32_t min_diag_hits, int32_t diag_bin_width, int32_t max_cands,
                                          int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores,
@@ -345,15 +356,17 @@ int32_t ck_connected_components_device(int32_t ctx, const int32_t *d_pairs, int6
  * max_qlen sizes the grid only.  Uses nq * num_db * 4 bytes of context
  * scratch.  When more than top_k survive, the top_k are written in descending
  * count order (ties: lower id first), as clustkit's argsort(-scores) orders
- * them; otherwise in id order. */
+ * them; otherwise in id order.  The posting walk reads d_kmer_targets (the
+ * compact index of ck_kmer_targets_device) when it is not NULL, else the
+ * targets of d_kmer_entries; one of the two must be given. */
 int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                  const int64_t *d_qoffsets,
                                  const int32_t *d_qlengths, int32_t nq, int32_t max_qlen, int32_t k,
                                  int32_t alpha, const int64_t *d_kmer_offsets,
-                                 const int64_t *d_kmer_entries, const int32_t *d_kmer_freqs,
-                                 int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
-                                 int32_t top_k, int32_t *d_out_targets, int32_t *d_out_scores,
-                                 int32_t *d_out_n, void *stream);
+                                 const int64_t *d_kmer_entries, const int32_t *d_kmer_targets,
+                                 const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
+                                 int32_t min_total_hits, int32_t top_k, int32_t *d_out_targets,
+                                 int32_t *d_out_scores, int32_t *d_out_n, void *stream);
 
 /* ---------------------------------------------------- measurement probe
  * Sustained lane-operation rate of one integer instruction class on the

@@ -40,7 +40,7 @@ def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_
         _lib.check(lib.ck_search_kmer_candidates_device(
             ctx, d_q.data_ptr(), int(lens.sum()), d_off.data_ptr(), d_len.data_ptr(), nq,
             int(lens.max()) if nq else 0, db.k, db.alpha, db.d_kmer_offsets.data_ptr(),
-            db.d_kmer_entries.data_ptr(), db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n,
+            db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr, db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n,
             db.d_lengths.data_ptr(), int(mth), int(mdh), int(width), int(mc), int(topk), out_t.data_ptr(),
             out_s.data_ptr() if with_scores else None, out_d.data_ptr() if with_diags else None,
             out_n.data_ptr(), st))
@@ -55,12 +55,16 @@ def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_
 
 
 @pytest.mark.gpu
-def test_device_kmer_candidates_match_reference_c_scorer(ck, golden):
+@pytest.mark.parametrize("compact", [True, False])
+def test_device_kmer_candidates_match_reference_c_scorer(ck, golden, compact):
     """Every configuration of the golden set: targets, scores (Phase-A hits or
-    Phase-B runs) in the scorer's order, and the diagonal hints."""
+    Phase-B runs) in the scorer's order, and the diagonal hints; Phase A
+    reading the compact target index or the full entries."""
     from clustkit_gb300.search import DeviceDatabase
     g = golden("kmer_scorer_golden.npz")
-    db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], arena_queries=4, arena_residues=4 * 600)
+    db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], arena_queries=4, arena_residues=4 * 600,
+                        compact_index=compact)
+    assert (db.kmer_targets_ptr is not None) == compact
     assert db.freq_thresh == int(g["freq_thresh"])
     qs = _queries(g)
     for ci, (mth, mdh, width, mc, topk) in enumerate(g["configs"]):

@@ -77,14 +77,17 @@ def test_oracle_search_matches_reference(golden):
 
 
 @pytest.mark.gpu
-def test_device_index_and_phase_a(ck, golden):
+@pytest.mark.parametrize("compact", [True, False])
+def test_device_index_and_phase_a(ck, golden, compact):
     torch = pytest.importorskip("torch")
     from clustkit_gb300.search import DeviceDatabase, _Slot
     g = golden("search_golden.npz")
     db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["band_width"]),
-                        arena_queries=32, arena_residues=32 * 400)
+                        arena_queries=32, arena_residues=32 * 400, compact_index=compact)
     off, ent, fr = db.index_arrays()
     assert np.array_equal(ent, g["kmer_entries"])
+    if compact:  # clustkit's compact Phase-A index: the entries' sequence ids
+        assert np.array_equal(db.d_kmer_targets[: db.n_entries].cpu().numpy(), (ent >> 32).astype(np.int32))
     nz = np.nonzero(fr)[0]
     assert np.array_equal(nz, g["freq_nonzero_idx"]) and np.array_equal(fr[nz], g["freq_nonzero_val"])
     assert off[-1] == g["offsets_total"] and db.freq_thresh == int(g["freq_thresh"])
@@ -263,11 +266,12 @@ def test_oracle_similar_phase_a_matches_reference(golden):
 
 
 @pytest.mark.gpu
-def test_similar_phase_a_and_search_match_reference(ck, golden):
+@pytest.mark.parametrize("compact", [True, False])
+def test_similar_phase_a_and_search_match_reference(ck, golden, compact):
     from clustkit_gb300.search import DeviceDatabase, _Slot, search_batch
     g = golden("search_golden.npz")
     db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["sim_band_width"]),
-                        arena_queries=16, arena_residues=16 * 400)
+                        arena_queries=16, arena_residues=16 * 400, compact_index=compact)
     qs = _queries(g)
     sq = [qs[i] for i in g["sim_queries"]]
     slot = _Slot(db, 0, 1000)
