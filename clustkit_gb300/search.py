@@ -74,6 +74,7 @@ class Scoring:
     use_c_scoring: bool = False
     use_c_sw: bool = False
     c_sw_band_width: int = 50
+    band_width: int | None = None  # SW band without use_c_sw; None: the database's
 
     @property
     def similar(self) -> bool:
@@ -92,7 +93,7 @@ class Scoring:
     @property
     def graphable(self) -> bool:
         """No host synchronisation in the pipeline: exact Phase A, the database band."""
-        return not self.similar and not self.diagonal and not self.use_c_sw
+        return not self.similar and not self.diagonal and not self.use_c_sw and self.band_width is None
 
 
 def _torch():
@@ -331,7 +332,8 @@ class _Slot:
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
         self._mark(2)
-        self.last_band = int(sc.c_sw_band_width) if sc.use_c_sw else db.band_width
+        self.last_band = (int(sc.c_sw_band_width) if sc.use_c_sw else
+                          int(sc.band_width) if sc.band_width is not None else db.band_width)
         # dense pair list: (query, target) or (empty, empty) past a query's candidates
         q = self.d_slotq[:M]
         valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
@@ -404,8 +406,10 @@ class _Slot:
                 self.event.record(self.stream)
         self.batch = (nq, lens)
 
-    def results(self, top_k: int) -> list[list[SearchHit]]:
-        """Hits of the batch (after the slot's event): top_k per query."""
+    def results(self, top_k: int, evalue_normalize: bool = True) -> list[list[SearchHit]]:
+        """Hits of the batch (after the slot's event): top_k per query, ranked
+        by 0.267 * score - ln(qlen * tlen), or by the raw score when
+        evalue_normalize is off (clustkit/kmer_index.py:2315-2323)."""
         db = self.db
         _lib.check(db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream))
         nq, lens = self.batch
@@ -426,8 +430,11 @@ class _Slot:
         keep = (col < n[:, None]) & mask.astype(bool)
         qi, ci = np.nonzero(keep)
         t = tg[qi, ci]
-        rank = LAMBDA * scores[qi, ci].astype(np.float32) - np.log(
-            lens[qi].astype(np.float32) * db.lengths_host[t].astype(np.float32))
+        if evalue_normalize:
+            rank = LAMBDA * scores[qi, ci].astype(np.float32) - np.log(
+                lens[qi].astype(np.float32) * db.lengths_host[t].astype(np.float32))
+        else:
+            rank = scores[qi, ci].astype(np.float32)
         if top_k < K and len(qi):
             r2 = np.full((nq, K), -np.inf, np.float32)
             r2[qi, ci] = rank
@@ -473,6 +480,130 @@ def search_batch(db: DeviceDatabase, queries: list[np.ndarray], top_k: int = 10,
     finally:
         if own:
             slot.close()
+
+
+@dataclass
+class KmerSearchHit:
+    """One hit, with the fields of clustkit's SearchHit (clustkit/search.py:40-48)."""
+    query_id: str
+    target_id: str
+    identity: float
+    query_length: int
+    target_length: int
+    score: float = 0.0  # the rank value: E-value-normalised score, or the raw score
+
+
+@dataclass
+class SearchResults:
+    """Results for all queries, with the fields of clustkit's SearchResults
+    (clustkit/search.py:51-60)."""
+    hits: list[list[KmerSearchHit]]
+    num_queries: int
+    num_targets: int
+    num_candidates: int
+    num_aligned: int
+    runtime_seconds: float
+
+
+_DB_CACHE: dict = {}  # id(db_index) -> (db_index, k, freq_percentile, arena_residues, DeviceDatabase)
+
+_UNSUPPORTED = ("reduced_alphabet", "use_idf", "spaced_seeds", "extra_alphabets", "ml_prefilter_model")
+
+
+def _device_db(db_index, k: int, freq_percentile: float, residues: int, device) -> DeviceDatabase:
+    """The database resident on the GPU, built once per index object (and again
+    only when a call's queries need a larger staging arena)."""
+    hit = _DB_CACHE.get(id(db_index))
+    same = hit is not None and hit[0] is db_index and hit[1] == k and hit[2] == freq_percentile
+    if same and hit[3] >= residues:
+        return hit[4]
+    ds = db_index.dataset
+    arena = max(residues, hit[3] if same else 0, 64 * 400)
+    db = DeviceDatabase(ds.flat_sequences, ds.offsets, ds.lengths, k=k, freq_percentile=freq_percentile,
+                        arena_slots=1, arena_queries=64, arena_residues=arena, device=device)
+    _DB_CACHE.clear()  # one resident database at a time
+    _DB_CACHE[id(db_index)] = (db_index, k, freq_percentile, arena, db)
+    return db
+
+
+def search_kmer_index(db_index, query_dataset, threshold: float = 0.5, top_k: int = 10,
+                      band_width: int | None = None, device="cpu", min_total_hits: int = 2,
+                      min_diag_hits: int = 2, diag_bin_width: int = 10, max_cands_per_query: int = 2000,
+                      phase_a_topk: int = 10000, freq_percentile: float = 95.0, min_ungapped_score: int = 0,
+                      kmer_score_thresh: int = 13, local_alignment: bool = True, evalue_normalize: bool = True,
+                      reduced_alphabet: bool = False, reduced_k=5, use_idf: bool = False, spaced_seeds=None,
+                      extra_alphabets=None, ml_prefilter_model=None, use_c_sw: bool = False,
+                      c_sw_band_width: int = 50, use_c_scoring: bool = False) -> SearchResults:
+    """Drop-in for clustkit's search_kmer_index (clustkit/kmer_index.py:1475-2349)
+    on the GPU: the same arguments, defaults and results for its protein k-mer
+    paths -- exact Phase A, Phase B (min_diag_hits >= 2), BLOSUM62 similar
+    5-mers (kmer_score_thresh > 0, the default), the C scorer and C SW
+    settings -- with banded SW (score > 0 passes; ``threshold`` plays no part
+    there, as in clustkit), the E-value-style rank and the top_k hits per query.
+    ``db_index`` needs ``dataset`` (flat_sequences, offsets, lengths, ids) and
+    ``params`` (mode, kmer_size or kmer_index_k); ``query_dataset`` the same
+    compact fields.  The index is rebuilt on the device from the database
+    sequences (clustkit's layout) and kept resident between calls on the same
+    index object.  The band width, when not given, is clustkit's per-call
+    ``max(20, 0.3 * p95(query and database lengths))``.  ``device`` is the
+    GPU ("cpu" means the default GPU: there is no CPU path).  Options for the
+    search variants not built here raise NotImplementedError."""
+    start = time.perf_counter()
+    opts = {"reduced_alphabet": reduced_alphabet, "use_idf": use_idf, "spaced_seeds": spaced_seeds,
+            "extra_alphabets": extra_alphabets, "ml_prefilter_model": ml_prefilter_model}
+    for name in _UNSUPPORTED:
+        if opts[name]:
+            raise NotImplementedError(f"search_kmer_index: {name} is not built on the GPU")
+    if min_ungapped_score > 0:
+        raise NotImplementedError("search_kmer_index: the ungapped pre-filter is not built on the GPU")
+    if not local_alignment:
+        raise NotImplementedError("search_kmer_index: global (NW) alignment is not built on the GPU")
+    params = db_index.params
+    if params.get("mode", "protein") != "protein":
+        raise NotImplementedError("search_kmer_index: only the protein path is built on the GPU")
+    k = int(params.get("kmer_index_k", params.get("kmer_size", 5)))
+    if kmer_score_thresh > 0 and k != 5:
+        raise NotImplementedError("search_kmer_index: similar k-mer scoring is built for k = 5")
+    nq = len(query_dataset.lengths)
+    nd = len(db_index.dataset.lengths)
+    if nq == 0 or nd == 0:
+        return SearchResults([[] for _ in range(nq)], nq, nd, 0, 0, time.perf_counter() - start)
+    q_flat = np.asarray(query_dataset.flat_sequences, np.uint8)
+    q_off = np.asarray(query_dataset.offsets, np.int64)
+    q_len = np.asarray(query_dataset.lengths, np.int64)
+    queries = [q_flat[o:o + L] for o, L in zip(q_off, q_len)]
+    if band_width is None:
+        p95 = int(np.percentile(np.concatenate([q_len, np.asarray(db_index.dataset.lengths, np.int64)]), 95))
+        band_width = max(20, int(p95 * 0.3))
+    dev = "cuda:0" if device in (None, "cpu", "gpu", "cuda") else (
+        f"cuda:{device}" if isinstance(device, int) or str(device).isdigit() else str(device))
+    db = _device_db(db_index, k, float(freq_percentile), int(q_len.max(initial=1)) * 64, dev)
+    scoring = dict(min_diag_hits=int(min_diag_hits), diag_bin_width=int(diag_bin_width),
+                   phase_a_topk=int(phase_a_topk), use_c_scoring=bool(use_c_scoring), use_c_sw=bool(use_c_sw),
+                   c_sw_band_width=int(c_sw_band_width), band_width=int(band_width))
+    slot = _Slot(db, 0, int(max_cands_per_query))
+    hits: list[list[KmerSearchHit]] = []
+    n_cands = 0
+    q_ids, t_ids = query_dataset.ids, db_index.dataset.ids
+    t_len = db.lengths_host
+    try:
+        i = 0
+        while i < nq:  # chunks within the slot's query and residue capacity
+            j, res = i, 0
+            while j < nq and j - i < db.arena_queries and res + len(queries[j]) <= db.arena_residues:
+                res += len(queries[j])
+                j += 1
+            slot.launch(queries[i:j], int(min_total_hits), int(kmer_score_thresh), **scoring)
+            slot.event.synchronize()
+            n_cands += int(slot.h_n.numpy()[: j - i].sum())
+            for qi, hl in enumerate(slot.results(int(top_k), evalue_normalize=evalue_normalize)):
+                q = i + qi
+                hits.append([KmerSearchHit(q_ids[q], t_ids[h.target], h.identity, int(q_len[q]),
+                                           int(t_len[h.target]), h.rank) for h in hl])
+            i = j
+    finally:
+        slot.close()
+    return SearchResults(hits, nq, nd, n_cands, n_cands, time.perf_counter() - start)
 
 
 @dataclass

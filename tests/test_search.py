@@ -373,3 +373,68 @@ def test_c_oracle_kmer_candidates_match_reference_and_numpy(golden):
             want = so.kmer_candidates(q, 5, 20, off, ent, fr, thr, db_set.n, *cfg)
             for a, b in zip(got[qi], want):
                 assert np.array_equal(a, b), (cfg, qi)
+
+
+def _ref_like_index(g):
+    """The database and queries of a golden file in the shape of clustkit's
+    DatabaseIndex / SequenceDataset (the fields search_kmer_index reads)."""
+    import types
+    db = types.SimpleNamespace(flat_sequences=g["db_flat"], offsets=g["db_offsets"], lengths=g["db_lengths"],
+                               ids=[f"d{i}" for i in range(len(g["db_lengths"]))])
+    idx = types.SimpleNamespace(dataset=db, params={"mode": "protein", "kmer_size": int(g["k"])})
+    return idx
+
+
+def _ref_like_queries(flat, offs, lens, names):
+    import types
+    return types.SimpleNamespace(flat_sequences=flat, offsets=offs, lengths=lens, ids=list(names))
+
+
+@pytest.mark.gpu
+def test_search_kmer_index_dropin_matches_reference(ck, golden):
+    """The drop-in search_kmer_index, called with the arguments the golden run of
+    clustkit's own search_kmer_index used (exact Phase A; BLOSUM62 similar 5-mers
+    on a query subset), returns the same hits: target ids, identities and rank
+    scores, in order, with clustkit's per-call band width."""
+    from clustkit_gb300.search import search_kmer_index
+    g = golden("search_golden.npz")
+    idx = _ref_like_index(g)
+    qs = _ref_like_queries(g["q_flat"], g["q_offsets"], g["q_lengths"], [f"q{i}" for i in range(len(g["q_lengths"]))])
+    res = search_kmer_index(idx, qs, threshold=0.0, top_k=5, band_width=None, min_total_hits=2, min_diag_hits=1,
+                            max_cands_per_query=100000, freq_percentile=95.0, kmer_score_thresh=0,
+                            local_alignment=True, evalue_normalize=True)
+    want = _golden_hits(g)
+    assert res.num_queries == len(want) and res.num_targets == len(g["db_lengths"])
+    for qi, (hl, w) in enumerate(zip(res.hits, want)):
+        assert [int(h.target_id[1:]) for h in hl] == [x[0] for x in w], qi
+        assert [np.float32(h.identity) for h in hl] == [np.float32(x[1]) for x in w], qi
+        assert [np.float32(h.score) for h in hl] == [np.float32(x[2]) for x in w], qi
+        assert all(h.query_id == f"q{qi}" and h.query_length == g["q_lengths"][qi] for h in hl)
+        assert all(h.target_length == g["db_lengths"][int(h.target_id[1:])] for h in hl)
+    # similar 5-mers, clustkit's default scoring, on the golden query subset
+    sq = [int(i) for i in g["sim_queries"]]
+    lens = g["q_lengths"][sq]
+    flat = np.concatenate([g["q_flat"][g["q_offsets"][i]:g["q_offsets"][i] + g["q_lengths"][i]] for i in sq])
+    offs = np.concatenate([[0], np.cumsum(lens[:-1])]).astype(np.int64)
+    res2 = search_kmer_index(idx, _ref_like_queries(flat, offs, lens, [f"q{i}" for i in sq]), threshold=0.0,
+                             top_k=5, band_width=None, min_total_hits=2, min_diag_hits=1,
+                             max_cands_per_query=100000, freq_percentile=95.0, kmer_score_thresh=13)
+    want2 = {}
+    for q, t, i, s in zip(g["sim_hit_query"], g["sim_hit_target"], g["sim_hit_identity"], g["sim_hit_score"]):
+        want2.setdefault(int(q), []).append((int(t), float(i), float(s)))
+    for k, qi in enumerate(sq):
+        hl, w = res2.hits[k], want2.get(qi, [])
+        assert [int(h.target_id[1:]) for h in hl] == [x[0] for x in w], qi
+        assert [np.float32(h.identity) for h in hl] == [np.float32(x[1]) for x in w], qi
+        assert [np.float32(h.score) for h in hl] == [np.float32(x[2]) for x in w], qi
+
+
+def test_search_kmer_index_refuses_unbuilt_variants():
+    """Options for the search variants not built on the GPU fail loudly."""
+    import types
+    from clustkit_gb300.search import search_kmer_index
+    idx = types.SimpleNamespace(dataset=None, params={"mode": "protein", "kmer_size": 5})
+    for kw in ({"reduced_alphabet": True}, {"use_idf": True}, {"spaced_seeds": ["11011"]},
+               {"min_ungapped_score": 5}, {"local_alignment": False}):
+        with pytest.raises(NotImplementedError):
+            search_kmer_index(idx, None, **kw)
