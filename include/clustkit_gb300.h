@@ -1,6 +1,9 @@
 /*
- * clustkit_gb300.h -- C ABI of libckgpu.so, the GB300 (sm_103a) Align-phase
- * and sketch engine for clustkit.
+ * clustkit_gb300.h -- C ABI of libckgpu.so, the GB300 (sm_103a) engine for
+ * clustkit's Align phase (banded SW, sketches, Jaccard pre-filter) and the
+ * steps either side of it: LSH candidates, the k-mer search path (index,
+ * Phase A / similar k-mers / Phase B, hinted SW) and the similarity graph
+ * with its connected components.
  *
  * Conventions
  *   - Every ck_* entry point returns an int status (CK_OK on success) and
@@ -10,7 +13,10 @@
  *   - *_device entry points take device pointers and a cudaStream_t (passed as
  *     void*, NULL = the legacy default stream) and return once the work is
  *     enqueued; results are ready when that stream is synchronised.  Input
- *     errors found on the GPU are reported through ck_sw_status_device().
+ *     errors found on the GPU are reported through ck_sw_status_device() (or
+ *     ck_ctx_status() for a library context).  The ones that must size a
+ *     buffer from a device-side count first say "Blocking" and synchronise
+ *     their stream.
  *   - Pair lists are int32 [M][2]; sequences use clustkit's compact layout
  *     (clustkit/io.py:35-131): uint8 codes `flat`, int64 `offsets[N]`,
  *     int32 `lengths[N]`.  Protein codes are 0..19, unknown residues 20.
