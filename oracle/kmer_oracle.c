@@ -42,6 +42,7 @@ static int cmp_u64k(const void *x, const void *y) {
  * given order stays. */
 static int32_t top_by_score(int32_t *ids, int32_t *sc, int32_t *aux_d, int32_t n, int32_t k, uint64_t *tmp) {
     if (n <= k) return n;
+    if (k <= 0) return 0;
     for (int32_t i = 0; i < n; ++i)
         tmp[i] = ((uint64_t)(uint32_t)(0x7fffffff - sc[i]) << 32) | (uint32_t)i;
     qsort(tmp, (size_t)n, 8, cmp_u64k);
@@ -160,9 +161,11 @@ void or_kmer_candidates(const uint8_t *q_flat, const int64_t *q_offsets, const i
                 n = top_by_score(ids, sc, dg, n, max_cands, tmp);
             }
             out_n[qi] = n;
-            memcpy(out_targets + (int64_t)qi * max_cands, ids, (size_t)n * 4);
-            memcpy(out_scores + (int64_t)qi * max_cands, sc, (size_t)n * 4);
-            if (out_diags) memcpy(out_diags + (int64_t)qi * max_cands, dg, (size_t)n * 4);
+            if (n > 0) {
+                memcpy(out_targets + (int64_t)qi * max_cands, ids, (size_t)n * 4);
+                memcpy(out_scores + (int64_t)qi * max_cands, sc, (size_t)n * 4);
+                if (out_diags) memcpy(out_diags + (int64_t)qi * max_cands, dg, (size_t)n * 4);
+            }
         }
         free(counts);
         free(touched);
