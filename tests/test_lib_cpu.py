@@ -138,3 +138,30 @@ def test_adapter_host_logic_with_oracle_stub(golden, monkeypatch):
     with pytest.raises(NotImplementedError):
         pw.compute_pairwise_alignment(g["candidates"], None, g["lengths"], 0.5,
                                       flat_sequences=g["flat"], offsets=g["offsets"], use_sw=False)
+
+
+def test_search_entry_points_reject_bad_arguments():
+    """The search entry points validate their arguments before touching the
+    device: NULL outputs, a missing index or bad sizes give
+    CK_ERR_INVALID_ARGUMENT (no GPU needed to see it)."""
+    from clustkit_gb300 import _lib
+    lib = _lib.load()
+    INVALID = 1
+    z = np.zeros(16, np.int64)
+    p = z.ctypes.data
+    # compact targets: negative count, NULL buffers
+    assert lib.ck_kmer_targets_device(0, p, -1, p, None) == INVALID
+    assert lib.ck_kmer_targets_device(0, None, 10, p, None) == INVALID
+    # Phase A with neither entries nor compact targets
+    assert lib.ck_search_phase_a_device(0, p, 4, p, p, 1, 4, 5, 20, p, None, None, p, 10, 1, 2, 5,
+                                        p, p, p, None) == INVALID
+    # C-scorer twin: Phase B needs the full entries and the database lengths
+    assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, None, p, p, 10, 1, None, 2, 2, 10,
+                                                5, 100, p, p, p, p, None) == INVALID
+    assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, p, None, p, 10, 1, None, 2, 2, 10,
+                                                5, 100, p, p, p, p, None) == INVALID
+    # no output buffers / zero cap
+    assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, p, None, p, 10, 1, p, 2, 1, 10,
+                                                0, 100, p, p, p, p, None) == INVALID
+    assert lib.ck_search_phase_a_similar_device(0, p, 4, p, p, 1, 4, None, 13, p, p, None, p, 10, 1, 2, 5,
+                                                p, p, p, None) == INVALID
