@@ -30,6 +30,7 @@ CFG_WAVE_ALL_BELOW = 3
 CFG_WAVE_ADAPTIVE = 4
 CFG_WAVE_STREAM = 5
 CFG_WAVE_ROWS = 6
+CFG_SEARCH_CLUSTER = 7
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32

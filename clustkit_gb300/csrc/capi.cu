@@ -506,6 +506,7 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) return sw_set_wave(2, value);
     if (key == CK_CFG_WAVE_STREAM) return sw_set_wave(3, value);
     if (key == CK_CFG_WAVE_ROWS) return sw_set_wave(4, value);
+    if (key == CK_CFG_SEARCH_CLUSTER) return search_set_cluster(value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -520,6 +521,7 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) { *value = sw_wave(2); return CK_OK; }
     if (key == CK_CFG_WAVE_STREAM) { *value = sw_wave(3); return CK_OK; }
     if (key == CK_CFG_WAVE_ROWS) { *value = sw_wave(4); return CK_OK; }
+    if (key == CK_CFG_SEARCH_CLUSTER) { *value = search_cluster(); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

@@ -166,6 +166,8 @@ int32_t sw_set_variant(int32_t v);
 int32_t sw_variant();
 int32_t sw_set_wave(int32_t key, int32_t v);  // key 0: min rows, 1: all-pairs batch limit, 2: adaptive, 3: stream, 4: streamed strip rows
 int32_t sw_wave(int32_t key);
+int32_t search_set_cluster(int32_t v);  // similar-k-mer walk in cluster shared memory: 0 off, 1 auto, 2 on
+int32_t search_cluster();
 int32_t sw_run_device(const SwIn &in, const SwOut &out, int64_t M, int32_t engine,
                       const int8_t *sub_host, cudaStream_t st, SwCounters *ctr,
                       bool read_counters);

@@ -186,7 +186,17 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_WAVE_ROWS       rows per strip of that streamed schedule: 0
  *                          (default) the smallest of 4/8/16 whose strips can
  *                          rotate through the lanes at the call's band width;
- *                          4, 8 or 16: at least that many */
+ *                          4, 8 or 16: at least that many
+ *   CK_CFG_SEARCH_CLUSTER  the similar-k-mer posting walk with each query's
+ *                          count row in the shared memory of a 16-CTA
+ *                          thread-block cluster (adds as distributed
+ *                          shared-memory atomics instead of L2 atomics), for
+ *                          databases up to 524,288 sequences: 0 (default)
+ *                          never, 1 for batches of 4 or more queries, 2
+ *                          always; results are identical either way (the
+ *                          cluster form measured 2.6x slower on a 64-query
+ *                          batch: remote shared-memory atomics cost more
+ *                          than the L2 atomics they replace) */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
@@ -194,6 +204,7 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 #define CK_CFG_WAVE_ADAPTIVE 4
 #define CK_CFG_WAVE_STREAM 5
 #define CK_CFG_WAVE_ROWS 6
+#define CK_CFG_SEARCH_CLUSTER 7
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

@@ -266,9 +266,12 @@ def test_oracle_similar_phase_a_matches_reference(golden):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("compact", [True, False])
-def test_similar_phase_a_and_search_match_reference(ck, golden, compact):
+@pytest.mark.parametrize("compact,cluster", [(True, 2), (False, 2), (True, 0)])
+def test_similar_phase_a_and_search_match_reference(ck, golden, compact, cluster, search_cluster):
+    """Golden similar-k-mer Phase A and search; the posting walk through
+    cluster shared memory (2) and through L2 atomics (0)."""
     from clustkit_gb300.search import DeviceDatabase, _Slot, search_batch
+    search_cluster(cluster)
     g = golden("search_golden.npz")
     db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["sim_band_width"]),
                         arena_queries=16, arena_residues=16 * 400, compact_index=compact)
@@ -295,12 +298,23 @@ def test_similar_phase_a_and_search_match_reference(ck, golden, compact):
         assert np.float32(a[2]) == np.float32(b[2]) and np.float32(a[3]) == np.float32(b[3])
 
 
+@pytest.fixture
+def search_cluster():
+    """Sets CK_CFG_SEARCH_CLUSTER for one test and restores it."""
+    from clustkit_gb300 import _lib
+    keep = _lib.get_config(_lib.CFG_SEARCH_CLUSTER)
+    yield lambda v: _lib.set_config(_lib.CFG_SEARCH_CLUSTER, int(v))
+    _lib.set_config(_lib.CFG_SEARCH_CLUSTER, keep)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("thresh", [11, 13, 15])
-def test_similar_phase_a_cap_vs_oracle(ck, thresh):
+@pytest.mark.parametrize("thresh,cluster", [(11, 1), (13, 1), (15, 1), (13, 0), (13, 2)])
+def test_similar_phase_a_cap_vs_oracle(ck, thresh, cluster, search_cluster):
     """Capped and uncapped outputs of the neighbour scoring against the oracle,
-    on a database large enough that most queries hit the cap."""
+    on a database large enough that most queries hit the cap (posting walk:
+    1 by batch size, 0 L2 atomics, 2 cluster shared memory)."""
     from clustkit_gb300.search import DeviceDatabase, _Slot
+    search_cluster(cluster)
     db_set = synth.generate_families(200, 8, median=150, lo=40, hi=400, seed=thresh)
     db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=8, arena_residues=8 * 500)
     off, ent, fr = db.index_arrays()
