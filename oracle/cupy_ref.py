@@ -1,6 +1,6 @@
 """The reference's CuPy GPU path, run without CuPy.
 
-BASELINE/TEST INFRASTRUCTURE ONLY: bench.py times it as the reference's GPU
+BASELINE AND TEST INFRASTRUCTURE ONLY: bench.py times it as the reference's GPU
 baseline beside the CPU baseline; nothing in the product calls it.
 
 The kernel is clustkit's own CuPy source (clustkit/pairwise.py:1215-1402),
