@@ -211,6 +211,25 @@ def reference_gpu_baseline(s, pairs, d_flat, d_off, d_len, stream, n_sample: int
             "source": "clustkit/pairwise.py:1215-1402 kernel + :1480-1547 batching (CuPy not installed)"}
 
 
+def hbm_check(s, pairs, kernel_s):
+    """Why the bound is integer issue and not HBM: the strip kernel's
+    algorithmic bytes (both sequences, the pair, two offsets, two lengths and
+    the 17 output bytes per pair) and its measured DRAM traffic (ncu, the
+    window spilling from L2) against the measured copy bandwidth."""
+    L = s.lengths.astype(np.int64)
+    alg = int((L[pairs[:, 0]] + L[pairs[:, 1]]).sum()) + len(pairs) * (8 + 16 + 8 + 17)
+    peak = None
+    try:
+        peak = float(json.loads((Path(__file__).resolve().parent / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+        basis = "of measured"
+    except (OSError, ValueError, KeyError):
+        peak, basis = 6800.0, "of fallback"
+    alg_gbs = alg / kernel_s / 1e9
+    dram_gbs = STRIP_DRAM_BYTES_PER_LAUNCH / kernel_s / 1e9
+    return {"algorithmic_bytes": alg, "algorithmic_gbs": alg_gbs, "dram_gbs_ncu": dram_gbs, "peak_gbs": peak,
+            "frac_algorithmic": alg_gbs / peak, "frac_dram": dram_gbs / peak, "peak_basis": basis}
+
+
 def cpu_baseline(s, pairs, target_s: float = 12.0, use_ref: bool = True):
     import oracle
     from clustkit_gb300.blosum import BLOSUM62
@@ -471,7 +490,8 @@ def run_ours(args, world, rank, local):
                      "kernel": "sw_strip_kernel", "kernel_ms": kernel_s * 1e3,
                      "gcups_kernel": gcups_kernel, "gcups_roof": p_int32 / 1e9 / OPS_PER_CELL,
                      "probe_gops": {k: v / 1e9 for k, v in rates.items()},
-                     "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL)},
+                     "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL),
+                     "hbm_check": hbm_check(s, pairs, kernel_s)},
         "cpu_baseline": cpu,
         "reference_cupy_path": gpu_ref,
         "rows_per_strip": _lib.get_config(_lib.CFG_ROWS_PER_STRIP),
