@@ -755,7 +755,30 @@ def run_search(args, n_db_fam=50000):
             c_path["cpu_baseline"] = search_cpu_baseline(db, s, qs[1500:])
             log(f"search C path on the host cores: {c_path['cpu_baseline']}")
         out["c_path_phase_b_hinted_sw"] = c_path
+    out["summary"] = search_summary(out)
     return out
+
+
+def search_summary(out):
+    """One line per scoring mode: the one-query loop, the server at its lowest
+    offered rate and its highest achieved rate (p50/p99 in ms)."""
+    modes = {"exact": out if "plain_loop" in out else None, "similar": out.get("similar_kmers_thresh13"),
+             "c_path": out.get("c_path_phase_b_hinted_sw")}
+    summ = {}
+    for name, m in modes.items():
+        if not m:
+            continue
+        sweep = m["continuous_batching"]
+        low, top = sweep[0], max(sweep, key=lambda r: r["achieved_qps"])
+        summ[name] = {"one_query_p50_ms": m["plain_loop"]["p50_ms"],
+                      "server_low_rate": {"offered_qps": low["offered_qps"], "p50_ms": low["p50_ms"],
+                                          "p99_ms": low["p99_ms"]},
+                      "server_max_achieved_qps": top["achieved_qps"],
+                      "at_max": {"offered_qps": top["offered_qps"], "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"]}}
+        if "cpu_baseline" in m:
+            summ[name]["host_cores_qps"] = m["cpu_baseline"]["value"]
+            summ[name]["server_vs_host_cores"] = top["achieved_qps"] / m["cpu_baseline"]["value"]
+    return summ
 
 
 def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
