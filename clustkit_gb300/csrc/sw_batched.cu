@@ -951,8 +951,8 @@ static int32_t g_rows_per_strip = 0;  // 0: by band width (8 up to w = 64, else 
 static int32_t g_variant = 1;
 // every pair runs one warp per pair when a call has at most this many pairs;
 // in larger calls, long pairs do: rows >= max(min rows, the adaptive bound)
-static int32_t g_wave_all_below = 24576;
-static int32_t g_wave_min_rows = 256;
+static int32_t g_wave_all_below = 40960;
+static int32_t g_wave_min_rows = 512;
 static int32_t g_wave_adaptive = 1;
 // stream the strips of consecutive pairs through a warp: 1 when the call has
 // more warp-per-pair pairs than warps, 2 always, 0 never

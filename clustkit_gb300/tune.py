@@ -38,11 +38,11 @@ KEYS = {
     "wave_adaptive": _lib.CFG_WAVE_ADAPTIVE,
 }
 
-DEFAULT = {"rows_per_strip": 0, "strip_variant": 1, "wave_min_rows": 256, "wave_all_below": 24576,
+DEFAULT = {"rows_per_strip": 0, "strip_variant": 1, "wave_min_rows": 512, "wave_all_below": 40960,
            "wave_adaptive": 1}
 
 # bin-edge candidates: (wave_min_rows, wave_adaptive); 1 << 30 = never by length
-BIN_EDGES = [(256, 1), (512, 0), (1024, 0), (2048, 0), (4096, 0), (1 << 30, 0)]
+BIN_EDGES = [(512, 1), (256, 1), (512, 0), (1024, 0), (2048, 0), (4096, 0), (1 << 30, 0)]
 TILINGS = [(r, v) for r in (8, 16, 24) for v in (0, 1, 2, 3)]
 
 _cache: dict = {}

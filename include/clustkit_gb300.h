@@ -171,10 +171,10 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs to align (the
  *                          count is taken on the device, after empty and
  *                          skipped pairs) run every pair one warp per pair
- *                          (default 24576)
+ *                          (default 40960)
  *   CK_CFG_WAVE_MIN_ROWS   in larger calls with band_width > 0, pairs with at
  *                          least this many rows (shorter side) run one warp
- *                          per pair instead of one lane per pair (default 256)
+ *                          per pair instead of one lane per pair (default 512)
  *   CK_CFG_WAVE_ADAPTIVE   1 (default): raise that row bound to where a pair's
  *                          one-lane time would pass the call's expected
  *                          kernel time, from the call's cell count; 0:
