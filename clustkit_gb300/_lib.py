@@ -68,7 +68,8 @@ SIGNATURES = {
     "ck_search_phase_a_similar_device": (_I32, [_I32, _P, _I64, _P, _P, _I32, _I32, _P, _I32, _P, _P, _P, _P,
                                                 _I32, _I32, _I32, _I32, _P, _P, _P, _P]),
     "ck_search_kmer_candidates_device": (_I32, [_I32, _P, _I64, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _P,
-                                                _I32, _I32, _P, _I32, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P]),
+                                                _I32, _I32, _P, _I32, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _I64,
+                                                _P]),
     "ck_graph_csr_device": (_I32, [_I32, _P, _P, _I64, _I64, _P, _P, _P, _P, _P]),
     "ck_connected_components_device": (_I32, [_I32, _P, _I64, _I64, _P, _P, _P, _P]),
     "ck_sketch": (_I32, [_P, _I64, _P, _P, _I64, _I32, _I32, _I32, ctypes.c_uint64, _P]),

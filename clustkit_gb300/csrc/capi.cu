@@ -30,6 +30,7 @@ struct ScratchSet {
     size_t cap[SLOT_COUNT] = {};
     int32_t *err = nullptr;
     bool frozen = false;  // buffers may be baked into a captured CUDA graph: never reallocate
+    bool dirty[SLOT_COUNT] = {};  // a kept-zero buffer whose last user may not have cleaned it
 };
 
 struct DeviceState {
@@ -149,6 +150,35 @@ void *scratch(int slot, size_t bytes, int32_t *status) {
     return s->buf[slot];
 }
 
+// A buffer that is all zero when the call's work starts, for users that
+// restore the zeros they write (so no per-call clear is needed): cleared on
+// the stream when it is (re)allocated or after scratch_mark_dirty.
+void *scratch_zeroed(int slot, size_t bytes, cudaStream_t st, int32_t *status) {
+    ScratchSet *s = current_set(status);
+    if (!s) return nullptr;
+    const void *before = s->buf[slot];
+    void *p = scratch(slot, bytes, status);
+    if (!p) return nullptr;
+    if (p != before || s->dirty[slot]) {
+        const cudaError_t e = cudaMemsetAsync(p, 0, s->cap[slot], st);
+        if (e != cudaSuccess) { *status = cuda_status(e, "cudaMemsetAsync(zeroed scratch)"); return nullptr; }
+        s->dirty[slot] = false;
+    }
+    return p;
+}
+
+void scratch_mark_dirty(int slot) {
+    int32_t status = CK_OK;
+    ScratchSet *s = current_set(&status);
+    if (s) s->dirty[slot] = true;
+}
+
+void scratch_clear_dirty(int slot) {
+    int32_t status = CK_OK;
+    ScratchSet *s = current_set(&status);
+    if (s) s->dirty[slot] = false;
+}
+
 int32_t *device_error_word(int32_t *status) {
     ScratchSet *s = current_set(status);
     return s ? s->err : nullptr;
@@ -266,6 +296,10 @@ static int32_t read_and_clear_error(cudaStream_t st) {
     }
     if (h & ERRBIT_SEQ_EXTENT) {
         set_error(CK_ERR_OUT_OF_RANGE, "sequence extent outside the flat buffer");
+        return CK_ERR_OUT_OF_RANGE;
+    }
+    if (h & ERRBIT_CAPACITY) {
+        set_error(CK_ERR_OUT_OF_RANGE, "Phase-B diagonal bins beyond the caller's bins_capacity (skipped)");
         return CK_ERR_OUT_OF_RANGE;
     }
     if (h & ERRBIT_SCHEDULE) {

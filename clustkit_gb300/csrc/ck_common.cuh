@@ -32,6 +32,7 @@ enum : int32_t {
     ERRBIT_PAIR_INDEX = 1,     // pair index outside [0, n_seqs)
     ERRBIT_SEQ_EXTENT = 2,     // offsets[i] + lengths[i] outside [0, flat_len]
     ERRBIT_SCHEDULE = 4,       // a streamed warp-per-pair strip missed its start step (internal)
+    ERRBIT_CAPACITY = 8,       // a device-side count passed the caller's bound (Phase-B bins)
 };
 
 // ---------------------------------------------------------------- SW constants
@@ -189,6 +190,9 @@ void reset_thread_status();
 
 // Per-device scratch: grow-only buffers owned by the library.
 void *scratch(int slot, size_t bytes, int32_t *status);
+void *scratch_zeroed(int slot, size_t bytes, cudaStream_t st, int32_t *status);
+void scratch_mark_dirty(int slot);
+void scratch_clear_dirty(int slot);
 int32_t *device_error_word(int32_t *status);
 const int8_t *device_sub_matrix(const int8_t *host20x20, int32_t *status);
 int current_device();
@@ -211,6 +215,7 @@ enum ScratchSlot {
     SLOT_SEARCH_CAND,
     SLOT_SEARCH_IDX,
     SLOT_SEARCH_SCORES,
+    SLOT_SEARCH_BINS,
     SLOT_SEARCH_TMP0,
     SLOT_SEARCH_TMP1,
     SLOT_SEARCH_TMP2,

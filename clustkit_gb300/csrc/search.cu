@@ -708,7 +708,7 @@ __global__ void pb_bin_count_kernel(const uint8_t *__restrict__ qflat, int64_t q
                                     const int64_t *__restrict__ kmer_entries, const int32_t *__restrict__ kmer_freqs,
                                     int32_t freq_thresh, int32_t num_db, const int32_t *__restrict__ idx_row,
                                     int32_t topk, const int64_t *__restrict__ base, int32_t width,
-                                    int32_t *__restrict__ bins, int32_t *err) {
+                                    int32_t *__restrict__ bins, int64_t bins_cap, int32_t *err) {
     const int32_t q = blockIdx.y;
     const int lane = threadIdx.x & 31;
     const int32_t L = qlen[q];
@@ -740,6 +740,7 @@ __global__ void pb_bin_count_kernel(const uint8_t *__restrict__ qflat, int64_t q
             const int64_t dbin = ((int64_t)(int32_t)(entry & 0xffffffff) - p + L) / width;
             const int64_t at = bq[i] + dbin;
             if (dbin < 0 || at >= bq[i + 1]) { atomicOr(err, ERRBIT_SEQ_EXTENT); continue; }
+            if (at >= bins_cap) { atomicOr(err, ERRBIT_CAPACITY); continue; }
             atomicAdd(&bins[at], 1);
         }
     }
@@ -747,8 +748,10 @@ __global__ void pb_bin_count_kernel(const uint8_t *__restrict__ qflat, int64_t q
 
 // A warp per selected target: its longest run (first bin on ties); kept ones
 // are written into the (cleared) count row and listed for the final selection.
+// The bins it reads are reset to zero, so a kept-zero bin buffer needs no
+// clearing before the next call.
 __global__ void pb_best_kernel(const int32_t *__restrict__ sel, const int32_t *__restrict__ sel_n, int32_t topk,
-                               const int64_t *__restrict__ base, const int32_t *__restrict__ bins,
+                               const int64_t *__restrict__ base, int32_t *__restrict__ bins, int64_t bins_cap,
                                const int32_t *__restrict__ qlen, int32_t width, int32_t min_diag_hits,
                                int32_t num_db, int32_t *__restrict__ counts, int32_t *__restrict__ hint_sel,
                                int32_t *__restrict__ cand, int32_t *__restrict__ n_cand) {
@@ -757,10 +760,12 @@ __global__ void pb_best_kernel(const int32_t *__restrict__ sel, const int32_t *_
     const int32_t n = sel_n[q];
     const int32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-        const int64_t b0 = base[(int64_t)q * topk + i], b1 = base[(int64_t)q * topk + i + 1];
+        const int64_t b0 = base[(int64_t)q * topk + i];
+        const int64_t b1 = min(base[(int64_t)q * topk + i + 1], bins_cap);
         int32_t best = 0, first = INT32_MAX;
         for (int64_t x = b0 + lane; x < b1; x += 32) {
             const int32_t c = bins[x];
+            if (c) bins[x] = 0;
             if (c > best) { best = c; first = (int32_t)(x - b0); }
         }
         const int32_t m = __reduce_max_sync(0xffffffffu, best);
@@ -1075,6 +1080,7 @@ namespace ck {
 struct CandArgs {
     PhaseAArgs a;  // Phase A part (sub_host null); top_k there = max_cands
     const int32_t *db_len; int32_t min_diag_hits, width, phase_a_topk; int32_t *out_diags;
+    int64_t bins_capacity;  // >= 0: the caller's bound on the bins (no host sync); < 0: sized from the scan
 };
 
 static int32_t candidates_impl(void *pv) {
@@ -1119,19 +1125,29 @@ static int32_t candidates_impl(void *pv) {
     void *tmp = scratch(SLOT_SORT_TEMP, tb, &status);
     if (!tmp) return status;
     CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, base, base, (int64_t)(nq * topk + 1), a.st));
-    int64_t total = 0;
-    CK_CUDA(cudaMemcpyAsync(&total, base + nq * topk, 8, cudaMemcpyDeviceToHost, a.st));
-    CK_CUDA(cudaStreamSynchronize(a.st));
-    int32_t *bins = (int32_t *)scratch(SLOT_SEARCH_TMP1, (size_t)(total > 0 ? total : 1) * 4, &status);
+    // the bins: a kept-zero buffer of the caller's bounded size (pb_best_kernel
+    // resets what it reads; bins past the bound are skipped and flagged), or
+    // sized from the scan's total read back here
+    int64_t cap = c.bins_capacity;
+    int32_t *bins = nullptr;
+    if (cap >= 0) {
+        bins = (int32_t *)scratch_zeroed(SLOT_SEARCH_BINS, (size_t)(cap > 0 ? cap : 1) * 4, a.st, &status);
+    } else {
+        CK_CUDA(cudaMemcpyAsync(&cap, base + nq * topk, 8, cudaMemcpyDeviceToHost, a.st));
+        CK_CUDA(cudaStreamSynchronize(a.st));
+        bins = (int32_t *)scratch(SLOT_SEARCH_TMP1, (size_t)(cap > 0 ? cap : 1) * 4, &status);
+        if (bins && cap > 0) CK_CUDA(cudaMemsetAsync(bins, 0, (size_t)cap * 4, a.st));
+    }
     if (!bins) return status;
-    if (total > 0) CK_CUDA(cudaMemsetAsync(bins, 0, (size_t)total * 4, a.st));
+    // from here to pb_best_kernel a failure leaves counts in the kept-zero buffer
+    if (c.bins_capacity >= 0) scratch_mark_dirty(SLOT_SEARCH_BINS);
     const int32_t npos = a.max_qlen - a.k + 1;
     if (npos > 0) {
         int bx = (npos + 7) / 8;
         if (bx > 16) bx = 16;
         pb_bin_count_kernel<<<dim3((unsigned)bx, (unsigned)a.nq), 256, 0, a.st>>>(
             a.qflat, a.qflat_len, a.qoff, a.qlen, a.k, a.alpha, a.kmer_offsets, a.kmer_entries, a.kmer_freqs,
-            a.freq_thresh, a.num_db, idx_row, topk, base, c.width, bins, err);
+            a.freq_thresh, a.num_db, idx_row, topk, base, c.width, bins, cap, err);
         CK_CUDA(cudaGetLastError());
     }
     // final cap over the kept targets: from their list, or a scan of the row
@@ -1142,9 +1158,10 @@ static int32_t candidates_impl(void *pv) {
     CK_CUDA(cudaMemsetAsync(n_cand, 0, nq * 4, a.st));
     CK_CUDA(cudaMemsetAsync(counts, 0, nq * (size_t)a.num_db * 4, a.st));
     const dim3 g2((unsigned)std::min(64, (topk + 7) / 8), (unsigned)a.nq);
-    pb_best_kernel<<<g2, 256, 0, a.st>>>(sel, sel_n, topk, base, bins, a.qlen, c.width, c.min_diag_hits, a.num_db,
-                                         counts, hint_sel, cand, n_cand);
+    pb_best_kernel<<<g2, 256, 0, a.st>>>(sel, sel_n, topk, base, bins, cap, a.qlen, c.width, c.min_diag_hits,
+                                         a.num_db, counts, hint_sel, cand, n_cand);
     CK_CUDA(cudaGetLastError());
+    if (c.bins_capacity >= 0) scratch_clear_dirty(SLOT_SEARCH_BINS);
     CK_TRY(select_rows(counts, a.nq, a.num_db, c.min_diag_hits, a.top_k, INT32_MAX, 24, cand, n_cand,
                        a.out_targets, a.out_scores, a.out_n, true, a.st));
     if (c.out_diags) {
@@ -1164,7 +1181,7 @@ extern "C" int32_t ck_search_kmer_candidates_device(
     const int64_t *d_kmer_entries, const int32_t *d_kmer_targets, const int32_t *d_kmer_freqs, int32_t freq_thresh,
     int32_t num_db, const int32_t *d_db_lengths, int32_t min_total_hits, int32_t min_diag_hits,
     int32_t diag_bin_width, int32_t max_cands, int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores,
-    int32_t *d_out_diags, int32_t *d_out_n, void *stream) {
+    int32_t *d_out_diags, int32_t *d_out_n, int64_t bins_capacity, void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
     if (nq < 0 || nq > 65535 || qflat_len < 0 || max_cands < 1 || k < 1 || alpha < 1 || num_db < 0 ||
@@ -1177,6 +1194,6 @@ extern "C" int32_t ck_search_kmer_candidates_device(
     CandArgs c{PhaseAArgs{nullptr, 0, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, k, alpha,
                           d_kmer_offsets, d_kmer_entries, d_kmer_targets, d_kmer_freqs, freq_thresh, num_db,
                           min_total_hits, max_cands, d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream},
-               d_db_lengths, min_diag_hits, diag_bin_width, phase_a_topk, d_out_diags};
+               d_db_lengths, min_diag_hits, diag_bin_width, phase_a_topk, d_out_diags, bins_capacity};
     return run_in_context(ctx, candidates_impl, &c);
 }

@@ -92,8 +92,15 @@ class Scoring:
 
     @property
     def graphable(self) -> bool:
-        """No host synchronisation in the pipeline: exact Phase A, the database band."""
-        return not self.similar and not self.diagonal and not self.use_c_sw and self.band_width is None
+        """The pipeline can run without host synchronisation (every mode but
+        the similar-k-mer one, which sizes its neighbour list on the host;
+        Phase B needs its bin bound to fit, see _Slot.bins_bound)."""
+        return not self.similar
+
+
+# largest Phase-B bin buffer a slot keeps resident (int32 counters); beyond it
+# the bins are sized per call from a device count (one host synchronisation)
+BINS_CAP = 1 << 29
 
 
 def _torch():
@@ -134,6 +141,7 @@ class DeviceDatabase:
         self.k = int(k)
         self.alpha = 20
         self.lengths_host = lengths
+        self.max_len = int(self.lengths_host[: self.n].max()) if self.n else 0
         self.slots = int(arena_slots)
         self.arena_queries = int(arena_queries)
         self.arena_residues = int(arena_residues)
@@ -234,7 +242,7 @@ class _Slot:
         # optional stage events: start, after the H2D copy, after Phase A, after SW, end
         self.stage_events = None
         self.graphs: dict = {}  # batch-size bucket -> captured pipeline
-        self.graph_min_hits = None
+        self.graph_scoring = None
         self.last_band = db.band_width  # band of the last enqueued batch
 
     def close(self):
@@ -292,6 +300,22 @@ class _Slot:
         hl[nq:n_all] = 0
         return nq, lens, tot
 
+    def bins_bound(self, nq: int, res_bytes: int, sc: Scoring) -> int:
+        """Upper bound on the Phase-B bin counters of a batch of nq queries with
+        res_bytes residues in all: each of at most phase_a_topk selected targets
+        per query has (qlen + tlen) / width + 1 bins; -1 when above BINS_CAP."""
+        db = self.db
+        topk = min(int(sc.phase_a_topk), db.n)
+        w = max(1, int(sc.diag_bin_width))
+        bound = topk * ((int(res_bytes) + nq * db.max_len) // w + nq)
+        return bound if bound <= BINS_CAP else -1
+
+    def can_capture(self, sc: Scoring) -> bool:
+        """Whether the pipeline for ``sc`` can be captured in graphs on this slot."""
+        if not sc.graphable:
+            return False
+        return not sc.diagonal or self.bins_bound(self.db.arena_queries, self.db.arena_residues, sc) >= 0
+
     def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, sc: Scoring):
         """The device pipeline of a batch of nq queries on this slot's stream:
         H2D, k-mer scoring, pair list, SW, D2H.  For exact Phase A with the
@@ -324,7 +348,7 @@ class _Slot:
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, db.d_lengths.data_ptr(), min_total_hits,
                 int(sc.min_diag_hits), int(sc.diag_bin_width), K, int(sc.phase_a_topk),
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_diags.data_ptr(),
-                self.d_n.data_ptr(), st))
+                self.d_n.data_ptr(), self.bins_bound(nq, res_bytes, sc), st))
         else:
             _lib.check(lib.ck_search_phase_a_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
@@ -352,7 +376,7 @@ class _Slot:
         self.h_mask[:M].copy_(self.d_mask[:M], non_blocking=True)
         self._mark(4)
 
-    def capture_graphs(self, min_total_hits: int, buckets=GRAPH_BUCKETS):
+    def capture_graphs(self, sc: Scoring | int, buckets=GRAPH_BUCKETS):
         """Capture the pipeline once per batch-size bucket in CUDA graphs.
 
         Every buffer is sized first by an uncaptured run of the largest
@@ -364,7 +388,10 @@ class _Slot:
         buckets = sorted({b for b in buckets if b <= db.arena_queries} | {db.arena_queries})
         self.stage_events = None
         self._fill_host([], pad_to=buckets[-1])  # every query slot an empty query
-        sc = Scoring(int(min_total_hits), 0)
+        if not isinstance(sc, Scoring):  # a minimum hit count: exact Phase A
+            sc = Scoring(int(sc), 0)
+        if not self.can_capture(sc):
+            raise ValueError("this scoring cannot run without host synchronisation on this slot")
         with torch.cuda.stream(self.stream):
             self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, sc)
         self.stream.synchronize()
@@ -380,19 +407,19 @@ class _Slot:
         with torch.cuda.stream(self.stream):
             for b in buckets:
                 self.graphs[b].replay()
-        self.graph_min_hits = int(min_total_hits)
+        self.graph_scoring = sc
         self.stream.synchronize()
 
     def launch(self, queries: list[np.ndarray], min_total_hits: int, kmer_score_thresh: int = 0, **scoring):
         """Enqueue the whole pipeline for a batch on this slot's stream
-        (``scoring``: the other fields of Scoring).  The similar-k-mer scoring
-        and Phase B size buffers on the host, so they run call by call; exact
-        Phase-A batches replay the captured graphs."""
+        (``scoring``: the other fields of Scoring).  Batches with the scoring the
+        slot's graphs were captured for replay them; others (the similar-k-mer
+        scoring sizes its neighbour list on the host) run call by call."""
         torch = _torch()
         db = self.db
         sc = Scoring(int(min_total_hits), int(kmer_score_thresh), **scoring)
         bucket = None
-        if self.graphs and sc.graphable and sc.min_total_hits == self.graph_min_hits:
+        if self.graphs and sc == self.graph_scoring:
             bucket = next((b for b in sorted(self.graphs) if b >= len(queries)), None)
         if bucket is not None:
             nq, lens, tot = self._fill_host(queries, pad_to=bucket)
@@ -659,8 +686,8 @@ class SearchServer:
         wl = max(1, min(400, db.arena_residues // self.max_batch))
         warm = [rng.integers(0, 20, wl).astype(np.uint8) for _ in range(self.max_batch)]
         for s in self.slots:
-            if use_graphs and sc.graphable:
-                s.capture_graphs(min_total_hits)
+            if use_graphs and s.can_capture(sc):
+                s.capture_graphs(sc)
             s.launch(warm, min_total_hits, self.kmer_score_thresh, **self.scoring)
             s.event.synchronize()
             s.results(1)

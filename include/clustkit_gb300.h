@@ -331,8 +331,15 @@ int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, in
  * C scorer sorts its hits instead) is needed only for Phase B.  The k-mer
  * entries are the full (target << 32 | position) ones (needed for Phase B);
  * d_kmer_targets (may be NULL) is the compact Phase-A index, which Phase A
- * then reads, as the C scorer reads its compact_entries.  Blocking (it sizes
- * the bins on the host). */
+ * then reads, as the C scorer reads its compact_entries.  Phase B keeps a
+ * diagonal-bin counter per (query, selected target, bin): sum over the
+ * selected targets of (qlen + tlen) / diag_bin_width + 1.  bins_capacity >= 0
+ * is the caller's bound on that number (for a batch: phase_a_topk x
+ * ((total query residues + nq x longest target) / diag_bin_width + nq)); the
+ * call then runs without host synchronisation, so it can be captured in a
+ * CUDA graph, and bins past the bound are skipped and reported as
+ * CK_ERR_OUT_OF_RANGE by ck_ctx_status.  bins_capacity < 0: the bins are
+ * sized from a device count read back on the host (blocking). */
 int32_t ck_search_kmer_candidates_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                          const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,
                                          int32_t max_qlen, int32_t k, int32_t alpha,
@@ -342,7 +349,8 @@ int32_t ck_search_kmer_candidates_device(int32_t ctx, const uint8_t *d_qflat, in
                                          const int32_t *d_db_lengths, int32_t min_total_hits,
                                          int32_t min_diag_hits, int32_t diag_bin_width, int32_t max_cands,
                                          int32_t phase_a_topk, int32_t *d_out_targets, int32_t *d_out_scores,
-                                         int32_t *d_out_diags, int32_t *d_out_n, void *stream);
+                                         int32_t *d_out_diags, int32_t *d_out_n, int64_t bins_capacity,
+                                         void *stream);
 
 /* ---------------------------------------------------- graph + components
  * The step after Align.  ck_graph_csr_device: the symmetric similarity graph

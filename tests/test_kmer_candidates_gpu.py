@@ -17,8 +17,16 @@ def _queries(g):
     return [g["q_flat"][o:o + L] for o, L in zip(g["q_offsets"], g["q_lengths"])]
 
 
-def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_scores=True):
-    """Per query (ids, scores, diags) from one call of the C-ABI entry point."""
+def _bins_bound(db, qs, width, topk):
+    """The caller's bound on the Phase-B bins (no host synchronisation)."""
+    return min(topk, db.n) * ((sum(len(q) for q in qs) + len(qs) * db.max_len) // width + len(qs))
+
+
+def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_scores=True, bins_capacity=-1,
+                       expect=0, ctx=None):
+    """Per query (ids, scores, diags) from one call of the C-ABI entry point
+    (``expect``: the status ck_ctx_status should report; ``ctx``: a library
+    context to reuse, else a fresh one)."""
     import torch
     from clustkit_gb300 import _lib
     lib, dev = db.lib, db.dev
@@ -32,9 +40,11 @@ def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_
     d_q, d_off, d_len = T(flat), T(offs), T(lens)
     fill = lambda n: torch.full((max(n, 1),), -7, dtype=torch.int32, device=dev)
     out_t, out_s, out_d, out_n = fill(nq * mc), fill(nq * mc), fill(nq * mc), fill(nq)
-    h = np.zeros(1, np.int32)
-    _lib.check(lib.ck_ctx_create(h.ctypes.data))
-    ctx = int(h[0])
+    own = ctx is None
+    if own:
+        h = np.zeros(1, np.int32)
+        _lib.check(lib.ck_ctx_create(h.ctypes.data))
+        ctx = int(h[0])
     st = torch.cuda.current_stream(dev).cuda_stream
     try:
         _lib.check(lib.ck_search_kmer_candidates_device(
@@ -43,10 +53,11 @@ def _device_candidates(db, qs, mth, mdh, width, mc, topk, with_diags=True, with_
             db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr, db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n,
             db.d_lengths.data_ptr(), int(mth), int(mdh), int(width), int(mc), int(topk), out_t.data_ptr(),
             out_s.data_ptr() if with_scores else None, out_d.data_ptr() if with_diags else None,
-            out_n.data_ptr(), st))
-        _lib.check(lib.ck_ctx_status(ctx, st))
+            out_n.data_ptr(), int(bins_capacity), st))
+        assert lib.ck_ctx_status(ctx, st) == expect
     finally:
-        lib.ck_ctx_destroy(ctx)
+        if own:
+            lib.ck_ctx_destroy(ctx)
     n = out_n.cpu().numpy()[:nq]
     t = out_t.cpu().numpy()[: nq * mc].reshape(nq, mc) if nq else np.zeros((0, mc), np.int32)
     s = out_s.cpu().numpy()[: nq * mc].reshape(nq, mc) if nq else t
@@ -68,7 +79,9 @@ def test_device_kmer_candidates_match_reference_c_scorer(ck, golden, compact):
     assert db.freq_thresh == int(g["freq_thresh"])
     qs = _queries(g)
     for ci, (mth, mdh, width, mc, topk) in enumerate(g["configs"]):
-        got = _device_candidates(db, qs, mth, mdh, width, mc, topk)
+        # bins sized on the host from the device count, or under the caller's bound
+        got = _device_candidates(db, qs, mth, mdh, width, mc, topk,
+                                 bins_capacity=_bins_bound(db, qs, width, topk) if compact else -1)
         for qi, (ids, sc, dg) in enumerate(got):
             assert np.array_equal(ids, g[f"c{ci}_q{qi}_targets"]), (ci, qi)
             assert np.array_equal(sc, g[f"c{ci}_q{qi}_scores"]), (ci, qi)
@@ -170,3 +183,37 @@ def test_search_with_diagonal_scoring_vs_oracle(ck, c_path):
         assert [np.float32(h.identity) for h in hits] == [np.float32(x[1]) for x in w], qi
         assert [np.float32(h.rank) for h in hits] == [np.float32(x[2]) for x in w], qi
     assert sum(len(h) for h in res) >= 14
+
+
+@pytest.mark.gpu
+def test_bounded_bins_reuse_and_overflow(ck):
+    """Phase B under the caller's bin bound keeps its buffer zero between calls
+    (repeated calls, shrinking and growing batches agree with the oracle); a
+    bound too small is reported as CK_ERR_OUT_OF_RANGE with nothing written
+    out of range, and the next call is correct again."""
+    from clustkit_gb300.search import DeviceDatabase
+    db_set = synth.generate_families(400, 8, median=250, lo=40, hi=900, seed=31)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=4, arena_residues=4 * 1000)
+    off, ent, fr = db.index_arrays()
+    rng = np.random.default_rng(4)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 12, replace=False)]
+    cfg = (2, 2, 10, 50, 500)
+
+    def check(sub_qs, got):
+        for qi, q in enumerate(sub_qs):
+            want = so.kmer_candidates(q, 5, 20, off, ent, fr, db.freq_thresh, db_set.n, *cfg)
+            for a, b in zip(got[qi], want):
+                assert np.array_equal(a, b), qi
+
+    from clustkit_gb300 import _lib
+    h = np.zeros(1, np.int32)
+    _lib.check(db.lib.ck_ctx_create(h.ctypes.data))
+    ctx = int(h[0])  # one context: its kept-zero bin buffer is reused call after call
+    try:
+        for sub_qs in (qs, qs[:3], qs[5:], qs, qs[:1]):
+            check(sub_qs, _device_candidates(db, sub_qs, *cfg, bins_capacity=_bins_bound(db, sub_qs, 10, 500),
+                                             ctx=ctx))
+        _device_candidates(db, qs, *cfg, bins_capacity=1000, expect=2, ctx=ctx)  # CK_ERR_OUT_OF_RANGE
+        check(qs, _device_candidates(db, qs, *cfg, bins_capacity=_bins_bound(db, qs, 10, 500), ctx=ctx))
+    finally:
+        db.lib.ck_ctx_destroy(ctx)

@@ -157,11 +157,11 @@ def test_search_entry_points_reject_bad_arguments():
                                         p, p, p, None) == INVALID
     # C-scorer twin: Phase B needs the full entries and the database lengths
     assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, None, p, p, 10, 1, None, 2, 2, 10,
-                                                5, 100, p, p, p, p, None) == INVALID
+                                                5, 100, p, p, p, p, -1, None) == INVALID
     assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, p, None, p, 10, 1, None, 2, 2, 10,
-                                                5, 100, p, p, p, p, None) == INVALID
+                                                5, 100, p, p, p, p, -1, None) == INVALID
     # no output buffers / zero cap
     assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, p, None, p, 10, 1, p, 2, 1, 10,
-                                                0, 100, p, p, p, p, None) == INVALID
+                                                0, 100, p, p, p, p, -1, None) == INVALID
     assert lib.ck_search_phase_a_similar_device(0, p, 4, p, p, 1, 4, None, 13, p, p, None, p, 10, 1, 2, 5,
                                                 p, p, p, None) == INVALID
