@@ -399,3 +399,37 @@ def test_reference_cupy_kernel_agrees(ck, bw):
     sims, mask = k.results(plan)
     ours = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, 0.3, pass_rule=PASS_CUPY)
     assert np.array_equal(sims, ours["sims"]) and np.array_equal(mask, ours["mask"])
+
+
+# routing configurations: (all_below, min_rows, adaptive, stream, rows)
+STRESS_ROUTES = [(40960, 512, 1, 1, 0),        # the defaults
+                 (1 << 30, 0, 0, 2, 0),         # every pair one warp, streamed
+                 (1 << 30, 0, 0, 0, 0),         # every pair one warp, per-pair schedule
+                 (0, 1 << 30, 0, 1, 0),         # every pair one lane
+                 (0, 64, 0, 2, 16)]             # split at 64 rows, streamed 16-row strips
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_randomised_routes_vs_oracle(ck, seed):
+    """Random mixes -- tiny to 3,000-residue sequences, unrelated and related
+    pairs, band widths from full (0) to 400, diagonal hints on half the pairs,
+    residue code 20 sprinkled in -- through every routing of the batched
+    engine, bit-exact against the oracle."""
+    rng = np.random.default_rng(1000 + seed)
+    dist = "pareto" if seed % 2 else "lognormal"
+    s = synth.generate_families(40, 6, median=0 if dist == "pareto" else int(rng.integers(60, 600)),
+                                lo=30 if dist == "pareto" else 1, hi=3000, seed=seed, length_dist=dist)
+    if seed % 3 == 0:  # unknown residues in some sequences
+        idx = rng.choice(len(s.flat), len(s.flat) // 200, replace=False)
+        s.flat[idx] = 20
+    pairs = synth.mixed_pairs(s, 3000, seed=seed + 7)
+    bw = int(rng.choice([0, 1, 7, 33, 100, 257, 400]))
+    L = s.lengths
+    sh = np.minimum(L[pairs[:, 0]], L[pairs[:, 1]])
+    hints = (rng.integers(-3000, 3000, len(pairs)) % (2 * sh + 5) - sh - 2).astype(np.int32)
+    hints[rng.random(len(pairs)) < 0.5] = 0
+    ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, diag_hints=hints)
+    for route in STRESS_ROUTES:
+        with wave_config(*route):
+            r = batch_sw(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62, diag_hints=hints)
+        _same(r, ref)
