@@ -738,24 +738,27 @@ def run_search(args, n_db_fam=50000):
            "band_width": db.band_width, "max_cands": 500, "top_k": 10}
     if "exact" in modes:
         exact = _measure_search_mode(db, qs, 0, (100, 1000, 3000, 10000, 20000), n_plain=300, n_stage=50,
-                                     n_batch=5)
-        out.update({"slots": exact.pop("slots"), "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)", **exact})
+                                     n_batch=5, batches_only=args.search_batches_only)
+        out.update({"slots": exact.pop("slots", None), "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)",
+                    **exact})
     if "similar" in modes:
         # clustkit's default scoring (BLOSUM62 similar 5-mers, threshold 13):
         # far more k-mer work per query, so the rates follow its batch rate
         out["similar_kmers_thresh13"] = _measure_search_mode(db, qs[3000:], 13, None, n_plain=30, n_stage=10,
-                                                             n_batch=2)
+                                                             n_batch=2, batches_only=args.search_batches_only)
     if "c_path" in modes:
         # clustkit's C path: exact 5-mers with Phase B (min_diag_hits 2, bin
         # 10, Phase-A top 10,000), SW at band 50 centred on the diagonal hints
         c_path = _measure_search_mode(db, qs[1500:], 0, None, n_plain=100, n_stage=20, n_batch=3,
                                       scoring={"min_diag_hits": 2, "diag_bin_width": 10, "phase_a_topk": 10000,
-                                               "use_c_scoring": True, "use_c_sw": True, "c_sw_band_width": 50})
-        if not args.no_cpu:
+                                               "use_c_scoring": True, "use_c_sw": True, "c_sw_band_width": 50},
+                                      batches_only=args.search_batches_only)
+        if not args.no_cpu and not args.search_batches_only:
             c_path["cpu_baseline"] = search_cpu_baseline(db, s, qs[1500:])
             log(f"search C path on the host cores: {c_path['cpu_baseline']}")
         out["c_path_phase_b_hinted_sw"] = c_path
-    out["summary"] = search_summary(out)
+    if not args.search_batches_only:
+        out["summary"] = search_summary(out)
     return out
 
 
@@ -829,9 +832,30 @@ def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
             "source": "restatements of clustkit/csrc/kmer_score.c:195-470 and sw_align.c:25-266"}
 
 
-def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scoring=None):
+def _batches_only(db, qs, thresh, n_batch, scoring):
+    """One warm-up batch, then n_batch full batches and nothing else: the
+    launch list of a profiler run then holds only batch pipelines."""
+    from clustkit_gb300.search import _Slot, search_batch
+    B = db.arena_queries
+    slot = _Slot(db, 0, 500)
+    slot.enable_stage_timing()
+    search_batch(db, qs[:B], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
+    stages = []
+    for r in range(n_batch):
+        search_batch(db, qs[B * (r + 1):B * (r + 2)], top_k=10, slot=slot, kmer_score_thresh=thresh, **scoring)
+        stages.append(slot.stage_ms())
+    slot.close()
+    med = np.median(np.array(stages), axis=0)
+    return {"batch_queries": B, "batches": n_batch,
+            "device_stage_ms_median_batch": {"h2d": float(med[0]), "phase_a": float(med[1]), "sw": float(med[2]),
+                                             "d2h": float(med[3])}}
+
+
+def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scoring=None, batches_only=False):
     from clustkit_gb300.search import SearchServer, _Slot, search_batch
     scoring = scoring or {}
+    if batches_only:
+        return _batches_only(db, qs, thresh, n_batch, scoring)
     B = db.arena_queries
     slot = _Slot(db, 0, 500)
     for q in qs[:min(20, n_plain)]:
@@ -921,6 +945,8 @@ def main():
                     help="most queries per search batch (the server's slot size)")
     ap.add_argument("--search-modes", default="exact,similar,c_path",
                     help="search leg scoring modes: exact, similar, c_path (comma list)")
+    ap.add_argument("--search-batches-only", action="store_true",
+                    help="search leg: only full batches per mode (a warm-up and a few), for profiler launch lists")
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24); 0 = library default")
     ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default")
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
