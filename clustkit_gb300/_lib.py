@@ -20,6 +20,7 @@ CK_ERR_CUDA = 3
 CK_ERR_OUT_OF_MEMORY = 4
 CK_ERR_UNSUPPORTED = 5
 CK_ERR_NO_DEVICE = 6
+CK_ERR_CAPACITY = 7
 
 PASS_CPU, PASS_NUMBA, PASS_CUPY, PASS_SCORE = 0, 1, 2, 3
 ENGINE_BATCHED, ENGINE_PLAIN = 0, 1
@@ -30,7 +31,6 @@ CFG_WAVE_ALL_BELOW = 3
 CFG_WAVE_ADAPTIVE = 4
 CFG_WAVE_STREAM = 5
 CFG_WAVE_ROWS = 6
-CFG_SEARCH_CLUSTER = 7
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -66,7 +66,7 @@ SIGNATURES = {
     "ck_ctx_freeze": (_I32, [_I32, _I32]),
     "ck_lsh_candidates_device": (_I32, [_I32, _P, _I64, _I32, _I32, _I32, _P, _P, _P, _I64, _P, _P]),
     "ck_search_phase_a_similar_device": (_I32, [_I32, _P, _I64, _P, _P, _I32, _I32, _P, _I32, _P, _P, _P, _P,
-                                                _I32, _I32, _I32, _I32, _P, _P, _P, _P]),
+                                                _I32, _I32, _I32, _I32, _P, _P, _P, _I64, _P]),
     "ck_search_kmer_candidates_device": (_I32, [_I32, _P, _I64, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _P,
                                                 _I32, _I32, _P, _I32, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _I64,
                                                 _P]),

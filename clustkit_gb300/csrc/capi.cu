@@ -167,6 +167,12 @@ void *scratch_zeroed(int slot, size_t bytes, cudaStream_t st, int32_t *status) {
     return p;
 }
 
+size_t scratch_capacity(int slot) {
+    int32_t status = CK_OK;
+    ScratchSet *s = current_set(&status);
+    return s ? s->cap[slot] : 0;
+}
+
 void scratch_mark_dirty(int slot) {
     int32_t status = CK_OK;
     ScratchSet *s = current_set(&status);
@@ -299,8 +305,12 @@ static int32_t read_and_clear_error(cudaStream_t st) {
         return CK_ERR_OUT_OF_RANGE;
     }
     if (h & ERRBIT_CAPACITY) {
-        set_error(CK_ERR_OUT_OF_RANGE, "Phase-B diagonal bins beyond the caller's bins_capacity (skipped)");
-        return CK_ERR_OUT_OF_RANGE;
+        set_error(CK_ERR_CAPACITY, "Phase-B diagonal bins beyond the caller's bins_capacity (skipped)");
+        return CK_ERR_CAPACITY;
+    }
+    if (h & ERRBIT_LIST) {
+        set_error(CK_ERR_CAPACITY, "similar k-mer neighbour list beyond the caller's list_capacity (truncated)");
+        return CK_ERR_CAPACITY;
     }
     if (h & ERRBIT_SCHEDULE) {
         set_error(CK_ERR_CUDA, "internal: a streamed warp-per-pair strip missed its start step");
@@ -540,7 +550,6 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) return sw_set_wave(2, value);
     if (key == CK_CFG_WAVE_STREAM) return sw_set_wave(3, value);
     if (key == CK_CFG_WAVE_ROWS) return sw_set_wave(4, value);
-    if (key == CK_CFG_SEARCH_CLUSTER) return search_set_cluster(value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -555,7 +564,6 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) { *value = sw_wave(2); return CK_OK; }
     if (key == CK_CFG_WAVE_STREAM) { *value = sw_wave(3); return CK_OK; }
     if (key == CK_CFG_WAVE_ROWS) { *value = sw_wave(4); return CK_OK; }
-    if (key == CK_CFG_SEARCH_CLUSTER) { *value = search_cluster(); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

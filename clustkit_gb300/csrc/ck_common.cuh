@@ -33,6 +33,7 @@ enum : int32_t {
     ERRBIT_SEQ_EXTENT = 2,     // offsets[i] + lengths[i] outside [0, flat_len]
     ERRBIT_SCHEDULE = 4,       // a streamed warp-per-pair strip missed its start step (internal)
     ERRBIT_CAPACITY = 8,       // a device-side count passed the caller's bound (Phase-B bins)
+    ERRBIT_LIST = 16,          // the similar-k-mer neighbour list passed the caller's bound
 };
 
 // ---------------------------------------------------------------- SW constants
@@ -167,8 +168,6 @@ int32_t sw_set_variant(int32_t v);
 int32_t sw_variant();
 int32_t sw_set_wave(int32_t key, int32_t v);  // key 0: min rows, 1: all-pairs batch limit, 2: adaptive, 3: stream, 4: streamed strip rows
 int32_t sw_wave(int32_t key);
-int32_t search_set_cluster(int32_t v);  // similar-k-mer walk in cluster shared memory: 0 off, 1 auto, 2 on
-int32_t search_cluster();
 int32_t sw_run_device(const SwIn &in, const SwOut &out, int64_t M, int32_t engine,
                       const int8_t *sub_host, cudaStream_t st, SwCounters *ctr,
                       bool read_counters);
@@ -191,6 +190,7 @@ void reset_thread_status();
 // Per-device scratch: grow-only buffers owned by the library.
 void *scratch(int slot, size_t bytes, int32_t *status);
 void *scratch_zeroed(int slot, size_t bytes, cudaStream_t st, int32_t *status);
+size_t scratch_capacity(int slot);  // bytes the slot holds now (0 when unallocated)
 void scratch_mark_dirty(int slot);
 void scratch_clear_dirty(int slot);
 int32_t *device_error_word(int32_t *status);

@@ -456,26 +456,61 @@ __global__ void cap_unpack_kernel(const uint64_t *__restrict__ keys, const int32
 // ----------------------------------------------------------------- similar k-mers
 // clustkit/kmer_index.py:1187-1291: with k = 5 every 5-mer whose BLOSUM62
 // column sum against a query 5-mer reaches the threshold T adds that sum to
-// each target of its posting list (frequency in (0, freq_thresh]).  Stage 1:
-// one thread per (query position, first two residues) enumerates the rest by
-// branch and bound -- the same pruning bound, max remaining row scores -- and
-// lists (5-mer value, score) per query, in a counting pass and then an
-// emitting pass; stage 2: a warp takes 32 listed 5-mers at a time and walks
-// their posting lists as one stream.
+// each target of its posting list (frequency in (0, freq_thresh]).  Stage 1
+// (nbr_list_kernel) lists the (query, 5-mer, score) triples in one pass;
+// stage 2 (nbr_walk_kernel) walks their posting lists.
+//
+// Stage 1 work items are (query position p, first two residues a0 a1), 400
+// per position.  A warp tests 32 items against clustkit's pruning bound (the
+// score so far plus the best remaining row scores must reach T); then, one
+// surviving item at a time, its lanes split the 400 (a2, a3) continuations
+// and each lane tries the 20 last residues, so no thread walks a heavy prefix
+// alone.  Hits go to the warp's shared-memory stage as 4-byte entries (value
+// | score << 22; 20^5 < 2^22, a score is at most 5 x 127); a full stage is
+// flushed to the list with one global reservation, as 8-byte entries
+// (query << 48 | score << 32 | value).  Which warp lists a triple first
+// varies from run to run; the walk's integer sums do not depend on the order.
 constexpr int32_t NB_PREFIX = 400;
+constexpr int NB_WARPS = 8;              // warps per block
+constexpr int32_t NB_STAGE = 1024;       // staged entries per warp (a round adds at most 32 x 20)
+constexpr uint32_t NB_SCORE_SHIFT = 22;
 
-// Work item (q, t): query position p = t / 400, first residues (a0, a1) =
-// (t % 400) / 20, t % 20; items are laid out q * stride + t.  The counting
-// pass writes each item's number of listed 5-mers, the emitting pass writes
-// them from the item's exclusive offset on (same enumeration order).
-template <bool EMIT>
-__global__ void nbr_enum_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len,
-                                const int64_t *__restrict__ qoff, const int32_t *__restrict__ qlen,
-                                const int8_t *__restrict__ sub, int32_t T, const int32_t *__restrict__ kmer_freqs,
-                                int32_t freq_thresh, int64_t stride, int64_t *__restrict__ item,
-                                uint64_t *__restrict__ list, int32_t *err) {
+__device__ __forceinline__ void nbr_flush(const uint32_t *stage, int32_t fill, int32_t q, uint64_t *list,
+                                          int64_t cap, unsigned long long *cursor, int lane) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(cursor, (unsigned long long)fill);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (int32_t i = lane; i < fill; i += 32) {
+        const unsigned long long at = base + (unsigned long long)i;
+        if (at < (unsigned long long)cap) {
+            const uint32_t x = stage[i];
+            list[at] = ((uint64_t)(uint32_t)q << 48) | ((uint64_t)(x >> NB_SCORE_SHIFT) << 32) |
+                       (uint64_t)(x & ((1u << NB_SCORE_SHIFT) - 1u));
+        }
+    }
+}
+
+// Lists every (query, 5-mer, score) triple; *cursor (zeroed by the caller)
+// ends as the number of triples, of which the first `cap` are written.
+__global__ void __launch_bounds__(NB_WARPS * 32)
+nbr_list_kernel(const uint8_t *__restrict__ qflat, int64_t qflat_len, const int64_t *__restrict__ qoff,
+                const int32_t *__restrict__ qlen, const int8_t *__restrict__ sub, int32_t T,
+                const int32_t *__restrict__ kmer_freqs, int32_t freq_thresh, uint64_t *__restrict__ list, int64_t cap,
+                unsigned long long *__restrict__ cursor, int32_t *err) {
+    constexpr uint32_t FULL = 0xffffffffu;
     __shared__ int32_t S[400];
     __shared__ int32_t mx[20];
+    __shared__ uint32_t stage_all[NB_WARPS][NB_STAGE];
+    const int32_t q = blockIdx.y;
+    const int32_t L = qlen[q];
+    const int64_t o = qoff[q];
+    // both exits are the same for the whole block (before its first barrier)
+    if (L < 0 || o < 0 || o + L > qflat_len) {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERRBIT_SEQ_EXTENT);
+        return;
+    }
+    const int64_t work = (int64_t)(L >= 5 ? L - 4 : 0) * NB_PREFIX;
+    if ((int64_t)blockIdx.x * NB_WARPS * 32 >= work) return;  // a shorter query than the batch's longest
     for (int i = threadIdx.x; i < 400; i += blockDim.x) S[i] = sub[i];
     __syncthreads();
     if (threadIdx.x < 20) {
@@ -484,86 +519,131 @@ __global__ void nbr_enum_kernel(const uint8_t *__restrict__ qflat, int64_t qflat
         mx[threadIdx.x] = m;
     }
     __syncthreads();
-    const int32_t q = blockIdx.y;
-    const int32_t L = qlen[q];
-    const int64_t o = qoff[q];
-    const bool bad = L < 0 || o < 0 || o + L > qflat_len;
-    if (bad && threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERRBIT_SEQ_EXTENT);
-    const uint8_t *sq = qflat + (bad ? 0 : o);
-    const int64_t work = bad ? 0 : (int64_t)(L >= 5 ? L - 4 : 0) * NB_PREFIX;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < stride;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t found = 0;
-        int64_t at = EMIT ? item[(int64_t)q * stride + t] : 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *stage = stage_all[warp];
+    const uint8_t *sq = qflat + o;
+    const int64_t step = (int64_t)gridDim.x * NB_WARPS * 32;
+    int32_t fill = 0;  // warp-uniform
+    for (int64_t t0 = ((int64_t)blockIdx.x * NB_WARPS + warp) * 32; t0 < work; t0 += step) {
+        const int64_t t = t0 + lane;
+        bool live = false;
+        int32_t p = 0, s1 = 0, v1 = 0;
         if (t < work) {
-            const int32_t p = (int32_t)(t / NB_PREFIX), pre = (int32_t)(t % NB_PREFIX);
-            const int32_t a0 = pre / 20, a1 = pre % 20;
+            p = (int32_t)(t / NB_PREFIX);
+            const int32_t pre = (int32_t)(t - (int64_t)p * NB_PREFIX);
+            const int32_t a0 = pre / 20, a1 = pre - a0 * 20;
             const int32_t q0 = sq[p], q1 = sq[p + 1], q2 = sq[p + 2], q3 = sq[p + 3], q4 = sq[p + 4];
             if (q0 < 20 && q1 < 20 && q2 < 20 && q3 < 20 && q4 < 20) {
-                const int32_t m4 = mx[q4], m34 = mx[q3] + m4, m234 = mx[q2] + m34;
+                const int32_t m234 = mx[q2] + mx[q3] + mx[q4];
                 const int32_t s0 = S[q0 * 20 + a0];
-                const int32_t s1 = s0 + S[q1 * 20 + a1];
-                if (s0 + mx[q1] + m234 >= T && s1 + m234 >= T) {
-                    const int32_t v1 = a0 * 160000 + a1 * 8000;
-                    for (int32_t a2 = 0; a2 < 20; ++a2) {
-                        const int32_t s2 = s1 + S[q2 * 20 + a2];
-                        if (s2 + m34 < T) continue;
-                        for (int32_t a3 = 0; a3 < 20; ++a3) {
-                            const int32_t s3 = s2 + S[q3 * 20 + a3];
-                            if (s3 + m4 < T) continue;
-                            const int32_t v3 = v1 + a2 * 400 + a3 * 20;
-                            for (int32_t a4 = 0; a4 < 20; ++a4) {
-                                const int32_t s4 = s3 + S[q4 * 20 + a4];
-                                if (s4 < T) continue;
-                                const int32_t v = v3 + a4;
-                                const int32_t f = kmer_freqs[v];
-                                if (f == 0 || f > freq_thresh) continue;
-                                if (EMIT) list[at++] = ((uint64_t)(uint32_t)s4 << 32) | (uint32_t)v;
-                                else ++found;
+                s1 = s0 + S[q1 * 20 + a1];
+                live = s0 + mx[q1] + m234 >= T && s1 + m234 >= T;
+                v1 = a0 * 160000 + a1 * 8000;
+            }
+        }
+        uint32_t lm = __ballot_sync(FULL, live);
+        while (lm) {
+            const int src = __ffs(lm) - 1;
+            lm &= lm - 1;
+            const int32_t P = __shfl_sync(FULL, p, src);
+            const int32_t S1 = __shfl_sync(FULL, s1, src);
+            const int32_t V1 = __shfl_sync(FULL, v1, src);
+            const int32_t q2 = sq[P + 2], q3 = sq[P + 3], q4 = sq[P + 4];
+            const int32_t m4 = mx[q4], m34 = mx[q3] + m4;
+            const int32_t *S4 = S + q4 * 20;
+            for (int32_t c0 = 0; c0 < 400; c0 += 32) {
+                const int32_t c = c0 + lane;
+                uint32_t bits = 0;
+                int32_t s3 = 0, v3 = 0;
+                if (c < 400) {
+                    const int32_t a2 = c / 20, a3 = c - a2 * 20;
+                    const int32_t s2 = S1 + S[q2 * 20 + a2];
+                    s3 = s2 + S[q3 * 20 + a3];
+                    if (s2 + m34 >= T && s3 + m4 >= T) {
+                        v3 = V1 + a2 * 400 + a3 * 20;
+#pragma unroll
+                        for (int a4 = 0; a4 < 20; ++a4) {
+                            if (s3 + S4[a4] >= T) {
+                                const int32_t f = __ldg(kmer_freqs + v3 + a4);
+                                if (f != 0 && f <= freq_thresh) bits |= 1u << a4;
                             }
                         }
                     }
                 }
+                if (!__any_sync(FULL, bits != 0)) continue;
+                const int32_t n = __popc(bits);
+                int32_t incl = n;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int32_t x = __shfl_up_sync(FULL, incl, d);
+                    if (lane >= d) incl += x;
+                }
+                const int32_t tot = __shfl_sync(FULL, incl, 31);
+                if (fill + tot > NB_STAGE) {
+                    __syncwarp();
+                    nbr_flush(stage, fill, q, list, cap, cursor, lane);
+                    __syncwarp();
+                    fill = 0;
+                }
+                int32_t at = fill + incl - n;
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    stage[at++] = (uint32_t)(v3 + b) | ((uint32_t)(s3 + S4[b]) << NB_SCORE_SHIFT);
+                }
+                fill += tot;
             }
         }
-        if (!EMIT) item[(int64_t)q * stride + t] = found;
+    }
+    if (fill > 0) {
+        __syncwarp();
+        nbr_flush(stage, fill, q, list, cap, cursor, lane);
     }
 }
 
-// A warp per listed 5-mer: its posting list's targets each gain its score.
-// Query q's entries are list[item[q * stride] .. item[(q + 1) * stride]).
 __global__ void fill_kernel(int32_t *a, int32_t n, int32_t v) {
     for (int32_t i = threadIdx.x; i < n; i += blockDim.x) a[i] = v;
 }
 
-// A warp takes 32 listed 5-mers at once: each lane loads one (value, score)
-// and its posting-list bounds -- 32 independent loads instead of 32 chains
-// -- then the warp walks the concatenated lists, lane k of each round taking
-// entry k of the stream (its list found by a binary search over the lanes'
-// exclusive prefix sums of list lengths) and adding the 5-mer's score to
-// the entry's target.
-__global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int64_t *__restrict__ item,
-                                    int64_t stride, const int64_t *__restrict__ kmer_offsets,
-                                    const int64_t *__restrict__ kmer_entries,
-                                    const int32_t *__restrict__ kmer_targets, int32_t num_db,
-                                    int32_t *__restrict__ counts, int32_t *err) {
+// Stage 2.  Block b walks triples [b * chunk, (b + 1) * chunk) of the list,
+// which the listing pass fills about one query at a time: the blocks in
+// flight then add into one or two queries' count rows, which stay in L2 (a
+// grid-stride walk, whose warps drift apart over the whole list, kept every
+// row of a 64-query batch live: 25.7 GB of DRAM writes instead of 0.24, and
+// 1.5x the time).
+// A warp takes 32 triples at once: each lane loads one and its posting-list
+// bounds -- 32 independent loads instead of 32 chains -- then the warp walks
+// the concatenated lists, lane k of each round taking entry k of the stream
+// (its list found by a binary search over the lanes' exclusive prefix sums
+// of list lengths) and adding the triple's score to the entry's target in
+// the triple's query row.  A list longer than `cap` (the listing pass
+// counted more triples than it could write) is reported.
+__global__ void nbr_walk_kernel(const uint64_t *__restrict__ list, const unsigned long long *__restrict__ cursor,
+                                int64_t cap, int64_t chunk, int32_t nq, const int64_t *__restrict__ kmer_offsets,
+                                const int64_t *__restrict__ kmer_entries, const int32_t *__restrict__ kmer_targets,
+                                int32_t num_db, int32_t *__restrict__ counts, int32_t *err) {
     constexpr uint32_t FULL = 0xffffffffu;
-    const int32_t q = blockIdx.y;
     const int lane = threadIdx.x & 31;
-    const int64_t e0 = item[(int64_t)q * stride], e1 = item[(int64_t)(q + 1) * stride];
-    int32_t *c = counts + (int64_t)q * num_db;
-    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    for (int64_t base = e0 + wid * 32; base < e1; base += warps * 32) {
+    const unsigned long long listed = *cursor;
+    if (listed > (unsigned long long)cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERRBIT_LIST);
+    const int64_t n = (int64_t)(listed < (unsigned long long)cap ? listed : (unsigned long long)cap);
+    const int64_t c0 = (int64_t)blockIdx.x * chunk;
+    const int64_t c1 = c0 + chunk < n ? c0 + chunk : n;
+    for (int64_t base = c0 + (threadIdx.x >> 5) * 32; base < c1; base += blockDim.x) {
         const int64_t e = base + lane;
         int64_t b = 0;
-        int32_t len = 0, w = 0;
-        if (e < e1) {
+        int32_t len = 0, w = 0, qq = 0;
+        if (e < c1) {
             const uint64_t x = list[e];
             const int32_t v = (int32_t)(x & 0xffffffffu);
-            w = (int32_t)(x >> 32);
-            b = kmer_offsets[v];
-            len = (int32_t)(kmer_offsets[v + 1] - b);
+            w = (int32_t)((x >> 32) & 0xffffu);
+            qq = (int32_t)(x >> 48);
+            if (qq < nq) {
+                b = kmer_offsets[v];
+                len = (int32_t)(kmer_offsets[v + 1] - b);
+            } else {
+                atomicOr(err, ERRBIT_PAIR_INDEX);
+            }
         }
         int32_t incl = len;
 #pragma unroll
@@ -587,6 +667,7 @@ __global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int
             }
             const int64_t h = __shfl_sync(FULL, b, o) + (k - __shfl_sync(FULL, excl, o));
             const int32_t wo = __shfl_sync(FULL, w, o);
+            const int32_t qo = __shfl_sync(FULL, qq, o);
             if (k < total) {
                 const int32_t t = entry_target(kmer_entries, kmer_targets, h);
                 if (t < 0 || t >= num_db) {
@@ -595,86 +676,11 @@ __global__ void nbr_postings_kernel(const uint64_t *__restrict__ list, const int
                     // no candidate list here (most of the database crosses
                     // min_hits in this mode; the select scans the row): the
                     // add's result is unused
-                    atomicAdd(&c[t], wo);
+                    atomicAdd(&counts[(int64_t)qo * num_db + t], wo);
                 }
             }
         }
     }
-}
-
-// The same walk with the query's count row in the distributed shared memory
-// of a thread-block cluster instead of global memory: one cluster per query,
-// CTA r of the cluster holding targets [r * chunk, (r + 1) * chunk) (chunk a
-// power of two, so a target's owner is a shift), every warp of the cluster
-// taking 32 listed 5-mers at a time, and each posting's add an atomic on the
-// owning CTA's shared memory rather than on L2.  The row is zeroed and
-// written back by its owners, with a cluster barrier on each side of the walk
-// (every thread reaches both: no early exit).
-__global__ void __launch_bounds__(1024, 1)
-nbr_cluster_kernel(const uint64_t *__restrict__ list, const int64_t *__restrict__ item, int64_t stride,
-                   const int64_t *__restrict__ kmer_offsets, const int64_t *__restrict__ kmer_entries,
-                   const int32_t *__restrict__ kmer_targets, int32_t num_db, int32_t chunk_shift,
-                   int32_t *__restrict__ counts, int32_t *err) {
-    namespace cg = cooperative_groups;
-    constexpr uint32_t FULL = 0xffffffffu;
-    extern __shared__ int32_t s_row[];
-    cg::cluster_group cluster = cg::this_cluster();
-    const int32_t rank = (int32_t)cluster.block_rank();
-    const int32_t cs = (int32_t)cluster.num_blocks();
-    const int32_t chunk = 1 << chunk_shift;
-    const int32_t q = blockIdx.y;
-    for (int32_t i = threadIdx.x; i < chunk; i += blockDim.x) s_row[i] = 0;
-    cluster.sync();
-    const int lane = threadIdx.x & 31;
-    const int64_t e0 = item[(int64_t)q * stride], e1 = item[(int64_t)(q + 1) * stride];
-    const int64_t wpc = blockDim.x >> 5;
-    const int64_t nw = (int64_t)cs * wpc;
-    for (int64_t base = e0 + ((int64_t)rank * wpc + (threadIdx.x >> 5)) * 32; base < e1; base += nw * 32) {
-        const int64_t e = base + lane;
-        int64_t b = 0;
-        int32_t len = 0, w = 0;
-        if (e < e1) {
-            const uint64_t x = list[e];
-            const int32_t v = (int32_t)(x & 0xffffffffu);
-            w = (int32_t)(x >> 32);
-            b = kmer_offsets[v];
-            len = (int32_t)(kmer_offsets[v + 1] - b);
-        }
-        int32_t incl = len;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int32_t t = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += t;
-        }
-        const int32_t excl = incl - len;
-        const int32_t total = __shfl_sync(FULL, incl, 31);
-        for (int32_t k0 = 0; k0 < total; k0 += 32) {
-            const int32_t k = k0 + lane;
-            int32_t o = 0;
-#pragma unroll
-            for (int step = 16; step; step >>= 1) {
-                const int32_t cand = o + step;
-                if (__shfl_sync(FULL, excl, cand) <= k) o = cand;
-            }
-            const int64_t h = __shfl_sync(FULL, b, o) + (k - __shfl_sync(FULL, excl, o));
-            const int32_t wo = __shfl_sync(FULL, w, o);
-            if (k < total) {
-                const int32_t t = entry_target(kmer_entries, kmer_targets, h);
-                const int32_t owner = t >> chunk_shift;
-                if (t < 0 || t >= num_db || owner >= cs) {
-                    atomicOr(err, ERRBIT_PAIR_INDEX);
-                } else {
-                    int32_t *row = cluster.map_shared_rank(s_row, (unsigned)owner);
-                    atomicAdd(row + (t & (chunk - 1)), wo);
-                }
-            }
-        }
-    }
-    cluster.sync();
-    const int64_t t0 = (int64_t)rank << chunk_shift;
-    const int32_t n = (int32_t)std::min<int64_t>(chunk, (int64_t)num_db - t0);
-    int32_t *c = counts + (int64_t)q * num_db + t0;
-    for (int32_t i = threadIdx.x; i < n; i += blockDim.x) c[i] = s_row[i];
 }
 
 // ----------------------------------------------------------------- Phase B
@@ -798,6 +804,7 @@ struct PhaseAArgs {
     const int32_t *kmer_freqs; int32_t freq_thresh; int32_t num_db; int32_t min_hits; int32_t top_k;
     int32_t *out_targets; int32_t *out_scores; int32_t *out_n; cudaStream_t st;
     bool ordered = true;  // capped rows in (score desc, id asc) order, not only the set
+    int64_t list_capacity = -1;  // similar k-mers: caller's bound on listed triples, < 0 sized here
 };
 
 // The select, then the order of rows capped above CAND_CAP.  `ordered`:
@@ -844,68 +851,6 @@ static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, in
     return CK_OK;
 }
 
-// Similar-k-mer posting walk through cluster shared memory: 0 never (the
-// default: measured 2.6x slower than the L2-atomic walk on a 64-query batch of
-// the 500k-sequence database, 95 against 36 ms, and 3-5x on one query), 1 for
-// batches of at least CLUSTER_MIN_QUERIES queries, 2 always (when the row fits).
-static int32_t g_search_cluster = 0;
-constexpr int32_t CLUSTER_MIN_QUERIES = 4;
-constexpr int32_t CLUSTER_MAX_SHIFT = 15;  // 32,768 int32 counters (128 KB) per CTA
-
-// Launches nbr_cluster_kernel when the setting, the batch and the database
-// size allow it and the device can co-schedule such a cluster; false (with
-// *status untouched) when the caller should take the global-atomic walk.
-static bool launch_nbr_cluster(const uint64_t *list, const int64_t *item, int64_t stride, const PhaseAArgs &a,
-                               int32_t *counts, int32_t *err, int32_t *status) {
-    if (g_search_cluster == 0 || (g_search_cluster == 1 && a.nq < CLUSTER_MIN_QUERIES) || a.num_db < 1) return false;
-    // 16 CTAs (the non-portable maximum) per query, each owning a power-of-two slice
-    constexpr int32_t CS = 16;
-    int32_t shift = 10;
-    while (shift < CLUSTER_MAX_SHIFT && ((int64_t)CS << shift) < a.num_db) ++shift;
-    if (((int64_t)CS << shift) < a.num_db) return false;
-    const size_t smem = (size_t)4 << shift;
-    auto kern = nbr_cluster_kernel;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)CS, (unsigned)a.nq, 1);
-    cfg.blockDim = dim3(1024, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = a.st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CS;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int n_clusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&n_clusters, kern, &cfg) != cudaSuccess || n_clusters < 1) {
-        cudaGetLastError();
-        return false;
-    }
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, list, item, stride, a.kmer_offsets, a.kmer_entries,
-                                             a.kmer_targets, a.num_db, shift, counts, err);
-    if (e != cudaSuccess) {
-        *status = cuda_status(e, "nbr_cluster_kernel launch");
-        return false;
-    }
-    return true;
-}
-
-int32_t search_set_cluster(int32_t v) {
-    if (v < 0 || v > 2) {
-        set_error(CK_ERR_INVALID_ARGUMENT, "search cluster setting must be 0, 1 or 2");
-        return CK_ERR_INVALID_ARGUMENT;
-    }
-    g_search_cluster = v;
-    return CK_OK;
-}
-int32_t search_cluster() { return g_search_cluster; }
-
 static int32_t phase_a_impl(void *pv) {
     PhaseAArgs &a = *(PhaseAArgs *)pv;
     int32_t status = CK_OK;
@@ -940,45 +885,58 @@ static int32_t phase_a_impl(void *pv) {
         const int8_t *d_sub = device_sub_matrix(a.sub_host, &status);
         if (!d_sub) return status;
         if (npos > 0) {
-            // items: nq x stride, plus one trailing entry that ends the last query's range
-            const int64_t stride = (int64_t)npos * NB_PREFIX;
-            const int64_t n_items = (int64_t)a.nq * stride + 1;
-            int64_t *item = (int64_t *)scratch(SLOT_SEARCH_TMP0, (size_t)n_items * 8, &status);
-            if (!item) return status;
-            // enough blocks per query that a small batch still spreads over every SM
-            int bx = (int)((stride + 255) / 256);
-            const int bx_cap = std::max(64, 8 * sm_count() / std::max(1, (int)a.nq));
-            if (bx > bx_cap) bx = bx_cap;
-            const dim3 grid((unsigned)bx, (unsigned)a.nq);
-            nbr_enum_kernel<false><<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, d_sub,
-                                                            a.score_thresh, a.kmer_freqs, a.freq_thresh, stride,
-                                                            item, nullptr, err);
-            CK_CUDA(cudaGetLastError());
-            CK_CUDA(cudaMemsetAsync(item + n_items - 1, 0, 8, a.st));
-            size_t tb = 0;
-            CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb, item, item, n_items, a.st));
-            void *tmp = scratch(SLOT_SORT_TEMP, tb, &status);
-            if (!tmp) return status;
-            CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, item, item, n_items, a.st));
-            int64_t total = 0;
-            CK_CUDA(cudaMemcpyAsync(&total, item + n_items - 1, 8, cudaMemcpyDeviceToHost, a.st));
-            CK_CUDA(cudaStreamSynchronize(a.st));
-            uint64_t *list = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)(total > 0 ? total : 1) * 8, &status);
+            unsigned long long *cursor = (unsigned long long *)scratch(SLOT_SEARCH_TMP0, 8, &status);
+            if (!cursor) return status;
+            const bool bounded = a.list_capacity >= 0;
+            // unbounded: the list scratch as it stands (at least 1 Mi triples); a
+            // call that lists more grows it to the count and lists again
+            int64_t cap = bounded ? a.list_capacity
+                                  : std::max<int64_t>((int64_t)(scratch_capacity(SLOT_SEARCH_TMP1) / 8), 1 << 20);
+            uint64_t *list = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)std::max<int64_t>(cap, 1) * 8, &status);
             if (!list) return status;
-            nbr_enum_kernel<true><<<grid, 256, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, d_sub,
-                                                           a.score_thresh, a.kmer_freqs, a.freq_thresh, stride,
-                                                           item, list, err);
-            CK_CUDA(cudaGetLastError());
-            if (!launch_nbr_cluster(list, item, stride, a, counts, err, &status)) {
-                if (status != CK_OK) return status;
-                int by = (int)((total / (a.nq > 0 ? a.nq : 1) + 255) / 256);  // 8 warps x 32 5-mers
-                const int by_cap = std::max(4 * sm_count(), 16 * sm_count() / std::max(1, (int)a.nq));
-                if (by > by_cap) by = by_cap;
-                if (by < 1) by = 1;
-                nbr_postings_kernel<<<dim3((unsigned)by, (unsigned)a.nq), 256, 0, a.st>>>(
-                    list, item, stride, a.kmer_offsets, a.kmer_entries, a.kmer_targets, a.num_db, counts, err);
+            if (!bounded) cap = (int64_t)(scratch_capacity(SLOT_SEARCH_TMP1) / 8);
+            // one block per 256 items of the longest query: blocks start in
+            // query order, so the list fills (and the walk later runs) about
+            // one query at a time -- the walk's count-row atomics then hit L2
+            // (interleaving ten queries' rows cost it 1.5x)
+            const int64_t groups = ((int64_t)npos * NB_PREFIX + NB_WARPS * 32 - 1) / (NB_WARPS * 32);
+            const dim3 grid((unsigned)groups, (unsigned)a.nq);
+            int64_t listed = -1;
+            for (int pass = 0; pass < 2; ++pass) {
+                CK_CUDA(cudaMemsetAsync(cursor, 0, 8, a.st));
+                nbr_list_kernel<<<grid, NB_WARPS * 32, 0, a.st>>>(a.qflat, a.qflat_len, a.qoff, a.qlen, d_sub,
+                                                                   a.score_thresh, a.kmer_freqs, a.freq_thresh, list,
+                                                                   cap, cursor, err);
                 CK_CUDA(cudaGetLastError());
+                if (bounded) break;
+                unsigned long long h = 0;
+                CK_CUDA(cudaMemcpyAsync(&h, cursor, 8, cudaMemcpyDeviceToHost, a.st));
+                CK_CUDA(cudaStreamSynchronize(a.st));
+                listed = (int64_t)h;
+                if (listed <= cap) break;
+                // a quarter over the count, so that the next, slightly larger
+                // batch does not list twice as well
+                list = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)(listed + listed / 4) * 8, &status);
+                if (!list) return status;
+                cap = (int64_t)(scratch_capacity(SLOT_SEARCH_TMP1) / 8);
             }
+            // the walk's grid: one block per chunk of the count when it is
+            // known, else of the bound (blocks past the count exit at once).
+            // A chunk (a multiple of 256, at most 2048 triples) leaves at
+            // least two blocks per resident slot, and the resident blocks
+            // within about two queries' triples
+            const int64_t n_walk = listed >= 0 ? listed : cap;
+            const int64_t resident = (int64_t)8 * sm_count();
+            int64_t chunk = std::min<int64_t>(2 * n_walk / ((int64_t)a.nq * resident), n_walk / (2 * resident));
+            chunk = std::min<int64_t>(2048, std::max<int64_t>(256, chunk / 256 * 256));
+            const int64_t bw = std::max<int64_t>(1, (n_walk + chunk - 1) / chunk);
+            if (bw > INT32_MAX) {
+                set_error(CK_ERR_UNSUPPORTED, "similar k-mer phase A: neighbour list too long");
+                return CK_ERR_UNSUPPORTED;
+            }
+            nbr_walk_kernel<<<(unsigned)bw, 256, 0, a.st>>>(list, cursor, cap, chunk, a.nq, a.kmer_offsets,
+                                                            a.kmer_entries, a.kmer_targets, a.num_db, counts, err);
+            CK_CUDA(cudaGetLastError());
             // the select scans the whole count row (no candidate list in this mode)
             fill_kernel<<<1, 256, 0, a.st>>>(n_cand, a.nq, CAND_CAP + 1);
             CK_CUDA(cudaGetLastError());
@@ -1060,7 +1018,8 @@ extern "C" int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *
                                                     const int64_t *d_kmer_entries, const int32_t *d_kmer_targets,
                                                     const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
                                                     int32_t min_total_hits, int32_t top_k, int32_t *d_out_targets,
-                                                    int32_t *d_out_scores, int32_t *d_out_n, void *stream) {
+                                                    int32_t *d_out_scores, int32_t *d_out_n, int64_t list_capacity,
+                                                    void *stream) {
     std::lock_guard<std::mutex> lock(library_mutex());
     reset_thread_status();
     if (nq < 0 || nq > 65535 || qflat_len < 0 || top_k < 1 || num_db < 0 || !sub_matrix_host ||
@@ -1072,6 +1031,7 @@ extern "C" int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *
     PhaseAArgs a{sub_matrix_host, kmer_score_thresh, d_qflat, qflat_len, d_qoffsets, d_qlengths, nq, max_qlen, 5,
                  20, d_kmer_offsets, d_kmer_entries, d_kmer_targets, d_kmer_freqs, freq_thresh, num_db,
                  min_total_hits, top_k, d_out_targets, d_out_scores, d_out_n, (cudaStream_t)stream};
+    a.list_capacity = list_capacity;
     return run_in_context(ctx, phase_a_impl, &a);
 }
 

@@ -340,7 +340,7 @@ class _Slot:
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen, _SUB.ctypes.data,
                 int(sc.kmer_score_thresh), db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
                 db.kmer_targets_ptr, db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
-                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
+                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), -1, st))
         elif sc.diagonal:  # the C scorer's Phase A + Phase B, with diagonal hints
             _lib.check(lib.ck_search_kmer_candidates_device(
                 self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,

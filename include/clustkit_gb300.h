@@ -39,6 +39,11 @@ extern "C" {
 #define CK_ERR_OUT_OF_MEMORY     4
 #define CK_ERR_UNSUPPORTED       5  /* parameter outside what the kernels implement   */
 #define CK_ERR_NO_DEVICE         6
+#define CK_ERR_CAPACITY          7  /* a caller-bounded device buffer (Phase-B bins,
+                                       neighbour list) was too small: the call's
+                                       results are incomplete; run it again with
+                                       a larger bound (reported at the next
+                                       status check of the context)            */
 
 /* --------------------------------------------------- pass / fail rules
  * clustkit decides pass/fail differently on each of its three SW paths; the
@@ -137,9 +142,9 @@ int32_t ck_sw_batch_device_noalloc(const int32_t *d_pairs, int64_t M, const uint
                                    int32_t *d_scores, int32_t *d_matches, int32_t *d_shorter,
                                    uint8_t *d_mask, void *stream);
 
-/* Synchronises `stream`, returns CK_OK or CK_ERR_OUT_OF_RANGE for the GPU
- * checks of the ck_*_device calls since the previous ck_sw_status_device on
- * this device, and clears the flag. */
+/* Synchronises `stream`, returns CK_OK, CK_ERR_OUT_OF_RANGE or
+ * CK_ERR_CAPACITY for the GPU checks of the ck_*_device calls since the
+ * previous ck_sw_status_device on this device, and clears the flag. */
 int32_t ck_sw_status_device(void *stream);
 
 /* Work counters of the last ck_sw_batch / ck_sw_batch_device call on this
@@ -187,16 +192,9 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *                          (default) the smallest of 4/8/16 whose strips can
  *                          rotate through the lanes at the call's band width;
  *                          4, 8 or 16: at least that many
- *   CK_CFG_SEARCH_CLUSTER  the similar-k-mer posting walk with each query's
- *                          count row in the shared memory of a 16-CTA
- *                          thread-block cluster (adds as distributed
- *                          shared-memory atomics instead of L2 atomics), for
- *                          databases up to 524,288 sequences: 0 (default)
- *                          never, 1 for batches of 4 or more queries, 2
- *                          always; results are identical either way (the
- *                          cluster form measured 2.6x slower on a 64-query
- *                          batch: remote shared-memory atomics cost more
- *                          than the L2 atomics they replace) */
+ *                          (key 7, a cluster-shared-memory form of the
+ *                          similar-k-mer posting walk, is retired: it
+ *                          measured 2.6x slower than the L2-atomic walk) */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
@@ -204,7 +202,6 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 #define CK_CFG_WAVE_ADAPTIVE 4
 #define CK_CFG_WAVE_STREAM 5
 #define CK_CFG_WAVE_ROWS 6
-#define CK_CFG_SEARCH_CLUSTER 7
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 
@@ -245,8 +242,9 @@ int32_t ck_ctx_destroy(int32_t handle);
  * calls on this context (size them with one uncaptured call of the largest
  * shape first). */
 int32_t ck_ctx_freeze(int32_t handle, int32_t frozen);
-/* Synchronises `stream` and returns CK_OK or CK_ERR_OUT_OF_RANGE for GPU-side
- * input checks of the context's calls since its last status read. */
+/* Synchronises `stream` and returns CK_OK, CK_ERR_OUT_OF_RANGE (GPU-side
+ * input checks) or CK_ERR_CAPACITY (a caller-bounded buffer too small) for
+ * the context's calls since its last status read. */
 int32_t ck_ctx_status(int32_t handle, void *stream);
 /* ck_sw_batch_device with the scratch of context `ctx`. */
 int32_t ck_sw_batch_device_ctx(int32_t ctx, const int32_t *d_pairs, int64_t M, const uint8_t *d_flat,
@@ -302,8 +300,15 @@ int32_t ck_lsh_candidates_device(int32_t ctx, const uint64_t *d_sketches, int64_
  * is >= kmer_score_thresh adds that score to each target of its posting list
  * (k-mers with frequency 0 or above freq_thresh skipped); sums are int32, not
  * saturated; survivors and cap as above.  d_kmer_targets (may be NULL) as
- * in ck_search_phase_a_device.  Blocking (it sizes its neighbour list on the
- * host). */
+ * in ck_search_phase_a_device.
+ * The (query, 5-mer, score) triples are listed once into a device list that
+ * the posting walk then reads.  list_capacity < 0: the library sizes that
+ * list from its scratch, reads the count on the host (blocking) and, when it
+ * was too small, grows it and lists again.  list_capacity >= 0: at most that
+ * many triples (8 bytes each in the context's scratch), no host
+ * synchronisation (the call can be captured in a CUDA graph); a call that
+ * lists more walks only the first list_capacity and the next status check
+ * reports CK_ERR_CAPACITY. */
 int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                          const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,
                                          int32_t max_qlen, const int8_t *sub_matrix_host,
@@ -311,7 +316,8 @@ int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, in
                                          const int64_t *d_kmer_entries, const int32_t *d_kmer_targets,
                                          const int32_t *d_kmer_freqs, int32_t freq_thresh, int32_t num_db,
                                          int32_t min_total_hits, int32_t top_k, int32_t *d_out_targets,
-                                         int32_t *d_out_scores, int32_t *d_out_n, void *stream);
+                                         int32_t *d_out_scores, int32_t *d_out_n, int64_t list_capacity,
+                                         void *stream);
 
 /* The k-mer scorer of clustkit's C/OpenMP search path (batch_score_queries_c,
  * clustkit/csrc/kmer_score.c:420-470, bound at clustkit/kmer_index.py:
@@ -338,7 +344,7 @@ int32_t ck_search_phase_a_similar_device(int32_t ctx, const uint8_t *d_qflat, in
  * ((total query residues + nq x longest target) / diag_bin_width + nq)); the
  * call then runs without host synchronisation, so it can be captured in a
  * CUDA graph, and bins past the bound are skipped and reported as
- * CK_ERR_OUT_OF_RANGE by ck_ctx_status.  bins_capacity < 0: the bins are
+ * CK_ERR_CAPACITY by ck_ctx_status.  bins_capacity < 0: the bins are
  * sized from a device count read back on the host (blocking). */
 int32_t ck_search_kmer_candidates_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,
                                          const int64_t *d_qoffsets, const int32_t *d_qlengths, int32_t nq,

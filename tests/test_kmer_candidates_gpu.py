@@ -189,7 +189,7 @@ def test_search_with_diagonal_scoring_vs_oracle(ck, c_path):
 def test_bounded_bins_reuse_and_overflow(ck):
     """Phase B under the caller's bin bound keeps its buffer zero between calls
     (repeated calls, shrinking and growing batches agree with the oracle); a
-    bound too small is reported as CK_ERR_OUT_OF_RANGE with nothing written
+    bound too small is reported as CK_ERR_CAPACITY with nothing written
     out of range, and the next call is correct again."""
     from clustkit_gb300.search import DeviceDatabase
     db_set = synth.generate_families(400, 8, median=250, lo=40, hi=900, seed=31)
@@ -213,7 +213,7 @@ def test_bounded_bins_reuse_and_overflow(ck):
         for sub_qs in (qs, qs[:3], qs[5:], qs, qs[:1]):
             check(sub_qs, _device_candidates(db, sub_qs, *cfg, bins_capacity=_bins_bound(db, sub_qs, 10, 500),
                                              ctx=ctx))
-        _device_candidates(db, qs, *cfg, bins_capacity=1000, expect=2, ctx=ctx)  # CK_ERR_OUT_OF_RANGE
+        _device_candidates(db, qs, *cfg, bins_capacity=1000, expect=_lib.CK_ERR_CAPACITY, ctx=ctx)
         check(qs, _device_candidates(db, qs, *cfg, bins_capacity=_bins_bound(db, qs, 10, 500), ctx=ctx))
     finally:
         db.lib.ck_ctx_destroy(ctx)

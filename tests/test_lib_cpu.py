@@ -164,4 +164,4 @@ def test_search_entry_points_reject_bad_arguments():
     assert lib.ck_search_kmer_candidates_device(0, p, 4, p, p, 1, 4, 5, 20, p, p, None, p, 10, 1, p, 2, 1, 10,
                                                 0, 100, p, p, p, p, -1, None) == INVALID
     assert lib.ck_search_phase_a_similar_device(0, p, 4, p, p, 1, 4, None, 13, p, p, None, p, 10, 1, 2, 5,
-                                                p, p, p, None) == INVALID
+                                                p, p, p, -1, None) == INVALID

@@ -266,12 +266,10 @@ def test_oracle_similar_phase_a_matches_reference(golden):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("compact,cluster", [(True, 2), (False, 2), (True, 0)])
-def test_similar_phase_a_and_search_match_reference(ck, golden, compact, cluster, search_cluster):
-    """Golden similar-k-mer Phase A and search; the posting walk through
-    cluster shared memory (2) and through L2 atomics (0)."""
+@pytest.mark.parametrize("compact", [True, False])
+def test_similar_phase_a_and_search_match_reference(ck, golden, compact):
+    """Golden similar-k-mer Phase A and search (compact and full index)."""
     from clustkit_gb300.search import DeviceDatabase, _Slot, search_batch
-    search_cluster(cluster)
     g = golden("search_golden.npz")
     db = DeviceDatabase(g["db_flat"], g["db_offsets"], g["db_lengths"], band_width=int(g["sim_band_width"]),
                         arena_queries=16, arena_residues=16 * 400, compact_index=compact)
@@ -298,23 +296,12 @@ def test_similar_phase_a_and_search_match_reference(ck, golden, compact, cluster
         assert np.float32(a[2]) == np.float32(b[2]) and np.float32(a[3]) == np.float32(b[3])
 
 
-@pytest.fixture
-def search_cluster():
-    """Sets CK_CFG_SEARCH_CLUSTER for one test and restores it."""
-    from clustkit_gb300 import _lib
-    keep = _lib.get_config(_lib.CFG_SEARCH_CLUSTER)
-    yield lambda v: _lib.set_config(_lib.CFG_SEARCH_CLUSTER, int(v))
-    _lib.set_config(_lib.CFG_SEARCH_CLUSTER, keep)
-
-
 @pytest.mark.gpu
-@pytest.mark.parametrize("thresh,cluster", [(11, 1), (13, 1), (15, 1), (13, 0), (13, 2)])
-def test_similar_phase_a_cap_vs_oracle(ck, thresh, cluster, search_cluster):
+@pytest.mark.parametrize("thresh", [11, 13, 15])
+def test_similar_phase_a_cap_vs_oracle(ck, thresh):
     """Capped and uncapped outputs of the neighbour scoring against the oracle,
-    on a database large enough that most queries hit the cap (posting walk:
-    1 by batch size, 0 L2 atomics, 2 cluster shared memory)."""
+    on a database large enough that most queries hit the cap."""
     from clustkit_gb300.search import DeviceDatabase, _Slot
-    search_cluster(cluster)
     db_set = synth.generate_families(200, 8, median=150, lo=40, hi=400, seed=thresh)
     db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=8, arena_residues=8 * 500)
     off, ent, fr = db.index_arrays()
@@ -334,6 +321,72 @@ def test_similar_phase_a_cap_vs_oracle(ck, thresh, cluster, search_cluster):
             slot.results(3)
         finally:
             slot.close()
+
+
+def _similar_call(db, qs, top_k, list_capacity, ctx, expect=0, thresh=13):
+    """(ids, scores) rows from one ck_search_phase_a_similar_device call in
+    library context ``ctx`` (``expect``: the status ck_ctx_status reports)."""
+    import torch
+    from clustkit_gb300 import _lib
+    from clustkit_gb300.search import _SUB
+    lib, dev = db.lib, db.dev
+    nq = len(qs)
+    lens = np.array([len(q) for q in qs], np.int32)
+    offs = np.concatenate([[0], np.cumsum(lens[:-1])]).astype(np.int64)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_q, d_off, d_len = T(np.concatenate(qs).astype(np.uint8)), T(offs), T(lens)
+    out_t = torch.full((nq * top_k,), -7, dtype=torch.int32, device=dev)
+    out_s = torch.full_like(out_t, -7)
+    out_n = torch.full((nq,), -7, dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(lib.ck_search_phase_a_similar_device(
+        ctx, d_q.data_ptr(), int(lens.sum()), d_off.data_ptr(), d_len.data_ptr(), nq, int(lens.max()),
+        _SUB.ctypes.data, thresh, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr,
+        db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, 2, top_k, out_t.data_ptr(), out_s.data_ptr(),
+        out_n.data_ptr(), int(list_capacity), st))
+    assert lib.ck_ctx_status(ctx, st) == expect
+    n = out_n.cpu().numpy()
+    t = out_t.cpu().numpy().reshape(nq, top_k)
+    s = out_s.cpu().numpy().reshape(nq, top_k)
+    return [(t[i, :n[i]], s[i, :n[i]]) for i in range(nq)]
+
+
+@pytest.mark.gpu
+def test_similar_neighbour_list_bounds(ck):
+    """The neighbour list three ways on one batch: sized by the library in a
+    fresh context (more triples than its first list holds, so it grows and
+    lists again), under an ample caller bound (no host synchronisation), and
+    under a bound too small (CK_ERR_CAPACITY, after which the context is
+    usable again) -- the first two identical, and one query of them against
+    the oracle."""
+    from clustkit_gb300 import _lib
+    from clustkit_gb300.search import DeviceDatabase
+    db_set = synth.generate_families(600, 8, median=350, lo=60, hi=1200, seed=5)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_queries=8, arena_residues=8 * 2500)
+    rng = np.random.default_rng(6)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 5, replace=False)]
+    qs += [synth.random_sequences(1, median=2000, lo=1800, hi=2200, seed=9).seq(0).copy()]
+    top_k = 400
+    h = np.zeros(1, np.int32)
+    ctxs = []
+    try:
+        for _ in range(2):
+            _lib.check(db.lib.ck_ctx_create(h.ctypes.data))
+            ctxs.append(int(h[0]))
+        sized = _similar_call(db, qs, top_k, -1, ctxs[0])
+        bounded = _similar_call(db, qs, top_k, 1 << 26, ctxs[1])
+        for a, b in zip(sized, bounded):
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        _similar_call(db, qs, top_k, 1000, ctxs[1], expect=_lib.CK_ERR_CAPACITY)
+        again = _similar_call(db, qs, top_k, 1 << 26, ctxs[1])
+        for a, b in zip(sized, again):
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        off, ent, fr = db.index_arrays()
+        ids, sc = so.phase_a_similar(qs[0], off, ent, fr, db.freq_thresh, db_set.n, 2, top_k, BLOSUM62, 13)
+        assert np.array_equal(sized[0][0], ids) and np.array_equal(sized[0][1], sc)
+    finally:
+        for c in ctxs:
+            db.lib.ck_ctx_destroy(c)
 
 
 def test_oracle_kmer_candidates_match_reference_c_scorer(golden):
