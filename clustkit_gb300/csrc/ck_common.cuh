@@ -221,6 +221,7 @@ enum ScratchSlot {
     SLOT_SEARCH_TMP2,
     SLOT_SEARCH_TMP3,
     SLOT_SEARCH_TMP4,
+    SLOT_SEARCH_ROWSEL,
     SLOT_HOST_IO0,
     SLOT_HOST_IO1,
     SLOT_HOST_IO2,

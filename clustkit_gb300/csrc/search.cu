@@ -229,6 +229,7 @@ __global__ void phase_a_count_kernel(const uint8_t *__restrict__ qflat, int64_t 
 }
 
 constexpr int SELECT_THREADS = 1024;
+constexpr int SELECT_UNROLL = 8;  // row values a thread loads at once
 
 // Block-wide radix selection, 8 bits per level from bit `top_shift` down, over
 // the values get(i), i < n, that are >= min_hits: sh[2] = their number; when it
@@ -245,9 +246,22 @@ __device__ void radix_threshold(Get get, int32_t n, int32_t min_hits, int32_t to
         for (int i = tid; i < 256; i += SELECT_THREADS) hist[i] = 0;
         __syncthreads();
         const uint32_t prefix = (uint32_t)sh[0];
-        for (int32_t i = tid; i < n; i += SELECT_THREADS) {
-            const int32_t v = get(i);
-            if (v >= min_hits && ((uint32_t)v & mask) == prefix) atomicAdd(&hist[((uint32_t)v >> shift) & 255u], 1);
+        // SELECT_UNROLL independent loads per thread before any is used:
+        // one block reads a whole count row per pass, so the pass is bound
+        // by the loads it keeps in flight
+        for (int32_t base = 0; base < n; base += SELECT_UNROLL * SELECT_THREADS) {
+            int32_t v[SELECT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SELECT_UNROLL; ++u) {
+                const int32_t i = base + u * SELECT_THREADS + tid;
+                v[u] = i < n ? get(i) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < SELECT_UNROLL; ++u) {
+                const int32_t i = base + u * SELECT_THREADS + tid;
+                if (i < n && v[u] >= min_hits && ((uint32_t)v[u] & mask) == prefix)
+                    atomicAdd(&hist[((uint32_t)v[u] >> shift) & 255u], 1);
+            }
         }
         __syncthreads();
         if (tid == 0) {
@@ -310,7 +324,7 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
                       int32_t clamp, int32_t top_shift, const int32_t *__restrict__ cand,
                       const int32_t *__restrict__ n_cand, int32_t *__restrict__ out_targets,
                       int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n,
-                      int32_t *__restrict__ capped_n) {
+                      int32_t *__restrict__ capped_n, int32_t skip_rows) {
     using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
     __shared__ typename BlockScan::TempStorage scan_tmp;
     __shared__ uint64_t s_buf[CAND_CAP];  // sorted candidate ids, later the capped output's sort keys
@@ -323,6 +337,7 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
     int32_t *o_s = out_scores ? out_scores + (int64_t)q * top_k : nullptr;
     auto val = [&](int32_t t) { const int32_t v = c[t]; return v > clamp ? clamp : v; };
     const bool from_list = min_hits >= 1 && n_cand[q] <= CAND_CAP;
+    if (skip_rows && !from_list) return;  // selected by the row_* kernels
     int32_t *s_id = (int32_t *)s_buf;
 
     if (from_list) {
@@ -363,12 +378,21 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
         const int32_t b1 = min(num_db, b0 + chunk);
         const uint32_t lt = (1u << lane) - 1u;
         int32_t n_strict = 0, n_eq = 0;
-        for (int32_t base = b0; base < b1; base += 32) {
-            const int32_t t = base + lane;
-            const int32_t v = t < b1 ? val(t) : -1;
-            const bool surv = t < b1 && v >= min_hits;
-            n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v > thr)));
-            n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v == thr));
+        for (int32_t base = b0; base < b1; base += 32 * SELECT_UNROLL) {
+            int32_t vv[SELECT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SELECT_UNROLL; ++u) {
+                const int32_t t = base + u * 32 + lane;
+                vv[u] = t < b1 ? val(t) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < SELECT_UNROLL; ++u) {
+                const int32_t t = base + u * 32 + lane;
+                const int32_t v = vv[u];
+                const bool surv = t < b1 && v >= min_hits;
+                n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v > thr)));
+                n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v == thr));
+            }
         }
         __shared__ int32_t w_strict[NW], w_eq[NW], w_eq_base[NW], w_out_base[NW];
         if (lane == 0) { w_strict[warp] = n_strict; w_eq[warp] = n_eq; }
@@ -386,22 +410,31 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
         }
         __syncthreads();
         int32_t eq_seen = w_eq_base[warp], written = w_out_base[warp];
-        for (int32_t base = b0; base < b1; base += 32) {
-            const int32_t t = base + lane;
-            const int32_t v = t < b1 ? val(t) : -1;
-            const bool surv = t < b1 && v >= min_hits;
-            const bool strict = surv && (thr < 0 || v > thr);
-            const bool is_eq = surv && thr >= 0 && v == thr;
-            const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
-            const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
-            const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
-            if (sel) {
-                const int32_t at = written + __popc(sel_b & lt);
-                o_t[at] = t;
-                if (o_s) o_s[at] = v;
+        for (int32_t base = b0; base < b1; base += 32 * SELECT_UNROLL) {
+            int32_t vv[SELECT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SELECT_UNROLL; ++u) {
+                const int32_t t = base + u * 32 + lane;
+                vv[u] = t < b1 ? val(t) : 0;
             }
-            eq_seen += __popc(eq_b);
-            written += __popc(sel_b);
+#pragma unroll
+            for (int u = 0; u < SELECT_UNROLL; ++u) {
+                const int32_t t = base + u * 32 + lane;
+                const int32_t v = vv[u];
+                const bool surv = t < b1 && v >= min_hits;
+                const bool strict = surv && (thr < 0 || v > thr);
+                const bool is_eq = surv && thr >= 0 && v == thr;
+                const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
+                const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
+                const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
+                if (sel) {
+                    const int32_t at = written + __popc(sel_b & lt);
+                    o_t[at] = t;
+                    if (o_s) o_s[at] = v;
+                }
+                eq_seen += __popc(eq_b);
+                written += __popc(sel_b);
+            }
         }
     }
     const int32_t total = sh[2];
@@ -423,6 +456,228 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
     if (tid == 0) {
         out_n[q] = n_out;
         if (capped_n) capped_n[q] = (total > top_k && top_k > CAND_CAP) ? n_out : 0;
+    }
+}
+
+// ----------------------------------------------------------------- row select
+// The same selection for the queries whose survivors are not all in their
+// candidate list, over the whole count row, by ROW_BLOCKS blocks per query
+// (one block scanning a 500,000-counter row took 0.37 ms for one query).
+// The row is cut into ROW_SLOTS warp slices in target order.  The radix
+// threshold runs digit by digit: row_hist_kernel adds each block's histogram
+// of the surviving values that match the digits so far into the query's
+// global one, row_pick_kernel picks the digit (the state stays on the
+// device: no host synchronisation).  Then row_count_kernel counts each
+// slice's values above and at the threshold, row_offsets_kernel turns those
+// into each slice's output position and its share of the ties (lowest ids
+// first), row_write_kernel writes the kept targets in id order and
+// row_sort_kernel puts a capped row in (value desc, id asc) order.
+// Per-query state: threshold (or -1: keep every survivor), count above its
+// last digit, survivors, mode (0 in progress, 1 threshold known, 2 a list
+// query: left to phase_a_select_kernel).
+constexpr int ROW_BLOCKS = 128;
+constexpr int ROW_THREADS = 256;
+constexpr int ROW_SLOTS = ROW_BLOCKS * (ROW_THREADS / 32);  // 1,024 warp slices per row
+
+__global__ void row_init_kernel(const int32_t *__restrict__ n_cand, int32_t min_hits, int32_t nq,
+                                int32_t *__restrict__ state) {
+    const int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const bool from_list = min_hits >= 1 && n_cand[q] <= CAND_CAP;
+    state[4 * q] = 0;
+    state[4 * q + 1] = 0;
+    state[4 * q + 2] = 0;
+    state[4 * q + 3] = from_list ? 2 : 0;
+}
+
+__device__ __forceinline__ int32_t row_value(const int32_t *c, int64_t t, int32_t clamp) {
+    const int32_t v = c[t];
+    return v > clamp ? clamp : v;
+}
+
+__global__ void __launch_bounds__(ROW_THREADS)
+row_hist_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t clamp, int32_t shift,
+                uint32_t mask, const int32_t *__restrict__ state, int32_t *__restrict__ ghist, int32_t W) {
+    __shared__ int32_t h[256];
+    const int32_t q = blockIdx.y;
+    if (state[4 * q + 3] != 0) return;  // the same for the whole block
+    const uint32_t prefix = (uint32_t)state[4 * q];
+    for (int i = threadIdx.x; i < 256; i += ROW_THREADS) h[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t slot = (int64_t)blockIdx.x * (ROW_THREADS / 32) + (threadIdx.x >> 5);
+    const int64_t a0 = slot * W, a1 = a0 + W < num_db ? a0 + W : num_db;
+    const int32_t *c = counts + (int64_t)q * num_db;
+    for (int64_t base = a0; base < a1; base += 32 * SELECT_UNROLL) {
+        int32_t v[SELECT_UNROLL];
+#pragma unroll
+        for (int u = 0; u < SELECT_UNROLL; ++u) {
+            const int64_t t = base + u * 32 + lane;
+            v[u] = t < a1 ? row_value(c, t, clamp) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < SELECT_UNROLL; ++u) {
+            const int64_t t = base + u * 32 + lane;
+            if (t < a1 && v[u] >= min_hits && ((uint32_t)v[u] & mask) == prefix)
+                atomicAdd(&h[((uint32_t)v[u] >> shift) & 255u], 1);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += ROW_THREADS)
+        if (h[i]) atomicAdd(&ghist[(int64_t)q * 256 + i], h[i]);
+}
+
+// One block per query: the digit of this pass (radix_threshold's rule), then
+// the histogram cleared for the next pass.
+__global__ void row_pick_kernel(int32_t *__restrict__ state, int32_t *__restrict__ ghist, int32_t top_k, int32_t shift,
+                                int32_t first, int32_t last) {
+    const int32_t q = blockIdx.x;
+    int32_t *s = state + 4 * q;
+    int32_t *g = ghist + (int64_t)q * 256;
+    if (threadIdx.x == 0 && s[3] == 0) {
+        if (first) {
+            int32_t total = 0;
+            for (int b = 0; b < 256; ++b) total += g[b];
+            s[2] = total;
+            if (total <= top_k) { s[0] = -1; s[1] = 0; s[3] = 1; }
+        }
+        if (s[3] == 0) {
+            int32_t above = s[1], b = 255;
+            for (; b > 0; --b) {
+                if (above + g[b] >= top_k) break;
+                above += g[b];
+            }
+            s[0] = (int32_t)((uint32_t)s[0] | ((uint32_t)b << shift));
+            s[1] = above;
+            if (last) s[3] = 1;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) g[i] = 0;
+}
+
+__global__ void __launch_bounds__(ROW_THREADS)
+row_count_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t clamp,
+                 const int32_t *__restrict__ state, int32_t W, int32_t *__restrict__ wcnt) {
+    const int32_t q = blockIdx.y;
+    if (state[4 * q + 3] != 1) return;
+    const int32_t thr = state[4 * q];
+    const int lane = threadIdx.x & 31;
+    const int64_t slot = (int64_t)blockIdx.x * (ROW_THREADS / 32) + (threadIdx.x >> 5);
+    const int64_t a0 = slot * W, a1 = a0 + W < num_db ? a0 + W : num_db;
+    const int32_t *c = counts + (int64_t)q * num_db;
+    int32_t n_strict = 0, n_eq = 0;
+    for (int64_t base = a0; base < a1; base += 32 * SELECT_UNROLL) {
+        int32_t v[SELECT_UNROLL];
+#pragma unroll
+        for (int u = 0; u < SELECT_UNROLL; ++u) {
+            const int64_t t = base + u * 32 + lane;
+            v[u] = t < a1 ? row_value(c, t, clamp) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < SELECT_UNROLL; ++u) {
+            const int64_t t = base + u * 32 + lane;
+            const bool surv = t < a1 && v[u] >= min_hits;
+            n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v[u] > thr)));
+            n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v[u] == thr));
+        }
+    }
+    if (lane == 0) {
+        wcnt[((int64_t)q * ROW_SLOTS + slot) * 2] = n_strict;
+        wcnt[((int64_t)q * ROW_SLOTS + slot) * 2 + 1] = n_eq;
+    }
+}
+
+// One thread per slice: ties are taken from the lowest slices (lowest ids)
+// until take_eq; each slice's output starts after the kept targets of the
+// slices before it.
+__global__ void __launch_bounds__(ROW_SLOTS)
+row_offsets_kernel(const int32_t *__restrict__ state, const int32_t *__restrict__ wcnt, int32_t top_k,
+                   int32_t *__restrict__ woff, int32_t *__restrict__ out_n, int32_t *__restrict__ capped_n) {
+    using Scan = cub::BlockScan<int32_t, ROW_SLOTS>;
+    __shared__ typename Scan::TempStorage tmp;
+    const int32_t q = blockIdx.x;
+    if (state[4 * q + 3] != 1) return;
+    const int32_t thr = state[4 * q], take_eq = top_k - state[4 * q + 1], total = state[4 * q + 2];
+    const int32_t i = threadIdx.x;
+    const int32_t strict = wcnt[((int64_t)q * ROW_SLOTS + i) * 2], eq = wcnt[((int64_t)q * ROW_SLOTS + i) * 2 + 1];
+    int32_t eq_base;
+    Scan(tmp).ExclusiveSum(eq, eq_base);
+    __syncthreads();
+    int32_t take = take_eq - eq_base;
+    take = thr < 0 ? 0 : (take < 0 ? 0 : (take > eq ? eq : take));
+    int32_t out_base;
+    Scan(tmp).ExclusiveSum(strict + take, out_base);
+    woff[((int64_t)q * ROW_SLOTS + i) * 2] = eq_base;
+    woff[((int64_t)q * ROW_SLOTS + i) * 2 + 1] = out_base;
+    if (i == 0) {
+        const int32_t n_out = total < top_k ? total : top_k;
+        out_n[q] = n_out;
+        if (capped_n) capped_n[q] = (total > top_k && top_k > CAND_CAP) ? n_out : 0;
+    }
+}
+
+__global__ void __launch_bounds__(ROW_THREADS)
+row_write_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t clamp,
+                 const int32_t *__restrict__ state, int32_t W, const int32_t *__restrict__ woff, int32_t top_k,
+                 int32_t *__restrict__ out_targets, int32_t *__restrict__ out_scores) {
+    const int32_t q = blockIdx.y;
+    if (state[4 * q + 3] != 1) return;
+    const int32_t thr = state[4 * q], take_eq = top_k - state[4 * q + 1];
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const int64_t slot = (int64_t)blockIdx.x * (ROW_THREADS / 32) + (threadIdx.x >> 5);
+    const int64_t a0 = slot * W, a1 = a0 + W < num_db ? a0 + W : num_db;
+    const int32_t *c = counts + (int64_t)q * num_db;
+    int32_t *o_t = out_targets + (int64_t)q * top_k;
+    int32_t *o_s = out_scores ? out_scores + (int64_t)q * top_k : nullptr;
+    int32_t eq_seen = woff[((int64_t)q * ROW_SLOTS + slot) * 2], written = woff[((int64_t)q * ROW_SLOTS + slot) * 2 + 1];
+    for (int64_t base = a0; base < a1; base += 32 * SELECT_UNROLL) {
+        int32_t v[SELECT_UNROLL];
+#pragma unroll
+        for (int u = 0; u < SELECT_UNROLL; ++u) {
+            const int64_t t = base + u * 32 + lane;
+            v[u] = t < a1 ? row_value(c, t, clamp) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < SELECT_UNROLL; ++u) {
+            const int64_t t = base + u * 32 + lane;
+            const bool surv = t < a1 && v[u] >= min_hits;
+            const bool strict = surv && (thr < 0 || v[u] > thr);
+            const bool is_eq = surv && thr >= 0 && v[u] == thr;
+            const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
+            const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
+            const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
+            if (sel) {
+                const int32_t at = written + __popc(sel_b & lt);
+                o_t[at] = (int32_t)t;
+                if (o_s) o_s[at] = v[u];
+            }
+            eq_seen += __popc(eq_b);
+            written += __popc(sel_b);
+        }
+    }
+}
+
+// A capped row of at most CAND_CAP kept targets in (value desc, id asc)
+// order, in shared memory (longer capped rows take the segmented sort).
+__global__ void __launch_bounds__(SELECT_THREADS)
+row_sort_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t clamp, const int32_t *__restrict__ state,
+                int32_t top_k, int32_t *__restrict__ out_targets, int32_t *__restrict__ out_scores) {
+    __shared__ uint64_t s_buf[CAND_CAP];
+    const int32_t q = blockIdx.x;
+    if (state[4 * q + 3] != 1 || state[4 * q + 2] <= top_k || top_k > CAND_CAP) return;
+    const int32_t *c = counts + (int64_t)q * num_db;
+    int32_t *o_t = out_targets + (int64_t)q * top_k;
+    int32_t *o_s = out_scores ? out_scores + (int64_t)q * top_k : nullptr;
+    for (int32_t i = threadIdx.x; i < top_k; i += SELECT_THREADS) {
+        const int32_t t = o_t[i];
+        s_buf[i] = ((uint64_t)(uint32_t)(0x7fffffff - row_value(c, t, clamp)) << 32) | (uint32_t)t;
+    }
+    block_bitonic<uint64_t>(s_buf, top_k, ~0ull);
+    for (int32_t i = threadIdx.x; i < top_k; i += SELECT_THREADS) {
+        o_t[i] = (int32_t)(s_buf[i] & 0xffffffffu);
+        if (o_s) o_s[i] = 0x7fffffff - (int32_t)(s_buf[i] >> 32);
     }
 }
 
@@ -815,6 +1070,7 @@ static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, in
                            int32_t clamp, int32_t top_shift, const int32_t *cand, const int32_t *n_cand,
                            int32_t *out_t, int32_t *out_s, int32_t *out_n, bool ordered, cudaStream_t st) {
     int32_t status = CK_OK;
+    if (nq <= 0) return CK_OK;
     const bool sort = top_k > CAND_CAP && ordered;
     int32_t *aux = nullptr;
     if (sort) {
@@ -829,8 +1085,37 @@ static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, in
             if (!out_s) return status;
         }
     }
+    // queries selected from their whole row: the row_* kernels
+    const size_t rs_ints = (size_t)nq * (4 + 256 + 4 * ROW_SLOTS);
+    int32_t *rs = (int32_t *)scratch(SLOT_SEARCH_ROWSEL, rs_ints * 4, &status);
+    if (!rs) return status;
+    int32_t *state = rs, *ghist = rs + 4 * (size_t)nq, *wcnt = ghist + 256 * (size_t)nq;
+    int32_t *woff = wcnt + 2 * (size_t)ROW_SLOTS * nq;
+    CK_CUDA(cudaMemsetAsync(ghist, 0, (size_t)nq * 256 * 4, st));
+    row_init_kernel<<<(nq + 255) / 256, 256, 0, st>>>(n_cand, min_hits, nq, state);
+    CK_CUDA(cudaGetLastError());
+    const int64_t slice = ((int64_t)num_db + ROW_SLOTS - 1) / ROW_SLOTS;
+    const int32_t W = (int32_t)std::max<int64_t>(32, (slice + 31) / 32 * 32);
+    const dim3 rg((unsigned)ROW_BLOCKS, (unsigned)nq);
+    for (int shift = top_shift; shift >= 0; shift -= 8) {
+        // the digits already fixed: bits shift + 8 .. top_shift + 7
+        const uint32_t mask = (uint32_t)((((uint64_t)1 << (top_shift + 8)) - 1) & ~(((uint64_t)1 << (shift + 8)) - 1));
+        row_hist_kernel<<<rg, ROW_THREADS, 0, st>>>(counts, num_db, min_hits, clamp, shift, mask, state, ghist, W);
+        CK_CUDA(cudaGetLastError());
+        row_pick_kernel<<<nq, 256, 0, st>>>(state, ghist, top_k, shift, shift == top_shift, shift == 0);
+        CK_CUDA(cudaGetLastError());
+    }
+    row_count_kernel<<<rg, ROW_THREADS, 0, st>>>(counts, num_db, min_hits, clamp, state, W, wcnt);
+    CK_CUDA(cudaGetLastError());
+    row_offsets_kernel<<<nq, ROW_SLOTS, 0, st>>>(state, wcnt, top_k, woff, out_n, aux);
+    CK_CUDA(cudaGetLastError());
+    row_write_kernel<<<rg, ROW_THREADS, 0, st>>>(counts, num_db, min_hits, clamp, state, W, woff, top_k, out_t, out_s);
+    CK_CUDA(cudaGetLastError());
+    row_sort_kernel<<<nq, SELECT_THREADS, 0, st>>>(counts, num_db, clamp, state, top_k, out_t, out_s);
+    CK_CUDA(cudaGetLastError());
+    // queries whose candidate lists hold all their survivors
     phase_a_select_kernel<<<nq, SELECT_THREADS, 0, st>>>(counts, num_db, min_hits, top_k, clamp, top_shift, cand,
-                                                         n_cand, out_t, out_s, out_n, aux);
+                                                         n_cand, out_t, out_s, out_n, aux, 1);
     CK_CUDA(cudaGetLastError());
     if (!sort) return CK_OK;
     const size_t items = (size_t)nq * top_k;
