@@ -466,7 +466,7 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
 // The row is cut into ROW_SLOTS warp slices in target order.  The radix
 // threshold runs digit by digit: row_hist_kernel adds each block's histogram
 // of the surviving values that match the digits so far into the query's
-// global one, row_pick_kernel picks the digit (the state stays on the
+// global one and its last block picks the digit (the state stays on the
 // device: no host synchronisation).  Then row_count_kernel counts each
 // slice's values above and at the threshold, row_offsets_kernel turns those
 // into each slice's output position and its share of the ties (lowest ids
@@ -474,34 +474,41 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
 // row_sort_kernel puts a capped row in (value desc, id asc) order.
 // Per-query state: threshold (or -1: keep every survivor), count above its
 // last digit, survivors, mode (0 in progress, 1 threshold known, 2 a list
-// query: left to phase_a_select_kernel).
+// query: left to phase_a_select_kernel).  The digit pick runs in the last
+// histogram block of each query (no launch of its own).
 constexpr int ROW_BLOCKS = 128;
 constexpr int ROW_THREADS = 256;
 constexpr int ROW_SLOTS = ROW_BLOCKS * (ROW_THREADS / 32);  // 1,024 warp slices per row
-
-__global__ void row_init_kernel(const int32_t *__restrict__ n_cand, int32_t min_hits, int32_t nq,
-                                int32_t *__restrict__ state) {
-    const int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
-    const bool from_list = min_hits >= 1 && n_cand[q] <= CAND_CAP;
-    state[4 * q] = 0;
-    state[4 * q + 1] = 0;
-    state[4 * q + 2] = 0;
-    state[4 * q + 3] = from_list ? 2 : 0;
-}
 
 __device__ __forceinline__ int32_t row_value(const int32_t *c, int64_t t, int32_t clamp) {
     const int32_t v = c[t];
     return v > clamp ? clamp : v;
 }
 
+// One radix digit of every row query's threshold.  Each block adds its
+// slice's histogram into the query's global one; the last block of the query
+// to finish (a counter, after a fence) picks the digit as radix_threshold
+// does, records the state and clears the histogram and the counter for the
+// next pass.  The first pass also sets every query's mode (a list query is
+// marked and skipped).
 __global__ void __launch_bounds__(ROW_THREADS)
 row_hist_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t clamp, int32_t shift,
-                uint32_t mask, const int32_t *__restrict__ state, int32_t *__restrict__ ghist, int32_t W) {
+                uint32_t mask, int32_t first, int32_t last, const int32_t *__restrict__ n_cand, int32_t top_k,
+                int32_t *__restrict__ state, int32_t *__restrict__ ghist, int32_t *__restrict__ done, int32_t W) {
     __shared__ int32_t h[256];
+    __shared__ int32_t is_last;
     const int32_t q = blockIdx.y;
-    if (state[4 * q + 3] != 0) return;  // the same for the whole block
-    const uint32_t prefix = (uint32_t)state[4 * q];
+    int32_t *s = state + 4 * q;
+    uint32_t prefix = 0;
+    if (first) {
+        if (min_hits >= 1 && n_cand[q] <= CAND_CAP) {  // a list query, the same for the whole block
+            if (blockIdx.x == 0 && threadIdx.x == 0) { s[0] = 0; s[1] = 0; s[2] = 0; s[3] = 2; }
+            return;
+        }
+    } else {
+        if (s[3] != 0) return;  // the same for the whole block
+        prefix = (uint32_t)s[0];
+    }
     for (int i = threadIdx.x; i < 256; i += ROW_THREADS) h[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -523,41 +530,38 @@ row_hist_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_
         }
     }
     __syncthreads();
+    int32_t *g = ghist + (int64_t)q * 256;
     for (int i = threadIdx.x; i < 256; i += ROW_THREADS)
-        if (h[i]) atomicAdd(&ghist[(int64_t)q * 256 + i], h[i]);
-}
-
-// One block of 256 threads per query: the histogram staged in shared memory
-// (a serial scan of global memory behind a data-dependent exit cost 17 us),
-// the digit of this pass (radix_threshold's rule), the global histogram
-// cleared for the next pass.
-__global__ void row_pick_kernel(int32_t *__restrict__ state, int32_t *__restrict__ ghist, int32_t top_k, int32_t shift,
-                                int32_t first, int32_t last) {
-    __shared__ int32_t g[256];
-    const int32_t q = blockIdx.x;
-    int32_t *s = state + 4 * q;
-    int32_t *gg = ghist + (int64_t)q * 256;
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) g[i] = gg[i];
+        if (h[i]) atomicAdd(&g[i], h[i]);
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0 && s[3] == 0) {
+    if (threadIdx.x == 0) is_last = atomicAdd(&done[q], 1) == (int32_t)gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    for (int i = threadIdx.x; i < 256; i += ROW_THREADS) h[i] = __ldcg(&g[i]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t above = first ? 0 : s[1], total = first ? 0 : s[2];
+        bool decided = false;
         if (first) {
-            int32_t total = 0;
-            for (int b = 0; b < 256; ++b) total += g[b];
-            s[2] = total;
-            if (total <= top_k) { s[0] = -1; s[1] = 0; s[3] = 1; }
+            for (int b = 0; b < 256; ++b) total += h[b];
+            if (total <= top_k) { s[0] = -1; s[1] = 0; s[2] = total; s[3] = 1; decided = true; }
         }
-        if (s[3] == 0) {
-            int32_t above = s[1], b = 255;
+        if (!decided) {
+            int32_t b = 255;
             for (; b > 0; --b) {
-                if (above + g[b] >= top_k) break;
-                above += g[b];
+                if (above + h[b] >= top_k) break;
+                above += h[b];
             }
-            s[0] = (int32_t)((uint32_t)s[0] | ((uint32_t)b << shift));
+            s[0] = (int32_t)(prefix | ((uint32_t)b << shift));
             s[1] = above;
-            if (last) s[3] = 1;
+            s[2] = total;
+            s[3] = last ? 1 : 0;
         }
+        done[q] = 0;
     }
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) gg[i] = 0;
+    for (int i = threadIdx.x; i < 256; i += ROW_THREADS) g[i] = 0;
 }
 
 __global__ void __launch_bounds__(ROW_THREADS)
@@ -1090,23 +1094,21 @@ static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, in
         }
     }
     // queries selected from their whole row: the row_* kernels
-    const size_t rs_ints = (size_t)nq * (4 + 256 + 4 * ROW_SLOTS);
+    const size_t rs_ints = (size_t)nq * (4 + 256 + 1 + 4 * ROW_SLOTS);
     int32_t *rs = (int32_t *)scratch(SLOT_SEARCH_ROWSEL, rs_ints * 4, &status);
     if (!rs) return status;
-    int32_t *state = rs, *ghist = rs + 4 * (size_t)nq, *wcnt = ghist + 256 * (size_t)nq;
-    int32_t *woff = wcnt + 2 * (size_t)ROW_SLOTS * nq;
-    CK_CUDA(cudaMemsetAsync(ghist, 0, (size_t)nq * 256 * 4, st));
-    row_init_kernel<<<(nq + 255) / 256, 256, 0, st>>>(n_cand, min_hits, nq, state);
-    CK_CUDA(cudaGetLastError());
+    int32_t *state = rs, *ghist = rs + 4 * (size_t)nq, *done = ghist + 256 * (size_t)nq;
+    int32_t *wcnt = done + (size_t)nq, *woff = wcnt + 2 * (size_t)ROW_SLOTS * nq;
+    CK_CUDA(cudaMemsetAsync(ghist, 0, (size_t)nq * 257 * 4, st));  // histograms and block counters
     const int64_t slice = ((int64_t)num_db + ROW_SLOTS - 1) / ROW_SLOTS;
     const int32_t W = (int32_t)std::max<int64_t>(32, (slice + 31) / 32 * 32);
     const dim3 rg((unsigned)ROW_BLOCKS, (unsigned)nq);
     for (int shift = top_shift; shift >= 0; shift -= 8) {
         // the digits already fixed: bits shift + 8 .. top_shift + 7
         const uint32_t mask = (uint32_t)((((uint64_t)1 << (top_shift + 8)) - 1) & ~(((uint64_t)1 << (shift + 8)) - 1));
-        row_hist_kernel<<<rg, ROW_THREADS, 0, st>>>(counts, num_db, min_hits, clamp, shift, mask, state, ghist, W);
-        CK_CUDA(cudaGetLastError());
-        row_pick_kernel<<<nq, 256, 0, st>>>(state, ghist, top_k, shift, shift == top_shift, shift == 0);
+        row_hist_kernel<<<rg, ROW_THREADS, 0, st>>>(counts, num_db, min_hits, clamp, shift, mask,
+                                                    shift == top_shift, shift == 0, n_cand, top_k, state, ghist,
+                                                    done, W);
         CK_CUDA(cudaGetLastError());
     }
     row_count_kernel<<<rg, ROW_THREADS, 0, st>>>(counts, num_db, min_hits, clamp, state, W, wcnt);
