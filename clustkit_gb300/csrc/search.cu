@@ -737,6 +737,7 @@ constexpr int32_t NB_PREFIX = 400;
 constexpr int NB_WARPS = 8;              // warps per block
 constexpr int32_t NB_STAGE = 1024;       // staged entries per warp (a round adds at most 32 x 20)
 constexpr uint32_t NB_SCORE_SHIFT = 22;
+constexpr int64_t NB_BLOCKS_PER_QUERY = 512;
 
 __device__ __forceinline__ void nbr_flush(const uint32_t *stage, int32_t fill, int32_t q, uint64_t *list,
                                           int64_t cap, unsigned long long *cursor, int lane) {
@@ -868,12 +869,15 @@ __global__ void fill_kernel(int32_t *a, int32_t n, int32_t v) {
     for (int32_t i = threadIdx.x; i < n; i += blockDim.x) a[i] = v;
 }
 
-// Stage 2.  Block b walks triples [b * chunk, (b + 1) * chunk) of the list,
-// which the listing pass fills about one query at a time: the blocks in
-// flight then add into one or two queries' count rows, which stay in L2 (a
-// grid-stride walk, whose warps drift apart over the whole list, kept every
-// row of a 64-query batch live: 25.7 GB of DRAM writes instead of 0.24, and
-// 1.5x the time).
+// Stage 2.  A persistent grid; each block takes chunks of the list in order
+// (a ticket counter) and walks them.  The listing pass fills the list about
+// one query at a time, so the blocks in flight add into one or two queries'
+// count rows, which stay in L2 (a grid-stride walk, whose warps drift apart
+// over the whole list, kept every row of a 64-query batch live: 25.7 GB of
+// DRAM writes instead of 0.24, and 1.5x the time).  The chunk comes from the
+// count on the device (a multiple of 256, at most 2,048 triples): at least
+// two per block, and the blocks in flight within about two queries' triples;
+// so the launch needs no count from the host.
 // A warp takes 32 triples at once: each lane loads one and its posting-list
 // bounds -- 32 independent loads instead of 32 chains -- then the warp walks
 // the concatenated lists, lane k of each round taking entry k of the stream
@@ -881,17 +885,13 @@ __global__ void fill_kernel(int32_t *a, int32_t n, int32_t v) {
 // of list lengths) and adding the triple's score to the entry's target in
 // the triple's query row.  A list longer than `cap` (the listing pass
 // counted more triples than it could write) is reported.
-__global__ void nbr_walk_kernel(const uint64_t *__restrict__ list, const unsigned long long *__restrict__ cursor,
-                                int64_t cap, int64_t chunk, int32_t nq, const int64_t *__restrict__ kmer_offsets,
-                                const int64_t *__restrict__ kmer_entries, const int32_t *__restrict__ kmer_targets,
-                                int32_t num_db, int32_t *__restrict__ counts, int32_t *err) {
+// Warps of the block take 32 triples of [c0, c1) at a time.
+__device__ __forceinline__ void walk_chunk(const uint64_t *__restrict__ list, int64_t c0, int64_t c1, int32_t nq,
+                                           const int64_t *__restrict__ kmer_offsets,
+                                           const int64_t *__restrict__ kmer_entries,
+                                           const int32_t *__restrict__ kmer_targets, int32_t num_db,
+                                           int32_t *__restrict__ counts, int32_t *err, int lane) {
     constexpr uint32_t FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long listed = *cursor;
-    if (listed > (unsigned long long)cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERRBIT_LIST);
-    const int64_t n = (int64_t)(listed < (unsigned long long)cap ? listed : (unsigned long long)cap);
-    const int64_t c0 = (int64_t)blockIdx.x * chunk;
-    const int64_t c1 = c0 + chunk < n ? c0 + chunk : n;
     for (int64_t base = c0 + (threadIdx.x >> 5) * 32; base < c1; base += blockDim.x) {
         const int64_t e = base + lane;
         int64_t b = 0;
@@ -943,6 +943,32 @@ __global__ void nbr_walk_kernel(const uint64_t *__restrict__ list, const unsigne
                 }
             }
         }
+    }
+}
+
+__global__ void nbr_walk_kernel(const uint64_t *__restrict__ list, const unsigned long long *__restrict__ cursor,
+                                int64_t cap, int32_t nq, const int64_t *__restrict__ kmer_offsets,
+                                const int64_t *__restrict__ kmer_entries, const int32_t *__restrict__ kmer_targets,
+                                int32_t num_db, int32_t *__restrict__ counts, unsigned long long *__restrict__ ticket,
+                                int32_t *err) {
+    __shared__ int64_t s_c0;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long listed = *cursor;
+    if (listed > (unsigned long long)cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERRBIT_LIST);
+    const int64_t n = (int64_t)(listed < (unsigned long long)cap ? listed : (unsigned long long)cap);
+    const int64_t G = gridDim.x;
+    int64_t chunk = 2 * n / ((int64_t)(nq > 0 ? nq : 1) * G);
+    if (n / (2 * G) < chunk) chunk = n / (2 * G);
+    chunk = chunk / 256 * 256;
+    chunk = chunk < 256 ? 256 : (chunk > 2048 ? 2048 : chunk);
+    for (;;) {
+        if (threadIdx.x == 0) s_c0 = (int64_t)atomicAdd(ticket, 1ull) * chunk;
+        __syncthreads();
+        const int64_t c0 = s_c0;
+        __syncthreads();  // every thread has read s_c0 before it is written again
+        if (c0 >= n) break;  // the same for the whole block
+        const int64_t c1 = c0 + chunk < n ? c0 + chunk : n;
+        walk_chunk(list, c0, c1, nq, kmer_offsets, kmer_entries, kmer_targets, num_db, counts, err, lane);
     }
 }
 
@@ -1176,8 +1202,10 @@ static int32_t phase_a_impl(void *pv) {
         const int8_t *d_sub = device_sub_matrix(a.sub_host, &status);
         if (!d_sub) return status;
         if (npos > 0) {
-            unsigned long long *cursor = (unsigned long long *)scratch(SLOT_SEARCH_TMP0, 8, &status);
+            // the listing's cursor and the walk's chunk ticket
+            unsigned long long *cursor = (unsigned long long *)scratch(SLOT_SEARCH_TMP0, 16, &status);
             if (!cursor) return status;
+            unsigned long long *ticket = cursor + 1;
             const bool bounded = a.list_capacity >= 0;
             // unbounded: the list scratch as it stands (at least 1 Mi triples); a
             // call that lists more grows it to the count and lists again
@@ -1186,12 +1214,14 @@ static int32_t phase_a_impl(void *pv) {
             uint64_t *list = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)std::max<int64_t>(cap, 1) * 8, &status);
             if (!list) return status;
             if (!bounded) cap = (int64_t)(scratch_capacity(SLOT_SEARCH_TMP1) / 8);
-            // one block per 256 items of the longest query: blocks start in
-            // query order, so the list fills (and the walk later runs) about
-            // one query at a time -- the walk's count-row atomics then hit L2
-            // (interleaving ten queries' rows cost it 1.5x)
+            // one block per 256 items of the longest query, at most
+            // NB_BLOCKS_PER_QUERY (longer queries loop; a graph captured for
+            // an arena-long query would otherwise launch ~10^5 empty blocks per
+            // query): blocks start in query order, so the list fills (and the
+            // walk later runs) about one query at a time -- the walk's
+            // count-row atomics then hit L2
             const int64_t groups = ((int64_t)npos * NB_PREFIX + NB_WARPS * 32 - 1) / (NB_WARPS * 32);
-            const dim3 grid((unsigned)groups, (unsigned)a.nq);
+            const dim3 grid((unsigned)std::min<int64_t>(groups, NB_BLOCKS_PER_QUERY), (unsigned)a.nq);
             int64_t listed = -1;
             for (int pass = 0; pass < 2; ++pass) {
                 CK_CUDA(cudaMemsetAsync(cursor, 0, 8, a.st));
@@ -1211,22 +1241,13 @@ static int32_t phase_a_impl(void *pv) {
                 if (!list) return status;
                 cap = (int64_t)(scratch_capacity(SLOT_SEARCH_TMP1) / 8);
             }
-            // the walk's grid: one block per chunk of the count when it is
-            // known, else of the bound (blocks past the count exit at once).
-            // A chunk (a multiple of 256, at most 2048 triples) leaves at
-            // least two blocks per resident slot, and the resident blocks
-            // within about two queries' triples
+            // the walk: one resident block per slot (8 of 256 threads per
+            // SM), fewer when the count is known to be small
             const int64_t n_walk = listed >= 0 ? listed : cap;
-            const int64_t resident = (int64_t)8 * sm_count();
-            int64_t chunk = std::min<int64_t>(2 * n_walk / ((int64_t)a.nq * resident), n_walk / (2 * resident));
-            chunk = std::min<int64_t>(2048, std::max<int64_t>(256, chunk / 256 * 256));
-            const int64_t bw = std::max<int64_t>(1, (n_walk + chunk - 1) / chunk);
-            if (bw > INT32_MAX) {
-                set_error(CK_ERR_UNSUPPORTED, "similar k-mer phase A: neighbour list too long");
-                return CK_ERR_UNSUPPORTED;
-            }
-            nbr_walk_kernel<<<(unsigned)bw, 256, 0, a.st>>>(list, cursor, cap, chunk, a.nq, a.kmer_offsets,
-                                                            a.kmer_entries, a.kmer_targets, a.num_db, counts, err);
+            const int64_t bw = std::max<int64_t>(1, std::min<int64_t>((int64_t)8 * sm_count(), (n_walk + 255) / 256));
+            CK_CUDA(cudaMemsetAsync(ticket, 0, 8, a.st));
+            nbr_walk_kernel<<<(unsigned)bw, 256, 0, a.st>>>(list, cursor, cap, a.nq, a.kmer_offsets, a.kmer_entries,
+                                                            a.kmer_targets, a.num_db, counts, ticket, err);
             CK_CUDA(cudaGetLastError());
             // the select scans the whole count row (no candidate list in this mode)
             fill_kernel<<<1, 256, 0, a.st>>>(n_cand, a.nq, CAND_CAP + 1);

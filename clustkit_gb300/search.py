@@ -92,15 +92,23 @@ class Scoring:
 
     @property
     def graphable(self) -> bool:
-        """The pipeline can run without host synchronisation (every mode but
-        the similar-k-mer one, which sizes its neighbour list on the host;
-        Phase B needs its bin bound to fit, see _Slot.bins_bound)."""
-        return not self.similar
+        """The pipeline can run without host synchronisation: every mode, under
+        a caller bound where the library would otherwise read a device count
+        (the Phase-B bins, _Slot.bins_bound; the similar-k-mer neighbour list,
+        _Slot.list_bound)."""
+        return True
 
 
 # largest Phase-B bin buffer a slot keeps resident (int32 counters); beyond it
 # the bins are sized per call from a device count (one host synchronisation)
 BINS_CAP = 1 << 29
+# Graph-replayed similar-k-mer batches list at most LIST_RATE neighbour triples
+# per arena residue (~5,000 per residue is typical at threshold 13 on a 500k
+# database, and arenas hold ~5x the residues of a typical batch); a batch that
+# lists more is run again call by call.  LIST_CAP bounds the list (8 bytes a
+# triple).
+LIST_RATE = 2048
+LIST_CAP = 1 << 28
 
 
 def _torch():
@@ -214,6 +222,8 @@ class _Slot:
         h = np.zeros(1, np.int32)
         _lib.check(db.lib.ck_ctx_create(h.ctypes.data))
         self.ctx = int(h[0])
+        self.ctx_spare = 0  # an unfrozen context for reruns of replayed batches, made on first use
+        self._batch_info = None  # (scoring, max_qlen, residues, replayed) of the batch in flight
         Q, K = db.arena_queries, max_cands
         self.seq0 = db.arena_seq0 + index * Q
         self.res0 = db.arena_res0 + index * db.arena_residues
@@ -247,9 +257,10 @@ class _Slot:
 
     def close(self):
         self.graphs.clear()
-        if self.ctx:
-            self.db.lib.ck_ctx_destroy(self.ctx)
-            self.ctx = 0
+        for name in ("ctx", "ctx_spare"):
+            if getattr(self, name):
+                self.db.lib.ck_ctx_destroy(getattr(self, name))
+                setattr(self, name, 0)
 
     def enable_stage_timing(self):
         torch = _torch()
@@ -310,22 +321,33 @@ class _Slot:
         bound = topk * ((int(res_bytes) + nq * db.max_len) // w + nq)
         return bound if bound <= BINS_CAP else -1
 
+    def list_bound(self, res_bytes: int) -> int:
+        """The caller bound on a similar-k-mer batch's neighbour triples
+        (LIST_RATE per residue of the slot arena); -1 when above LIST_CAP."""
+        bound = int(res_bytes) * LIST_RATE
+        return bound if bound <= LIST_CAP else -1
+
     def can_capture(self, sc: Scoring) -> bool:
         """Whether the pipeline for ``sc`` can be captured in graphs on this slot."""
         if not sc.graphable:
             return False
+        if sc.similar:
+            return self.list_bound(self.db.arena_residues) >= 0
         return not sc.diagonal or self.bins_bound(self.db.arena_queries, self.db.arena_residues, sc) >= 0
 
-    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, sc: Scoring):
+    def _enqueue(self, nq: int, max_qlen: int, res_bytes: int, sc: Scoring, bounded: bool = False,
+                 ctx: int | None = None):
         """The device pipeline of a batch of nq queries on this slot's stream:
-        H2D, k-mer scoring, pair list, SW, D2H.  For exact Phase A with the
-        database band there is no host synchronisation, so it can be captured
-        in a CUDA graph."""
+        H2D, k-mer scoring, pair list, SW, D2H.  ``bounded``: the similar-k-mer
+        neighbour list under the slot's list bound, so that no step reads a
+        device count on the host and the pipeline can be captured in a CUDA
+        graph.  ``ctx``: a library context other than the slot's."""
         torch = _torch()
         db = self.db
         K = self.max_cands
         M = nq * K
         lib = db.lib
+        ctx = self.ctx if ctx is None else ctx
         st = self.stream.cuda_stream
         self._mark(0)
         db.d_flat[self.res0:self.res0 + res_bytes].copy_(self.h_res[:res_bytes], non_blocking=True)
@@ -337,13 +359,14 @@ class _Slot:
         min_total_hits = int(sc.min_total_hits)
         if sc.similar:  # BLOSUM62 similar k-mers (k = 5), clustkit's default scoring
             _lib.check(lib.ck_search_phase_a_similar_device(
-                self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen, _SUB.ctypes.data,
+                ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen, _SUB.ctypes.data,
                 int(sc.kmer_score_thresh), db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(),
                 db.kmer_targets_ptr, db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
-                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), -1, st))
+                self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(),
+                self.list_bound(db.arena_residues) if bounded else -1, st))
         elif sc.diagonal:  # the C scorer's Phase A + Phase B, with diagonal hints
             _lib.check(lib.ck_search_kmer_candidates_device(
-                self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
+                ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
                 db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr,
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, db.d_lengths.data_ptr(), min_total_hits,
                 int(sc.min_diag_hits), int(sc.diag_bin_width), K, int(sc.phase_a_topk),
@@ -351,7 +374,7 @@ class _Slot:
                 self.d_n.data_ptr(), self.bins_bound(nq, res_bytes, sc), st))
         else:
             _lib.check(lib.ck_search_phase_a_device(
-                self.ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
+                ctx, db.d_flat.data_ptr(), db.flat_len, qoff_ptr, qlen_ptr, nq, max_qlen,
                 db.k, db.alpha, db.d_kmer_offsets.data_ptr(), db.d_kmer_entries.data_ptr(), db.kmer_targets_ptr,
                 db.d_kmer_freqs.data_ptr(), db.freq_thresh, db.n, min_total_hits, K,
                 self.d_targets.data_ptr(), self.d_counts.data_ptr(), self.d_n.data_ptr(), st))
@@ -364,7 +387,7 @@ class _Slot:
         self.d_pairs[:M, 0] = torch.where(valid, q + self.seq0, torch.full_like(q, db.empty_idx))
         self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M], torch.full_like(q, db.empty_idx))
         _lib.check(lib.ck_sw_batch_device_ctx(
-            self.ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
+            ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
             db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, self.last_band,
             _SUB.ctypes.data, 0.0, self.d_diags.data_ptr() if sc.hints else None, PASS_SCORE, ENGINE_BATCHED,
             self.d_sims.data_ptr(), self.d_scores.data_ptr(), None, None, self.d_mask.data_ptr(), st))
@@ -393,14 +416,14 @@ class _Slot:
         if not self.can_capture(sc):
             raise ValueError("this scoring cannot run without host synchronisation on this slot")
         with torch.cuda.stream(self.stream):
-            self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, sc)
+            self._enqueue(buckets[-1], db.arena_residues, db.arena_residues, sc, bounded=True)
         self.stream.synchronize()
         _lib.check(db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream))
         _lib.check(db.lib.ck_ctx_freeze(self.ctx, 1))
         for b in buckets:
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-                self._enqueue(b, db.arena_residues, db.arena_residues, sc)
+                self._enqueue(b, db.arena_residues, db.arena_residues, sc, bounded=True)
             self.graphs[b] = g
         # one replay of each (empty queries) so no graph's first upload falls
         # on a request
@@ -413,8 +436,7 @@ class _Slot:
     def launch(self, queries: list[np.ndarray], min_total_hits: int, kmer_score_thresh: int = 0, **scoring):
         """Enqueue the whole pipeline for a batch on this slot's stream
         (``scoring``: the other fields of Scoring).  Batches with the scoring the
-        slot's graphs were captured for replay them; others (the similar-k-mer
-        scoring sizes its neighbour list on the host) run call by call."""
+        slot's graphs were captured for replay them; others run call by call."""
         torch = _torch()
         db = self.db
         sc = Scoring(int(min_total_hits), int(kmer_score_thresh), **scoring)
@@ -432,13 +454,36 @@ class _Slot:
                 self._enqueue(nq, int(lens.max() if nq else 0), tot, sc)
                 self.event.record(self.stream)
         self.batch = (nq, lens)
+        self._batch_info = (sc, int(lens.max() if nq else 0), tot, bucket is not None)
+
+    def _rerun_unbounded(self):
+        """The batch in flight again, call by call in the slot's spare context
+        (unfrozen, so its neighbour list can grow): a replayed batch whose
+        listing passed the slot's list bound.  The pinned inputs still hold
+        the batch; the outputs land in the same buffers."""
+        torch = _torch()
+        if not self.ctx_spare:
+            h = np.zeros(1, np.int32)
+            _lib.check(self.db.lib.ck_ctx_create(h.ctypes.data))
+            self.ctx_spare = int(h[0])
+        sc, max_qlen, tot, _ = self._batch_info
+        nq = self.batch[0]
+        with torch.cuda.stream(self.stream):
+            self._enqueue(nq, max_qlen, tot, sc, ctx=self.ctx_spare)
+            self.event.record(self.stream)
+        self.event.synchronize()
+        _lib.check(self.db.lib.ck_ctx_status(self.ctx_spare, self.stream.cuda_stream))
 
     def results(self, top_k: int, evalue_normalize: bool = True) -> list[list[SearchHit]]:
         """Hits of the batch (after the slot's event): top_k per query, ranked
         by 0.267 * score - ln(qlen * tlen), or by the raw score when
         evalue_normalize is off (clustkit/kmer_index.py:2315-2323)."""
         db = self.db
-        _lib.check(db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream))
+        status = db.lib.ck_ctx_status(self.ctx, self.stream.cuda_stream)
+        if status == _lib.CK_ERR_CAPACITY and self._batch_info and self._batch_info[3] and self._batch_info[0].similar:
+            self._rerun_unbounded()
+        else:
+            _lib.check(status)
         nq, lens = self.batch
         K = self.max_cands
         n = self.h_n.numpy()[:nq]
@@ -669,6 +714,8 @@ class SearchServer:
         sc = Scoring(int(min_total_hits), self.kmer_score_thresh, **scoring)
         if sc.diagonal:  # Phase B: target -> selection row, selection and bin offsets
             per_slot += db.arena_queries * (db.n * 4 + min(sc.phase_a_topk, db.n) * 16)
+        if sc.similar and use_graphs:  # the bounded neighbour list (8 bytes a triple)
+            per_slot += max(0, db.arena_residues * LIST_RATE) * 8
         n_slots = int(max(1, min(db.slots, (free // 2) // max(per_slot, 1))))
         self.slots = [_Slot(db, i, max_cands) for i in range(n_slots)]
         self.free = list(self.slots)

@@ -180,14 +180,20 @@ _C_PATH = {"min_diag_hits": 2, "use_c_scoring": True, "use_c_sw": True}
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("use_graphs,thresh,scoring", [(True, 0, {}), (False, 0, {}), (False, 13, {}),
-                                                       (True, 0, _C_PATH)])
-def test_server_results_same_alone_and_in_mix(ck, use_graphs, thresh, scoring):
+@pytest.mark.parametrize("use_graphs,thresh,scoring,list_rate",
+                         [(True, 0, {}, None), (False, 0, {}, None), (False, 13, {}, None), (True, 13, {}, None),
+                          (True, 13, {}, 1), (True, 0, _C_PATH, None)])
+def test_server_results_same_alone_and_in_mix(ck, monkeypatch, use_graphs, thresh, scoring, list_rate):
     """Each query's hits are identical whether it is searched alone or lands
     in concurrent batches of the continuous-batching server (slots replaying
     captured CUDA graphs, or launching the pipeline call by call; exact,
-    similar-k-mer and Phase-B + hinted-SW scoring)."""
+    similar-k-mer and Phase-B + hinted-SW scoring).  ``list_rate`` 1: a
+    similar-k-mer list bound so small that every replayed batch overflows it
+    and is run again call by call in the slot's spare context."""
+    from clustkit_gb300 import search as search_mod
     from clustkit_gb300.search import DeviceDatabase, SearchServer, search_batch
+    if list_rate is not None:
+        monkeypatch.setattr(search_mod, "LIST_RATE", list_rate)
     db_set = synth.generate_families(400, 10, median=200, lo=40, hi=600, seed=92)
     db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_slots=3, arena_queries=16,
                         arena_residues=16 * 600)
@@ -201,9 +207,15 @@ def test_server_results_same_alone_and_in_mix(ck, use_graphs, thresh, scoring):
     try:
         futs = [server.submit(q) for q in qs]
         mixed = [f.result(timeout=120) for f in futs]
+        replaying = [bool(s.graphs) for s in server.slots]
+        spare = [s.ctx_spare for s in server.slots]
     finally:
         server.stop()
     assert len(server.slots) >= 2
+    if use_graphs:
+        assert all(replaying)
+    if list_rate is not None:  # every slot's warm-up batch already overflowed
+        assert all(spare)
     for a, b in zip(alone, mixed):
         assert [(h.target, h.identity, h.score, h.rank) for h in a] == \
             [(h.target, h.identity, h.score, h.rank) for h in b]
