@@ -315,16 +315,16 @@ __device__ void block_bitonic(K *a, int32_t n, K pad) {
 // the counts clamped to `clamp`): all of them in target-id order when at most
 // top_k, else the top_k by value -- ties to the lower target id -- in
 // descending value order, as clustkit's argsort(-scores) gives them
-// (kmer_index.py:893-899, :1320-1325).  Targets come from the query's
-// candidate list when it is complete (min_hits >= 1, at most CAND_CAP listed:
-// sorted by id in shared memory), else from a scan of the whole count row
-// (warp-contiguous ballot compaction).
+// (kmer_index.py:893-899, :1320-1325).  This kernel takes the queries whose
+// candidate list is complete (min_hits >= 1, at most CAND_CAP listed: sorted
+// by id in shared memory); the others are selected from their whole count row
+// by the row_* kernels.
 __global__ void __launch_bounds__(SELECT_THREADS)
 phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_t min_hits, int32_t top_k,
                       int32_t clamp, int32_t top_shift, const int32_t *__restrict__ cand,
                       const int32_t *__restrict__ n_cand, int32_t *__restrict__ out_targets,
                       int32_t *__restrict__ out_scores, int32_t *__restrict__ out_n,
-                      int32_t *__restrict__ capped_n, int32_t skip_rows) {
+                      int32_t *__restrict__ capped_n) {
     using BlockScan = cub::BlockScan<int32_t, SELECT_THREADS>;
     __shared__ typename BlockScan::TempStorage scan_tmp;
     __shared__ uint64_t s_buf[CAND_CAP];  // sorted candidate ids, later the capped output's sort keys
@@ -336,11 +336,9 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
     int32_t *o_t = out_targets + (int64_t)q * top_k;
     int32_t *o_s = out_scores ? out_scores + (int64_t)q * top_k : nullptr;
     auto val = [&](int32_t t) { const int32_t v = c[t]; return v > clamp ? clamp : v; };
-    const bool from_list = min_hits >= 1 && n_cand[q] <= CAND_CAP;
-    if (skip_rows && !from_list) return;  // selected by the row_* kernels
+    if (!(min_hits >= 1 && n_cand[q] <= CAND_CAP)) return;  // a row query: the row_* kernels
     int32_t *s_id = (int32_t *)s_buf;
-
-    if (from_list) {
+    {
         const int32_t n = n_cand[q];
         const int32_t *list = cand + (int64_t)q * CAND_CAP;
         for (int32_t i = tid; i < n; i += SELECT_THREADS) s_id[i] = list[i];
@@ -367,74 +365,6 @@ phase_a_select_kernel(const int32_t *__restrict__ counts, int32_t num_db, int32_
             __syncthreads();
             if (tid == 0) { sh_run_eq += eq_tot; sh_run_sel += sel_tot; }
             __syncthreads();
-        }
-    } else {
-        radix_threshold(val, num_db, min_hits, top_k, top_shift, hist, sh);
-        const int32_t thr = sh[0], take_eq = top_k - sh[1];
-        const int warp = tid >> 5, lane = tid & 31;
-        constexpr int NW = SELECT_THREADS / 32;
-        const int32_t chunk = ((num_db + NW - 1) / NW + 31) & ~31;
-        const int32_t b0 = warp * chunk;
-        const int32_t b1 = min(num_db, b0 + chunk);
-        const uint32_t lt = (1u << lane) - 1u;
-        int32_t n_strict = 0, n_eq = 0;
-        for (int32_t base = b0; base < b1; base += 32 * SELECT_UNROLL) {
-            int32_t vv[SELECT_UNROLL];
-#pragma unroll
-            for (int u = 0; u < SELECT_UNROLL; ++u) {
-                const int32_t t = base + u * 32 + lane;
-                vv[u] = t < b1 ? val(t) : 0;
-            }
-#pragma unroll
-            for (int u = 0; u < SELECT_UNROLL; ++u) {
-                const int32_t t = base + u * 32 + lane;
-                const int32_t v = vv[u];
-                const bool surv = t < b1 && v >= min_hits;
-                n_strict += __popc(__ballot_sync(0xffffffffu, surv && (thr < 0 || v > thr)));
-                n_eq += __popc(__ballot_sync(0xffffffffu, surv && thr >= 0 && v == thr));
-            }
-        }
-        __shared__ int32_t w_strict[NW], w_eq[NW], w_eq_base[NW], w_out_base[NW];
-        if (lane == 0) { w_strict[warp] = n_strict; w_eq[warp] = n_eq; }
-        __syncthreads();
-        if (tid == 0) {
-            int32_t eq_acc = 0, out_acc = 0;
-            for (int w = 0; w < NW; ++w) {
-                w_eq_base[w] = eq_acc;
-                w_out_base[w] = out_acc;
-                int32_t take = take_eq - eq_acc;
-                take = take < 0 ? 0 : (take > w_eq[w] ? w_eq[w] : take);
-                eq_acc += w_eq[w];
-                out_acc += w_strict[w] + (thr >= 0 ? take : 0);
-            }
-        }
-        __syncthreads();
-        int32_t eq_seen = w_eq_base[warp], written = w_out_base[warp];
-        for (int32_t base = b0; base < b1; base += 32 * SELECT_UNROLL) {
-            int32_t vv[SELECT_UNROLL];
-#pragma unroll
-            for (int u = 0; u < SELECT_UNROLL; ++u) {
-                const int32_t t = base + u * 32 + lane;
-                vv[u] = t < b1 ? val(t) : 0;
-            }
-#pragma unroll
-            for (int u = 0; u < SELECT_UNROLL; ++u) {
-                const int32_t t = base + u * 32 + lane;
-                const int32_t v = vv[u];
-                const bool surv = t < b1 && v >= min_hits;
-                const bool strict = surv && (thr < 0 || v > thr);
-                const bool is_eq = surv && thr >= 0 && v == thr;
-                const uint32_t eq_b = __ballot_sync(0xffffffffu, is_eq);
-                const bool sel = strict || (is_eq && eq_seen + __popc(eq_b & lt) < take_eq);
-                const uint32_t sel_b = __ballot_sync(0xffffffffu, sel);
-                if (sel) {
-                    const int32_t at = written + __popc(sel_b & lt);
-                    o_t[at] = t;
-                    if (o_s) o_s[at] = v;
-                }
-                eq_seen += __popc(eq_b);
-                written += __popc(sel_b);
-            }
         }
     }
     const int32_t total = sh[2];
@@ -1147,7 +1077,7 @@ static int32_t select_rows(const int32_t *counts, int32_t nq, int32_t num_db, in
     CK_CUDA(cudaGetLastError());
     // queries whose candidate lists hold all their survivors
     phase_a_select_kernel<<<nq, SELECT_THREADS, 0, st>>>(counts, num_db, min_hits, top_k, clamp, top_shift, cand,
-                                                         n_cand, out_t, out_s, out_n, aux, 1);
+                                                         n_cand, out_t, out_s, out_n, aux);
     CK_CUDA(cudaGetLastError());
     if (!sort) return CK_OK;
     const size_t items = (size_t)nq * top_k;
