@@ -40,6 +40,38 @@ def test_library_exports_every_declared_symbol():
     assert lib.ck_version() >= 100
 
 
+def test_header_constants_match_bindings():
+    """Every CK_OK / CK_ERR_* status and CK_CFG_* key the header defines has
+    the same value in the Python bindings."""
+    from clustkit_gb300 import _lib
+    text = (REPO / "include" / "clustkit_gb300.h").read_text()
+    defs = dict((n, int(v)) for n, v in re.findall(r"^#define\s+(CK_(?:OK|ERR_[A-Z_]+|CFG_[A-Z_]+))\s+(\d+)",
+                                                  text, flags=re.M))
+    assert "CK_ERR_CAPACITY" in defs and "CK_CFG_WAVE_ROWS" in defs
+    for name, value in defs.items():
+        py = name if not name.startswith("CK_CFG_") else "CFG_" + name[len("CK_CFG_"):]
+        assert getattr(_lib, py) == value, name
+
+
+def test_search_scoring_modes():
+    """Scoring's modes as search_kmer_index's keywords select them, and every
+    mode can be captured in CUDA graphs (under a caller bound where one is
+    needed)."""
+    from clustkit_gb300.search import Scoring
+    exact = Scoring(2, 0)
+    similar = Scoring(2, 13)
+    phase_b = Scoring(2, 0, min_diag_hits=2)
+    c_path = Scoring(2, 0, min_diag_hits=2, use_c_scoring=True, use_c_sw=True)
+    assert not exact.similar and not exact.diagonal and not exact.hints
+    assert similar.similar and not similar.diagonal and not similar.hints
+    assert phase_b.diagonal and not phase_b.hints
+    assert c_path.diagonal and c_path.hints
+    # similar k-mers take precedence over the C scorer's settings
+    assert not Scoring(2, 13, use_c_scoring=True, use_c_sw=True).hints
+    assert all(s.graphable for s in (exact, similar, phase_b, c_path))
+    assert exact == Scoring(2, 0) and exact != similar
+
+
 def test_library_is_built_for_sm103a():
     from clustkit_gb300 import build
     assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
