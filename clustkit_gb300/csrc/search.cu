@@ -1138,7 +1138,8 @@ static int32_t phase_a_impl(void *pv) {
             unsigned long long *ticket = cursor + 1;
             const bool bounded = a.list_capacity >= 0;
             // unbounded: the list scratch as it stands (at least 1 Mi triples); a
-            // call that lists more grows it to the count and lists again
+            // call that lists more reads the count, grows the list past it and
+            // lists again.  bounded: the caller's capacity, no host read
             int64_t cap = bounded ? a.list_capacity
                                   : std::max<int64_t>((int64_t)(scratch_capacity(SLOT_SEARCH_TMP1) / 8), 1 << 20);
             uint64_t *list = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)std::max<int64_t>(cap, 1) * 8, &status);
