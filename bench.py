@@ -744,8 +744,15 @@ def run_search(args, n_db_fam=50000):
     if "similar" in modes:
         # clustkit's default scoring (BLOSUM62 similar 5-mers, threshold 13):
         # far more k-mer work per query, so the rates follow its batch rate
-        out["similar_kmers_thresh13"] = _measure_search_mode(db, qs[3000:], 13, None, n_plain=30, n_stage=10,
-                                                             n_batch=3, batches_only=args.search_batches_only)
+        similar = _measure_search_mode(db, qs[3000:], 13, None, n_plain=30, n_stage=10, n_batch=3,
+                                       batches_only=args.search_batches_only)
+        if not args.no_cpu and not args.search_batches_only:
+            try:
+                similar["cpu_baseline"] = search_cpu_baseline_similar(db, s, qs[3000:])
+                log(f"search similar 5-mers on the host cores: {similar['cpu_baseline']}")
+            except Exception as e:  # a baseline that fails leaves the GPU figures standing
+                similar["cpu_baseline_error"] = repr(e)
+        out["similar_kmers_thresh13"] = similar
     if "c_path" in modes:
         # clustkit's C path: exact 5-mers with Phase B (min_diag_hits 2, bin
         # 10, Phase-A top 10,000), SW at band 50 centred on the diagonal hints
@@ -830,6 +837,57 @@ def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
             "stage_s": {"kmer_scorer": ts, "sw": tsw, "rank": trank},
             "sample": f"{n} queries of the stream, {npairs} candidate pairs, {threads} threads, {tot:.1f}s",
             "source": "restatements of clustkit/csrc/kmer_score.c:195-470 and sw_align.c:25-266"}
+
+
+def _similar_chain(off, ent, fr, freq_thresh, s, sample, band, thresh=13, max_cands=500, top_k=10):
+    """One pass of the similar-5-mer search chain on the host cores: the
+    scorer's C restatement (OpenMP over queries), the C SW at the database
+    band (OpenMP over pairs), the rank; (total, scorer, sw, rank seconds,
+    candidate pairs)."""
+    import oracle
+    from oracle import search_oracle as so
+    from clustkit_gb300.blosum import BLOSUM62
+    lens = np.array([len(q) for q in sample], np.int32)
+    q_off = np.zeros(len(sample), np.int64)
+    q_off[1:] = np.cumsum(lens[:-1])
+    q_flat = np.concatenate(sample).astype(np.uint8)
+    flat = np.concatenate([s.flat, q_flat])
+    offs = np.concatenate([s.offsets, q_off + len(s.flat)])
+    all_lens = np.concatenate([s.lengths, lens])
+    t0 = time.perf_counter()
+    cands = oracle.similar_candidates_batch(q_flat, q_off, lens, BLOSUM62, thresh, off, ent, fr, freq_thresh, s.n,
+                                            2, max_cands)
+    t1 = time.perf_counter()
+    qi = np.concatenate([np.full(len(c[0]), i, np.int32) for i, c in enumerate(cands)])
+    tg = np.concatenate([c[0] for c in cands]).astype(np.int32)
+    pairs = np.stack([qi + s.n, tg], axis=1)
+    r = oracle.sw_batch(pairs, flat, offs, all_lens, band, BLOSUM62)
+    t2 = time.perf_counter()
+    keep = r["scores"] > 0
+    so.rank_hits(np.stack([qi, tg], axis=1)[keep], r["sims"][keep], r["scores"][keep], lens, s.lengths,
+                 len(sample), top_k)
+    t3 = time.perf_counter()
+    return t3 - t0, t1 - t0, t2 - t1, t3 - t2, len(pairs)
+
+
+def search_cpu_baseline_similar(db, s, qs, target_s: float = 10.0):
+    """clustkit's default search scoring on the host cores, as C restatements
+    (the port): the BLOSUM62 similar-5-mer scorer (kmer_index.py:1187-1328,
+    OpenMP over queries; clustkit runs it in Numba, absent here), the C SW at
+    the database band (sw_align.c, OpenMP over pairs) and the rank, on a sample
+    of the same queries; queries/s of the whole chain."""
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_num_threads(threads)
+    off, ent, fr = db.index_arrays()
+    n = 16
+    dt = _similar_chain(off, ent, fr, db.freq_thresh, s, qs[:n], db.band_width)[0]
+    n = int(min(len(qs), max(n, n * target_s / max(dt, 1e-3))))
+    tot, ts, tsw, trank, npairs = _similar_chain(off, ent, fr, db.freq_thresh, s, qs[:n], db.band_width)
+    return {"value": n / tot, "unit": "queries/s", "cores": threads, "kind": "port",
+            "stage_s": {"kmer_scorer": ts, "sw": tsw, "rank": trank},
+            "sample": f"{n} queries of the stream, {npairs} candidate pairs, {threads} threads, {tot:.1f}s",
+            "source": "restatements of clustkit/kmer_index.py:1187-1328 and csrc/sw_align.c:25-266"}
 
 
 def _batches_only(db, qs, thresh, n_batch, scoring):

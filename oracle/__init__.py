@@ -13,6 +13,9 @@ function (reference paths relative to the clustkit project root):
 * ``jaccard``   -- clustkit/pairwise.py:1564-1612 (merge-walk Jaccard);
 * ``kmer_candidates_batch`` -- clustkit/csrc/kmer_score.c:195-470 (the C
   k-mer scorer: Phase A, top-K, Phase B diagonal runs and hints), from
+  ``oracle/kmer_oracle.c``;
+* ``similar_candidates_batch`` -- clustkit/kmer_index.py:1187-1328 (the
+  BLOSUM62 similar-5-mer scorer, clustkit's default search scoring), from
   ``oracle/kmer_oracle.c``.
 
 ``ref_sw_batch`` calls the reference's own sw_align.c, compiled from source
@@ -53,6 +56,10 @@ def _load():
                                            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P, _P]
         lib.or_set_num_threads.restype = None
+        lib.or_similar_candidates.restype = None
+        lib.or_similar_candidates.argtypes = [_P, _P, _P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P, _P,
+                                              ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                              _P, _P, _P]
         lib.or_set_num_threads.argtypes = [ctypes.c_int32]
         lib.or_max_threads.restype = ctypes.c_int32
         lib.or_fmix64_export.restype = ctypes.c_uint64
@@ -118,6 +125,28 @@ def kmer_candidates_batch(q_flat, q_offsets, q_lengths, k, alpha, kmer_offsets, 
                            int(min_total_hits), int(min_diag_hits), int(diag_bin_width), mc, int(phase_a_topk),
                            t.ctypes.data, s.ctypes.data, d.ctypes.data, n.ctypes.data)
     return [(t[i, :n[i]].copy(), s[i, :n[i]].copy(), d[i, :n[i]].copy()) for i in range(nq)]
+
+
+def similar_candidates_batch(q_flat, q_offsets, q_lengths, sub, thresh, kmer_offsets, kmer_entries, kmer_freqs,
+                             freq_thresh, num_db, min_total_hits, max_cands):
+    """Per query (ids, scores) of the similar-5-mer scorer's restatement
+    (k = 5 index over 20 codes), all queries in one OpenMP call."""
+    lib = _load()
+    q_flat = _c(q_flat if len(q_flat) else np.zeros(1, np.uint8), np.uint8)
+    q_offsets, q_lengths = _c(q_offsets, np.int64), _c(q_lengths, np.int32)
+    off, ent, fr = _c(kmer_offsets, np.int64), _c(kmer_entries, np.int64), _c(kmer_freqs, np.int32)
+    S = _c(np.asarray(sub).reshape(-1), np.int8)
+    if int(thresh) < 1:
+        raise ValueError("the similar-k-mer threshold must be >= 1")
+    nq = len(q_lengths)
+    mc = int(max_cands)
+    t = np.zeros((max(nq, 1), mc), np.int32)
+    s = np.zeros_like(t)
+    n = np.zeros(max(nq, 1), np.int32)
+    lib.or_similar_candidates(q_flat.ctypes.data, q_offsets.ctypes.data, q_lengths.ctypes.data, nq, S.ctypes.data,
+                              int(thresh), off.ctypes.data, ent.ctypes.data, fr.ctypes.data, int(freq_thresh),
+                              int(num_db), int(min_total_hits), mc, t.ctypes.data, s.ctypes.data, n.ctypes.data)
+    return [(t[i, :n[i]].copy(), s[i, :n[i]].copy()) for i in range(nq)]
 
 
 def sketches(flat, offsets, lengths, k, s, alphabet=20, seed=42):

@@ -7,6 +7,8 @@
  *
  *   or_kmer_candidates   clustkit/csrc/kmer_score.c:195-470
  *                        (score_query_full, batch_score_queries_c)
+ *   or_similar_candidates clustkit/kmer_index.py:1187-1328
+ *                        (_score_query_similar_k5: BLOSUM62 similar 5-mers)
  *
  * Per query: Phase A counts the hits of every valid k-mer (all codes below
  * alpha) whose frequency is at most freq_thresh, per database sequence,
@@ -175,5 +177,99 @@ void or_kmer_candidates(const uint8_t *q_flat, const int64_t *q_offsets, const i
         free(dg);
         free(tmp);
         free(hits);
+    }
+}
+
+/* clustkit's similar-k-mer scoring (k = 5, alphabet 20): for every query
+ * 5-mer of codes below 20, every 5-mer whose column-sum score under sub
+ * (int8 [20][20], row = query residue) reaches T, and whose frequency is in
+ * (0, freq_thresh], adds that score to each target of its posting list.
+ * The neighbours are enumerated by branch and bound on the best remaining
+ * row scores (the same set as a full scan).  Survivors have a sum of at
+ * least min_total_hits (every target when it is <= 0); written in id order
+ * when at most max_cands, else the best max_cands by (score desc, id asc) in
+ * that order.  T >= 1 (as clustkit's threshold), so a touched target's sum
+ * is positive.  Sums in int64 (written as int32).  OpenMP over queries. */
+void or_similar_candidates(const uint8_t *q_flat, const int64_t *q_offsets, const int32_t *q_lengths, int32_t nq,
+                           const int8_t *sub, int32_t T, const int64_t *kmer_offsets, const int64_t *kmer_entries,
+                           const int32_t *kmer_freqs, int32_t freq_thresh, int32_t num_db, int32_t min_total_hits,
+                           int32_t max_cands, int32_t *out_targets, int32_t *out_scores, int32_t *out_n) {
+    int32_t S[400], mx[20];
+    for (int i = 0; i < 400; ++i) S[i] = sub[i];
+    for (int a = 0; a < 20; ++a) {
+        int32_t m = S[a * 20];
+        for (int b = 1; b < 20; ++b) m = S[a * 20 + b] > m ? S[a * 20 + b] : m;
+        mx[a] = m;
+    }
+#pragma omp parallel
+    {
+        int64_t *counts = (int64_t *)calloc((size_t)num_db + 1, 8);
+        int32_t *touched = (int32_t *)malloc(((size_t)num_db + 1) * 4);
+        int32_t *ids = (int32_t *)malloc(((size_t)num_db + 1) * 4);
+        int32_t *sc = (int32_t *)malloc(((size_t)num_db + 1) * 4);
+        uint64_t *tmp = (uint64_t *)malloc(((size_t)num_db + 1) * 8);
+#pragma omp for schedule(dynamic, 1)
+        for (int32_t qi = 0; qi < nq; ++qi) {
+            const uint8_t *s = q_flat + q_offsets[qi];
+            const int32_t L = q_lengths[qi];
+            int32_t nt = 0;
+            for (int32_t p = 0; p + 5 <= L; ++p) {
+                const int32_t q0 = s[p], q1 = s[p + 1], q2 = s[p + 2], q3 = s[p + 3], q4 = s[p + 4];
+                if (q0 >= 20 || q1 >= 20 || q2 >= 20 || q3 >= 20 || q4 >= 20) continue;
+                const int32_t m4 = mx[q4], m34 = mx[q3] + m4, m234 = mx[q2] + m34, m1234 = mx[q1] + m234;
+                for (int32_t a0 = 0; a0 < 20; ++a0) {
+                    const int32_t s0 = S[q0 * 20 + a0];
+                    if (s0 + m1234 < T) continue;
+                    for (int32_t a1 = 0; a1 < 20; ++a1) {
+                        const int32_t s1 = s0 + S[q1 * 20 + a1];
+                        if (s1 + m234 < T) continue;
+                        for (int32_t a2 = 0; a2 < 20; ++a2) {
+                            const int32_t s2 = s1 + S[q2 * 20 + a2];
+                            if (s2 + m34 < T) continue;
+                            for (int32_t a3 = 0; a3 < 20; ++a3) {
+                                const int32_t s3 = s2 + S[q3 * 20 + a3];
+                                if (s3 + m4 < T) continue;
+                                for (int32_t a4 = 0; a4 < 20; ++a4) {
+                                    const int32_t s4 = s3 + S[q4 * 20 + a4];
+                                    if (s4 < T) continue;
+                                    const int32_t v = (((a0 * 20 + a1) * 20 + a2) * 20 + a3) * 20 + a4;
+                                    const int32_t f = kmer_freqs[v];
+                                    if (f == 0 || f > freq_thresh) continue;
+                                    for (int64_t h = kmer_offsets[v]; h < kmer_offsets[v + 1]; ++h) {
+                                        const int32_t t = (int32_t)(kmer_entries[h] >> 32);
+                                        if (counts[t] == 0) touched[nt++] = t;
+                                        counts[t] += s4;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            int32_t n = 0;
+            if (min_total_hits <= 0) {
+                for (int32_t t = 0; t < num_db; ++t) { ids[n] = t; sc[n] = (int32_t)counts[t]; ++n; }
+            } else {
+                qsort(touched, (size_t)nt, 4, cmp_i32);
+                for (int32_t i = 0; i < nt; ++i)
+                    if (counts[touched[i]] >= min_total_hits) {
+                        ids[n] = touched[i];
+                        sc[n] = (int32_t)counts[touched[i]];
+                        ++n;
+                    }
+            }
+            for (int32_t i = 0; i < nt; ++i) counts[touched[i]] = 0;
+            n = top_by_score(ids, sc, NULL, n, max_cands, tmp);
+            out_n[qi] = n;
+            if (n > 0) {
+                memcpy(out_targets + (int64_t)qi * max_cands, ids, (size_t)n * 4);
+                memcpy(out_scores + (int64_t)qi * max_cands, sc, (size_t)n * 4);
+            }
+        }
+        free(counts);
+        free(touched);
+        free(ids);
+        free(sc);
+        free(tmp);
     }
 }

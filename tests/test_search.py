@@ -277,6 +277,40 @@ def test_oracle_similar_phase_a_matches_reference(golden):
         assert np.array_equal(sc, g[f"q{qi}_sim_scores"]), qi
 
 
+def test_c_oracle_similar_matches_reference_and_numpy(golden):
+    """The C restatement of the similar-5-mer scorer (the host-core baseline
+    of that search mode) against the reference's own _score_query_similar_k5
+    (golden), and against the numpy restatement with binding caps at
+    thresholds 11/13/15."""
+    import oracle
+    g = golden("search_golden.npz")
+    off, ent, fr = _ref_index(g)
+    qs = _queries(g)
+    sq = [qs[i] for i in g["sim_queries"]]
+    nd = len(g["db_lengths"])
+
+    def flat(queries):
+        lens = np.array([len(q) for q in queries], np.int32)
+        return np.concatenate(queries).astype(np.uint8), np.concatenate([[0], np.cumsum(lens[:-1])]), lens
+
+    got = oracle.similar_candidates_batch(*flat(sq), BLOSUM62, 13, off, ent, fr, int(g["freq_thresh"]), nd, 2, nd)
+    for (ids, sc), qi in zip(got, g["sim_queries"]):
+        assert np.array_equal(ids, g[f"q{qi}_sim_ids"]), qi
+        assert np.array_equal(sc, g[f"q{qi}_sim_scores"]), qi
+    db_set = synth.generate_families(120, 6, median=150, lo=40, hi=400, seed=21)
+    off, ent, fr = so.build_kmer_index(db_set.flat, db_set.offsets, db_set.lengths, 5)
+    rng = np.random.default_rng(22)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 4, replace=False)]
+    qs += [synth.random_sequences(1, median=100, lo=60, hi=160, seed=23).seq(0).copy()]
+    freq_thresh = int(fr.max())
+    for thresh, cap in ((11, 40), (13, 7), (15, 300)):
+        got = oracle.similar_candidates_batch(*flat(qs), BLOSUM62, thresh, off, ent, fr, freq_thresh, db_set.n, 2,
+                                              cap)
+        for q, (ids, sc) in zip(qs, got):
+            want = so.phase_a_similar(q, off, ent, fr, freq_thresh, db_set.n, 2, cap, BLOSUM62, thresh)
+            assert np.array_equal(ids, want[0]) and np.array_equal(sc, want[1]), (thresh, cap)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("compact", [True, False])
 def test_similar_phase_a_and_search_match_reference(ck, golden, compact):
