@@ -47,9 +47,12 @@ WORKLOAD = {"workload": "align-50k: 5000 families x 10, median 350 [30,2000], k=
             "n_sequences": 50000, "threshold": THRESHOLD, "band_width": BAND_WIDTH,
             "l2": "flushed between timed steps (256 MiB write, outside the step events)"}
 OPS_PER_CELL = 6  # max-plus lane ops of the score recurrence: E, F: viaddmax+add; H: vimax3+add
-# dram__bytes_read.sum + dram__bytes_write.sum of one strip-kernel launch on this
-# workload, measured by an ncu --set full capture of the first timed launch
-STRIP_DRAM_BYTES_PER_LAUNCH = 23.566195e9 + 26.841081e9
+# DRAM traffic of the strip kernel: dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch on this workload from an ncu capture (the profile named here), per DP
+# cell of that launch; a run reports it scaled to its own cells and says so
+STRIP_PROFILE = "profiles/sw_strip_kernel_align50k.md"
+STRIP_PROFILE_CELLS = 46_229_358_568
+STRIP_DRAM_BYTES_PER_CELL = (23.566195e9 + 26.841081e9) / STRIP_PROFILE_CELLS
 
 
 def log(*a):
@@ -211,7 +214,7 @@ def reference_gpu_baseline(s, pairs, d_flat, d_off, d_len, stream, n_sample: int
             "source": "clustkit/pairwise.py:1215-1402 kernel + :1480-1547 batching (CuPy not installed)"}
 
 
-def hbm_check(s, pairs, kernel_s):
+def hbm_check(s, pairs, kernel_s, cells):
     """Why the bound is integer issue and not HBM: the strip kernel's
     algorithmic bytes (both sequences, the pair, two offsets, two lengths and
     the 17 output bytes per pair) and its measured DRAM traffic (ncu, the
@@ -225,46 +228,83 @@ def hbm_check(s, pairs, kernel_s):
     except (OSError, ValueError, KeyError):
         peak, basis = 6800.0, "of fallback"
     alg_gbs = alg / kernel_s / 1e9
-    dram_gbs = STRIP_DRAM_BYTES_PER_LAUNCH / kernel_s / 1e9
-    return {"algorithmic_bytes": alg, "algorithmic_gbs": alg_gbs, "dram_gbs_ncu": dram_gbs, "peak_gbs": peak,
-            "frac_algorithmic": alg_gbs / peak, "frac_dram": dram_gbs / peak, "peak_basis": basis}
+    dram_gbs = STRIP_DRAM_BYTES_PER_CELL * cells / kernel_s / 1e9
+    return {"algorithmic_bytes": alg, "algorithmic_gbs": alg_gbs, "dram_gbs_from_profile": dram_gbs,
+            "peak_gbs": peak, "frac_algorithmic": alg_gbs / peak, "frac_dram": dram_gbs / peak, "peak_basis": basis,
+            "dram_source": f"ncu DRAM bytes per cell from {STRIP_PROFILE} x this run's cells / this run's "
+                           f"kernel time"}
 
 
-def cpu_baseline(s, pairs, target_s: float = 12.0, use_ref: bool = True):
+def same_as_oracle(res, ref, threshold=None) -> bool:
+    """Every pair's score, identity numerator and denominator and float32
+    identity (bit pattern) equal the oracle's; with a threshold, also the
+    pass/fail mask under the C path's rule (sims >= t, clustkit/pairwise.py:107)."""
+    ok = all(np.array_equal(np.asarray(res[k]), ref[k]) for k in ("scores", "matches", "shorter"))
+    ok = ok and np.array_equal(np.asarray(res["sims"]).view(np.uint32), ref["sims"].view(np.uint32))
+    if threshold is not None:
+        ok = ok and np.array_equal(np.asarray(res["mask"]).astype(bool), ref["sims"] >= np.float32(threshold))
+    return bool(ok)
+
+
+def cpu_baseline(s, pairs, use_ref: bool = True):
+    """clustkit's CPU algorithm on every pair of the workload, on all host
+    cores: the host-core baseline (GCUPS over the whole pair list, ~15 s on
+    16 cores) and, from the same run, the oracle outputs that every GPU result
+    of the step is checked against.  Plus one thread on a ~3 s slice."""
     import oracle
     from clustkit_gb300.blosum import BLOSUM62
     from clustkit_gb300.cells import pair_cells
     threads = os.cpu_count() or 1
     kind = "reference" if (use_ref and oracle.ref_available()) else "port"
+    oracle.set_num_threads(threads)
+    t = time.perf_counter()
+    ref = oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+    dt_port = time.perf_counter() - t
+    cells = int(pair_cells(pairs, s.lengths, BAND_WIDTH).sum())
+    dt = dt_port
+    if kind == "reference":
+        t = time.perf_counter()
+        oracle.ref_sw_batch(pairs, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=threads)
+        dt = time.perf_counter() - t
     rng = np.random.default_rng(0)
     sample = pairs[rng.permutation(len(pairs))]
-
-    def run(p, nt=threads):
-        t = time.perf_counter()
-        if kind == "reference":
-            oracle.ref_sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=nt)
-        else:
-            oracle.set_num_threads(nt)
-            oracle.sw_batch(p, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
-        return time.perf_counter() - t
-
-    n = min(len(sample), 2000)
-    dt = run(sample[:n])
-    n = int(min(len(sample), max(n, n * target_s / max(dt, 1e-3))))
-    p = sample[:n]
-    dt = run(p)
-    cells = int(pair_cells(p, s.lengths, BAND_WIDTH).sum())
-    # one thread, on a ~3 s slice of the same sample
-    n1 = max(50, int(n * 3.0 / max(dt * threads, 1e-3)))
+    # one thread, on a ~3 s slice of the pairs in random order
+    n1 = int(min(len(pairs), max(50, len(pairs) * 3.0 / max(dt_port * threads, 1e-3))))
     p1 = sample[:n1]
-    dt1 = run(p1, 1)
+    oracle.set_num_threads(1)
+    t = time.perf_counter()
+    if kind == "reference":
+        oracle.ref_sw_batch(p1, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62, n_threads=1)
+    else:
+        oracle.sw_batch(p1, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+    dt1 = time.perf_counter() - t
     cells1 = int(pair_cells(p1, s.lengths, BAND_WIDTH).sum())
     oracle.set_num_threads(threads)
-    return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
-            "pairs_per_s": n / dt,
-            "sample": f"{n} random pairs of the workload ({cells} cells), {threads} threads, {dt:.1f}s",
+    base = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
+            "pairs_per_s": len(pairs) / dt,
+            "sample": f"every pair of the workload ({len(pairs)} pairs, {cells} cells), {threads} threads, "
+                      f"{dt:.1f}s",
             "single_thread": {"value": cells1 / dt1 / 1e9, "unit": "GCUPS", "pairs_per_s": n1 / dt1,
-                              "sample": f"{n1} pairs ({cells1} cells), 1 thread, {dt1:.1f}s"}}
+                              "sample": f"{n1} random pairs ({cells1} cells), 1 thread, {dt1:.1f}s"}}
+    return base, ref
+
+
+def oracle_on_sample(s, pairs, band_width, n, seed, results=None, hints=None):
+    """The oracle (all host threads) on a random sample of n pairs; with
+    results (this engine's outputs for every pair), whether they agree."""
+    import oracle
+    from clustkit_gb300.blosum import BLOSUM62
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(len(pairs), size=min(n, len(pairs)), replace=False))
+    oracle.set_num_threads(os.cpu_count() or 1)
+    t = time.perf_counter()
+    ref = oracle.sw_batch(pairs[idx], s.flat, s.offsets, s.lengths, band_width, BLOSUM62,
+                          diag_hints=None if hints is None else hints[idx])
+    dt = time.perf_counter() - t
+    out = {"pairs": int(len(idx)), "oracle_s": round(dt, 2)}
+    if results is not None:
+        out["bit_exact"] = same_as_oracle({k: np.asarray(v)[idx] for k, v in results.items()}, ref)
+    return out, idx, ref
 
 
 # ----------------------------------------------------------------------------- arms
@@ -333,6 +373,8 @@ def run_ours(args, world, rank, local):
         _lib.set_config(_lib.CFG_ROWS_PER_STRIP, args.rows)
     if args.variant >= 0:
         _lib.set_config(_lib.CFG_STRIP_VARIANT, args.variant)
+    if args.ctas:
+        _lib.set_config(_lib.CFG_CTAS_PER_SM, args.ctas)
     s, pairs, n_cand = build_workload(use_gpu=True, quick=args.quick)
     pairs = shard(pairs, world, rank)
     M = len(pairs)
@@ -392,15 +434,17 @@ def run_ours(args, world, rank, local):
     res_b = {k: v.cpu().numpy() for k, v in out.items()}
     sweep = {}
     if args.sweep:
-        keep = (_lib.get_config(_lib.CFG_ROWS_PER_STRIP), _lib.get_config(_lib.CFG_STRIP_VARIANT))
-        for rows in (8, 16, 24):
-            for var in range(4):
-                _lib.set_config(_lib.CFG_ROWS_PER_STRIP, rows)
-                _lib.set_config(_lib.CFG_STRIP_VARIANT, var)
-                t_r, _ = timed(ENGINE_BATCHED, 3, 1)
-                sweep[f"R{rows}_V{var}"] = round(cells / (t_r / 3) / 1e9, 1)
-        _lib.set_config(_lib.CFG_ROWS_PER_STRIP, keep[0])
-        _lib.set_config(_lib.CFG_STRIP_VARIANT, keep[1])
+        keys = (_lib.CFG_ROWS_PER_STRIP, _lib.CFG_STRIP_VARIANT, _lib.CFG_CTAS_PER_SM)
+        keep = [_lib.get_config(k) for k in keys]
+        for rows in (8, 16, 24, 32):
+            for ctas in ((2, 1) if rows <= 16 else (1,)):
+                for var in range(4):
+                    for k, v in zip(keys, (rows, var, ctas)):
+                        _lib.set_config(k, v)
+                    t_r, _ = timed(ENGINE_BATCHED, 3, 1)
+                    sweep[f"R{rows}_V{var}_C{ctas}"] = round(cells / (t_r / 3) / 1e9, 1)
+        for k, v in zip(keys, keep):
+            _lib.set_config(k, v)
     # ---- plain engine (the plain GPU form), same pairs
     plain_steps = max(1, min(args.steps, 3))
     lib.ck_sw_profile(1)
@@ -410,13 +454,6 @@ def run_ours(args, world, rank, local):
     res_p = {k: v.cpu().numpy() for k, v in out.items()}
     engines_agree = all(np.array_equal(res_b[k], res_p[k]) for k in res_b)
 
-    # ---- parity against the oracle on a sample
-    import oracle
-    rng = np.random.default_rng(7)
-    samp = rng.choice(M, size=min(M, 3000), replace=False)
-    ref = oracle.sw_batch(pairs[samp], s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
-    oracle_ok = all(np.array_equal(res_b[k][samp], ref[k]) for k in ("scores", "matches", "shorter")) \
-        and np.array_equal(res_b["sims"][samp], ref["sims"])
 
     # ---- e2e through the host-buffer C entry point, pinned host memory
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -456,10 +493,25 @@ def run_ours(args, world, rank, local):
         rates[name] = float(peak[0])
     # the recurrence's max-plus ops are DPX instructions: their measured rate is the roof
     p_int32 = rates["viaddmax_s32"]
+    # cell arithmetic alone, in the exact int32 form and two int16x2 forms
+    cell_forms = {}
+    for form, name in ((0, "int32_exact_key"), (1, "int16x2_score_only"), (2, "int16x2_match_select")):
+        _lib.check(lib.ck_probe_cell_rate(form, peak.ctypes.data))
+        cell_forms[name] = float(peak[0]) / 1e9
     kernel_s = float(np.mean(kt)) / 1e3 if kt and min(kt) > 0 else t_batched / args.steps
     gcups_kernel = cells / kernel_s / 1e9
     achieved = gcups_kernel * OPS_PER_CELL  # Gop/s
-    cpu = cpu_baseline(s, pairs) if (rank == 0 and not args.no_cpu) else None
+    # ---- clustkit's CPU algorithm on every pair: the host-core baseline and the
+    # oracle every GPU output of the step is compared with (--no-cpu: a 3,000-pair
+    # sample instead, for quick runs)
+    if rank == 0 and not args.no_cpu:
+        cpu, ref_all = cpu_baseline(s, pairs)
+        parity = {"vs_oracle_all_pairs": same_as_oracle(res_b, ref_all, THRESHOLD), "oracle_pairs": int(M)}
+        del ref_all
+    else:
+        cpu = None
+        chk, _, _ = oracle_on_sample(s, pairs, BAND_WIDTH, 3000, 7, res_b)
+        parity = {"vs_oracle_sample": chk["bit_exact"], "oracle_pairs": chk["pairs"]}
     gpu_ref = (reference_gpu_baseline(s, pairs, d_flat, d_off, d_len, stream)
                if (rank == 0 and not args.no_cpu) else None)
 
@@ -476,22 +528,24 @@ def run_ours(args, world, rank, local):
                   "pairs_per_s": world * M / t_plain * plain_steps,
                   "kernel_ms": float(np.mean(kt_plain)) if kt_plain else None, "steps": plain_steps},
         "speedup_vs_plain": (cells / (t_batched / args.steps)) / (cells / (t_plain / plain_steps)),
-        "bit_exact": {"batched_vs_plain_all_pairs": bool(engines_agree),
-                      "vs_oracle_sample": bool(oracle_ok), "e2e_vs_device": bool(e2e_ok),
-                      "oracle_sample_pairs": int(len(samp))},
+        "bit_exact": {"batched_vs_plain_all_pairs": bool(engines_agree), "e2e_vs_device": bool(e2e_ok),
+                      **parity},
         "e2e": {"value": world * cells / e2e_t * args.steps / 1e9, "unit": "GCUPS",
                 "pairs_per_s": world * M / e2e_t * args.steps,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "api": "ck_sw_batch (host buffers, pinned)"},
         "roofline": {"bound": "int", "achieved": achieved, "peak": p_int32 / 1e9, "unit": "Gop/s",
-                     "frac": achieved / (p_int32 / 1e9), "traffic": STRIP_DRAM_BYTES_PER_LAUNCH,
+                     "frac": achieved / (p_int32 / 1e9), "traffic": STRIP_DRAM_BYTES_PER_CELL * cells,
+                     "traffic_source": f"not measured in this run: ncu DRAM bytes per cell from {STRIP_PROFILE} "
+                                       f"x this run's {cells} cells (same workload, same kernel settings)",
                      "basis": f"{OPS_PER_CELL} int32 max-plus lane-ops per cell x cells / strip-kernel "
                               f"event time; peak = measured int32 DPX/ALU lane-op rate (in-repo probe)",
                      "kernel": "sw_strip_kernel", "kernel_ms": kernel_s * 1e3,
                      "gcups_kernel": gcups_kernel, "gcups_roof": p_int32 / 1e9 / OPS_PER_CELL,
                      "probe_gops": {k: v / 1e9 for k, v in rates.items()},
                      "frac_of_int16x2_roof": gcups_kernel / (rates["viaddmax_s16x2"] / 1e9 / OPS_PER_CELL),
-                     "hbm_check": hbm_check(s, pairs, kernel_s)},
+                     "cell_form_probe_gcups": cell_forms,
+                     "hbm_check": hbm_check(s, pairs, kernel_s, cells)},
         "cpu_baseline": cpu,
         "reference_cupy_path": gpu_ref,
         "rows_per_strip": _lib.get_config(_lib.CFG_ROWS_PER_STRIP),
@@ -502,7 +556,7 @@ def run_ours(args, world, rank, local):
     }
     if rank == 0 and (args.million == "on" or (args.million == "auto" and not args.quick)):
         try:
-            line["million"] = run_million(args)
+            line["million"] = run_million(args, p_int32)
         except Exception as e:
             line["million"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and (args.uneven == "on" or (args.uneven == "auto" and not args.quick)):
@@ -548,17 +602,22 @@ def run_uneven(args):
         tune.apply(tune.DEFAULT)
         same = all(np.array_equal(tuned[k], plain[k]) for k in ("scores", "matches", "shorter", "mask"))
         g = lambda ms: res.cells / (ms * 1e-3) / 1e9
+        # the tuned engine's outputs against the oracle on a random sample of the pairs
+        vs_oracle = None
+        if not args.no_cpu:
+            vs_oracle, _, _ = oracle_on_sample(s, pairs, bw, 250_000 if not args.quick else 20_000, bw, tuned)
         out["by_band"][str(bw)] = {"cells": res.cells, "gcups_default": g(ms_default), "gcups_tuned": g(ms_tuned),
                                    "gcups_plain": g(ms_plain), "tuned_vs_plain": ms_plain / ms_tuned,
-                                   "config": res.config, "wave_pairs": wave, "trials": len(res.trials),
-                                   "bit_exact_vs_plain": bool(same)}
+                                   "config": res.config, "confirm": res.confirm, "wave_pairs": wave,
+                                   "trials": len(res.trials), "bit_exact_vs_plain": bool(same),
+                                   "vs_oracle_sample": vs_oracle}
         log(f"uneven bw={bw}: {out['by_band'][str(bw)]}")
         del call
     return out
 
 
 # ----------------------------------------------------------------------------- 1M-sequence streaming
-def run_million(args):
+def run_million(args, int_peak=None):
     """1,000,000 sequences (100,000 families x 10, median 300, 30..1500), t = 0.4:
     sketches on the GPU, LSH on the GPU, the Jaccard pre-filter on the GPU, then
     every surviving pair through the batched SW engine in device-resident
@@ -679,6 +738,35 @@ def run_million(args):
         graph_ms = ga.elapsed_time(gb)
         del g
         lib.ck_ctx_destroy(ctx)
+    # every output of a random sample of the streamed pairs against the oracle: the
+    # stream runs once more (untimed) and the sampled pairs' results are gathered
+    # from each chunk's outputs
+    vs_oracle = None
+    if not args.no_cpu and M:
+        import oracle
+        rng = np.random.default_rng(4)
+        idx = np.sort(rng.choice(M, size=min(M, 100_000 if args.quick else 2_000_000), replace=False))
+        samp_pairs = pairs[T(idx)].cpu().numpy()
+        got = {k: np.empty(len(idx), dt) for k, dt in (("sims", np.float32), ("scores", np.int32),
+                                                       ("matches", np.int32), ("shorter", np.int32))}
+        for c0 in range(0, M, chunk):
+            m = min(chunk, M - c0)
+            _lib.check(lib.ck_sw_batch_device(
+                pairs[c0:].data_ptr(), m, d_flat.data_ptr(), len(s.flat), d_off.data_ptr(), d_len.data_ptr(),
+                s.n, BAND_WIDTH, sub.ctypes.data, THRESHOLD_MILLION, None, PASS_CPU, ENGINE_BATCHED,
+                outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(), outs[3].data_ptr(), outs[4].data_ptr(),
+                stream.cuda_stream))
+            sel = (idx >= c0) & (idx < c0 + m)
+            loc = T(idx[sel] - c0)
+            for k, o in zip(("sims", "scores", "matches", "shorter"), outs):
+                got[k][sel] = o[loc].cpu().numpy()
+        oracle.set_num_threads(os.cpu_count() or 1)
+        t_o = time.perf_counter()
+        ref = oracle.sw_batch(samp_pairs, s.flat, s.offsets, s.lengths, BAND_WIDTH, BLOSUM62)
+        vs_oracle = {"pairs": int(len(idx)), "bit_exact": same_as_oracle(got, ref),
+                     "oracle_s": round(time.perf_counter() - t_o, 2)}
+        del ref, got, samp_pairs
+    peak = int_peak if int_peak else None
     out = {"workload": f"million: {s.n} seqs ({n_fam} families x 10, median 300, 30..1500), t={THRESHOLD_MILLION}, "
                        f"k=5 s=128, LSH b={lp['num_bands']} L={lp['num_tables']}, Jaccard floor {floor:.6f}, "
                        f"bw={BAND_WIDTH}",
@@ -687,9 +775,14 @@ def run_million(args):
            "sw_ms": sw_ms, "gcups": gcups, "pairs_per_s": M / (sw_ms * 1e-3), "chunk_pairs": chunk,
            "sw_ms_graph_replay": graph_ms,
            "gcups_graph_replay": cells / (graph_ms * 1e-3) / 1e9 if graph_ms else None,
-           "roofline_frac": gcups * 1e9 * 6 / 20.06e12,
-           "hbm_gbs_est": gcups * 1.08,
-           "hbm_basis": "1.08 DRAM bytes per cell, the strip kernel's measured traffic on the 50k set"}
+           "roofline_frac": gcups * 1e9 * OPS_PER_CELL / peak if peak else None,
+           "roofline_peak_gops": peak / 1e9 if peak else None,
+           "roofline_basis": "SW-stream GCUPS x 6 ops per cell / the int32 DPX lane-op rate measured by the "
+                             "in-library probe in this run",
+           "hbm_gbs_est": gcups * STRIP_DRAM_BYTES_PER_CELL,
+           "hbm_basis": f"not measured in this run: {STRIP_DRAM_BYTES_PER_CELL:.3f} DRAM bytes per cell from "
+                        f"{STRIP_PROFILE} (ncu, the strip kernel on the 50k set) x this run's GCUPS",
+           "vs_oracle_sample": vs_oracle}
     log(f"million: {out}")
     return out
 
@@ -739,6 +832,12 @@ def run_search(args, n_db_fam=50000):
     if "exact" in modes:
         exact = _measure_search_mode(db, qs, 0, (100, 1000, 3000, 10000, 20000), n_plain=300, n_stage=50,
                                      n_batch=5, batches_only=args.search_batches_only)
+        if not args.no_cpu and not args.search_batches_only:
+            try:
+                exact["cpu_baseline"] = search_cpu_baseline(db, s, qs, mode="exact")
+                log(f"search exact 5-mers on the host cores: {exact['cpu_baseline']}")
+            except Exception as e:  # a baseline that fails leaves the GPU figures standing
+                exact["cpu_baseline_error"] = repr(e)
         out.update({"slots": exact.pop("slots", None), "kmer_scoring": "exact 5-mers (kmer_score_thresh 0)",
                     **exact})
     if "similar" in modes:
@@ -791,12 +890,16 @@ def search_summary(out):
     return summ
 
 
-def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
-    """clustkit's C search path on the host cores, as C restatements (the port):
-    the C k-mer scorer (kmer_score.c, Phase A + Phase B + hints, OpenMP over
-    queries), the C SW at band 50 centred on the hints (sw_align.c, OpenMP over
-    pairs) and the rank, on a sample of the same queries; queries/s of the
-    whole chain with the index resident in host memory."""
+def search_cpu_baseline(db, s, qs, target_s: float = 10.0, mode: str = "c_path"):
+    """A search chain of clustkit's on the host cores, as C restatements (the
+    port), on a sample of the same queries; queries/s of the whole chain with
+    the index resident in host memory.
+      mode "c_path": the C k-mer scorer (kmer_score.c, Phase A + Phase B +
+        hints, OpenMP over queries), the C SW at band 50 centred on the hints;
+      mode "exact": the same scorer with Phase B off -- exact 5-mer hit
+        counts, at least 2 hits, the top 500 (kmer_index.py:470-534) -- and
+        the C SW at the database band, unhinted (kmer_index.py:2226-2311);
+    both followed by the rank (sw_align.c over pairs, OpenMP)."""
     import oracle
     from oracle import search_oracle as so
     from clustkit_gb300.blosum import BLOSUM62
@@ -804,6 +907,8 @@ def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
     oracle.set_num_threads(threads)
     off, ent, fr = db.index_arrays()
     mc, topk = 500, 10000
+    exact = mode == "exact"
+    min_diag, band = (0, db.band_width) if exact else (2, 50)
 
     def run(sample):
         lens = np.array([len(q) for q in sample], np.int32)
@@ -815,13 +920,13 @@ def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
         all_lens = np.concatenate([s.lengths, lens])
         t0 = time.perf_counter()
         cands = oracle.kmer_candidates_batch(q_flat, q_off, lens, 5, 20, off, ent, fr, db.freq_thresh, s.n,
-                                             2, 2, 10, mc, topk)
+                                             2, min_diag, 10, mc, topk)
         t1 = time.perf_counter()
         qi = np.concatenate([np.full(len(c[0]), i, np.int32) for i, c in enumerate(cands)])
         tg = np.concatenate([c[0] for c in cands]).astype(np.int32)
-        hints = np.concatenate([c[2] for c in cands]).astype(np.int32)
+        hints = None if exact else np.concatenate([c[2] for c in cands]).astype(np.int32)
         pairs = np.stack([qi + s.n, tg], axis=1)
-        r = oracle.sw_batch(pairs, flat, offs, all_lens, 50, BLOSUM62, diag_hints=hints)
+        r = oracle.sw_batch(pairs, flat, offs, all_lens, band, BLOSUM62, diag_hints=hints)
         t2 = time.perf_counter()
         keep = r["scores"] > 0
         so.rank_hits(np.stack([qi, tg], axis=1)[keep], r["sims"][keep], r["scores"][keep], lens, s.lengths,
@@ -833,10 +938,13 @@ def search_cpu_baseline(db, s, qs, target_s: float = 10.0):
     dt = run(qs[:n])[0]
     n = int(min(len(qs), max(n, n * target_s / max(dt, 1e-3))))
     tot, ts, tsw, trank, npairs = run(qs[:n])
+    src = ("restatements of clustkit/kmer_index.py:470-534 (Phase A via the C scorer with Phase B off) and "
+           "csrc/sw_align.c:25-266" if exact else
+           "restatements of clustkit/csrc/kmer_score.c:195-470 and sw_align.c:25-266")
     return {"value": n / tot, "unit": "queries/s", "cores": threads, "kind": "port",
             "stage_s": {"kmer_scorer": ts, "sw": tsw, "rank": trank},
             "sample": f"{n} queries of the stream, {npairs} candidate pairs, {threads} threads, {tot:.1f}s",
-            "source": "restatements of clustkit/csrc/kmer_score.c:195-470 and sw_align.c:25-266"}
+            "source": src}
 
 
 def _similar_chain(off, ent, fr, freq_thresh, s, sample, band, thresh=13, max_cands=500, top_k=10):
@@ -986,12 +1094,14 @@ def _measure_search_mode(db, qs, thresh, rates, n_plain, n_stage, n_batch, scori
             t_end = time.perf_counter()
             p = server.latency_percentiles()
             sweep.append({"offered_qps": rate, "achieved_qps": n / (t_end - t_start), "queries": n,
-                          "p50_ms": p["p50_ms"], "p99_ms": p["p99_ms"]})
+                          "p50_ms": p["p50_ms"], "p99_ms": p["p99_ms"], "deferrals": server.deferrals,
+                          "peak_in_flight_mb": server.peak_in_flight_bytes / 2 ** 20})
             log(f"search (kmer_score_thresh {thresh}{', C path' if scoring else ''}) rate {rate}/s: {sweep[-1]}")
     finally:
         server.stop()
         gc.unfreeze()
-    return {"plain_loop": plain, "continuous_batching": sweep, "slots": len(server.slots)}
+    return {"plain_loop": plain, "continuous_batching": sweep, "slots": len(server.slots),
+            "mem_budget_mb": server.mem_budget / 2 ** 20, "batch_mb_full": server.per_slot_bytes / 2 ** 20}
 
 
 def main():
@@ -1008,7 +1118,8 @@ def main():
                     help="search leg scoring modes: exact, similar, c_path (comma list)")
     ap.add_argument("--search-batches-only", action="store_true",
                     help="search leg: only full batches per mode (a warm-up and a few), for profiler launch lists")
-    ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24); 0 = library default")
+    ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24/32); 0 = library default")
+    ap.add_argument("--ctas", type=int, default=0, help="strip kernel CTAs per SM (1/2); 0 = library default")
     ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default")
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
     ap.add_argument("--search", choices=["auto", "on", "off", "only"], default="auto",

@@ -31,6 +31,7 @@ CFG_WAVE_ALL_BELOW = 3
 CFG_WAVE_ADAPTIVE = 4
 CFG_WAVE_STREAM = 5
 CFG_WAVE_ROWS = 6
+CFG_CTAS_PER_SM = 8
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -56,9 +57,14 @@ SIGNATURES = {
     "ck_ctx_status": (_I32, [_I32, _P]),
     "ck_sw_batch_device_ctx": (_I32, [_I32, _P, _I64, _P, _I64, _P, _P, _I64, _I32, _P, ctypes.c_float, _P,
                                       _I32, _I32, _P, _P, _P, _P, _P, _P]),
+    "ck_ctx_upload_db": (_I32, [_I32, _P, _I64, _P, _P, _I64]),
+    "ck_ctx_submit": (_I32, [_I32, _P, _I64, _I32, _P, ctypes.c_float, _P, _I32, _I32, _P, _P, _P, _P, _P, _P]),
+    "ck_ctx_poll": (_I32, [_I32, _P]),
+    "ck_ctx_wait": (_I32, [_I32]),
     "ck_kmer_index_build_device": (_I32, [_I32, _P, _I64, _P, _P, _I64, _I32, _I32, _P, _P, _I64, _P, _P,
                                           _P]),
     "ck_kmer_targets_device": (_I32, [_I32, _P, _I64, _P, _P]),
+    "ck_search_pairs_device": (_I32, [_I32, _I32, _I32, _I32, _P, _P, _P, _P]),
     "ck_search_phase_a_device": (_I32, [_I32, _P, _I64, _P, _P, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _I32,
                                         _I32, _I32, _I32, _P, _P, _P, _P]),
     "ck_sw_last_counters": (_I32, [_P]),
@@ -77,6 +83,7 @@ SIGNATURES = {
     "ck_jaccard": (_I32, [_P, _I64, _P, _I64, _I32, ctypes.c_float, _P, _P]),
     "ck_jaccard_device": (_I32, [_P, _I64, _P, _I64, _I32, ctypes.c_float, _P, _P, _P]),
     "ck_probe_int_rate": (_I32, [_I32, _P]),
+    "ck_probe_cell_rate": (_I32, [_I32, _P]),
     "ck_sw_profile": (_I32, [_I32]),
     "ck_sw_last_kernel_ms": (_I32, [_P]),
     "ck_sw_set_config": (_I32, [_I32, _I32]),

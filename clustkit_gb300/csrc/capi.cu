@@ -31,7 +31,28 @@ struct ScratchSet {
     int32_t *err = nullptr;
     bool frozen = false;  // buffers may be baked into a captured CUDA graph: never reallocate
     bool dirty[SLOT_COUNT] = {};  // a kept-zero buffer whose last user may not have cleaned it
+    // resident sequence database of the submit/poll interface (ck_ctx_upload_db)
+    uint8_t *db_flat = nullptr;
+    int64_t *db_offsets = nullptr;
+    int32_t *db_lengths = nullptr;
+    int64_t db_flat_len = 0, db_n = 0;
+    bool db_ready = false;
+    // the one submission in flight (ck_ctx_submit .. ck_ctx_poll / ck_ctx_wait)
+    cudaEvent_t done = nullptr;
+    cudaStream_t pending_stream = nullptr;
+    bool pending = false;
 };
+
+void free_db(ScratchSet *set) {
+    if (set->db_flat) cudaFree(set->db_flat);
+    if (set->db_offsets) cudaFree(set->db_offsets);
+    if (set->db_lengths) cudaFree(set->db_lengths);
+    set->db_flat = nullptr;
+    set->db_offsets = nullptr;
+    set->db_lengths = nullptr;
+    set->db_flat_len = set->db_n = 0;
+    set->db_ready = false;
+}
 
 struct DeviceState {
     bool init = false;
@@ -490,6 +511,8 @@ int32_t ck_ctx_destroy(int32_t handle) {
     for (int i = 0; i < SLOT_COUNT; ++i)
         if (set->buf[i]) cudaFree(set->buf[i]);
     if (set->err) cudaFree(set->err);
+    free_db(set);
+    if (set->done) cudaEventDestroy(set->done);
     cudaSetDevice(prev);
     delete set;
     g_ctx[handle - 1] = nullptr;
@@ -523,6 +546,153 @@ int32_t ck_sw_batch_device_ctx(int32_t ctx, const int32_t *d_pairs, int64_t M, c
     });
 }
 
+// ------------------------------------------------ resident database, submit/poll
+static ScratchSet *ctx_set(int32_t handle) {
+    if (handle < 1 || handle > (int32_t)g_ctx.size() || !g_ctx[handle - 1]) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "unknown context handle");
+        return nullptr;
+    }
+    ScratchSet *set = g_ctx[handle - 1];
+    if (set->device != current_device()) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "context belongs to another device");
+        return nullptr;
+    }
+    return set;
+}
+
+int32_t ck_ctx_upload_db(int32_t ctx, const uint8_t *flat, int64_t flat_len, const int64_t *offsets,
+                         const int32_t *lengths, int64_t n_seqs) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    ScratchSet *set = ctx_set(ctx);
+    if (!set) return CK_ERR_INVALID_ARGUMENT;
+    if (flat_len < 0 || n_seqs < 0 || (flat_len > 0 && !flat) || (n_seqs > 0 && (!offsets || !lengths))) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "upload_db: NULL pointer or negative size");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    if (set->pending) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "upload_db: a submission on this context is still in flight");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    free_db(set);
+    CK_CUDA(cudaMalloc(&set->db_flat, (size_t)(flat_len > 0 ? flat_len : 1)));
+    CK_CUDA(cudaMalloc(&set->db_offsets, (size_t)(n_seqs > 0 ? n_seqs : 1) * 8));
+    CK_CUDA(cudaMalloc(&set->db_lengths, (size_t)(n_seqs > 0 ? n_seqs : 1) * 4));
+    if (flat_len) CK_CUDA(cudaMemcpy(set->db_flat, flat, (size_t)flat_len, cudaMemcpyHostToDevice));
+    if (n_seqs) {
+        CK_CUDA(cudaMemcpy(set->db_offsets, offsets, (size_t)n_seqs * 8, cudaMemcpyHostToDevice));
+        CK_CUDA(cudaMemcpy(set->db_lengths, lengths, (size_t)n_seqs * 4, cudaMemcpyHostToDevice));
+    }
+    set->db_flat_len = flat_len;
+    set->db_n = n_seqs;
+    set->db_ready = true;
+    return CK_OK;
+}
+
+int32_t ck_ctx_submit(int32_t ctx, const int32_t *pairs, int64_t M, int32_t band_width,
+                      const int8_t *sub_matrix, float threshold, const int32_t *diag_hints,
+                      int32_t pass_rule, int32_t engine, float *out_sims, int32_t *out_scores,
+                      int32_t *out_matches, int32_t *out_shorter, uint8_t *out_mask, void *stream) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    t_counters = SwCounters{};
+    ScratchSet *set = ctx_set(ctx);
+    if (!set) return CK_ERR_INVALID_ARGUMENT;
+    if (!set->db_ready) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "submit: no database uploaded to this context (ck_ctx_upload_db)");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    if (set->pending) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "submit: the previous submission on this context is still in "
+                                           "flight (ck_ctx_poll / ck_ctx_wait it first)");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    CK_TRY(check_sw_args(pairs, M, set->db_flat, set->db_flat_len, set->db_offsets, set->db_lengths, set->db_n,
+                         sub_matrix, pass_rule, engine));
+    if (!set->done) CK_CUDA(cudaEventCreateWithFlags(&set->done, cudaEventDisableTiming));
+    cudaStream_t st = (cudaStream_t)stream;
+    return with_context(ctx, [&]() -> int32_t {
+        int32_t status = CK_OK;
+        const size_t m = (size_t)M;
+        SwIn in{};
+        in.pairs = m ? (const int32_t *)upload(SLOT_HOST_IO0, pairs, m * 8, st, &status) : nullptr;
+        in.hints = (diag_hints && m) ? (const int32_t *)upload(SLOT_HOST_IO4, diag_hints, m * 4, st, &status)
+                                     : nullptr;
+        if (status != CK_OK) return status;
+        in.flat = set->db_flat;
+        in.offsets = set->db_offsets;
+        in.lengths = set->db_lengths;
+        in.n_seqs = set->db_n;
+        in.flat_len = set->db_flat_len;
+        in.band_width = band_width;
+        in.threshold = threshold;
+        in.pass_rule = pass_rule;
+        if (m) {
+            char *o = (char *)scratch(SLOT_HOST_IO5, m * 17 + 256, &status);
+            if (!o) return status;
+            SwOut out{};
+            out.sims = out_sims ? (float *)o : nullptr;
+            out.scores = out_scores ? (int32_t *)(o + m * 4) : nullptr;
+            out.matches = out_matches ? (int32_t *)(o + m * 8) : nullptr;
+            out.shorter = out_shorter ? (int32_t *)(o + m * 12) : nullptr;
+            out.mask = out_mask ? (uint8_t *)(o + m * 16) : nullptr;
+            CK_TRY(sw_run_device(in, out, M, engine, sub_matrix, st, &t_counters, false));
+            if (out_sims) CK_CUDA(cudaMemcpyAsync(out_sims, out.sims, m * 4, cudaMemcpyDeviceToHost, st));
+            if (out_scores) CK_CUDA(cudaMemcpyAsync(out_scores, out.scores, m * 4, cudaMemcpyDeviceToHost, st));
+            if (out_matches)
+                CK_CUDA(cudaMemcpyAsync(out_matches, out.matches, m * 4, cudaMemcpyDeviceToHost, st));
+            if (out_shorter)
+                CK_CUDA(cudaMemcpyAsync(out_shorter, out.shorter, m * 4, cudaMemcpyDeviceToHost, st));
+            if (out_mask) CK_CUDA(cudaMemcpyAsync(out_mask, out.mask, m, cudaMemcpyDeviceToHost, st));
+        }
+        CK_CUDA(cudaEventRecord(set->done, st));
+        set->pending_stream = st;
+        set->pending = true;
+        return CK_OK;
+    });
+}
+
+// The submission's outcome once its event has completed: the context's GPU
+// input checks since the last read.
+static int32_t ctx_finish(int32_t ctx, ScratchSet *set) {
+    set->pending = false;
+    return with_context(ctx, [&] { return read_and_clear_error(set->pending_stream); });
+}
+
+int32_t ck_ctx_poll(int32_t ctx, int32_t *out_done) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    if (!out_done) return CK_ERR_INVALID_ARGUMENT;
+    ScratchSet *set = ctx_set(ctx);
+    if (!set) return CK_ERR_INVALID_ARGUMENT;
+    *out_done = 1;
+    if (!set->pending) return CK_OK;
+    const cudaError_t e = cudaEventQuery(set->done);
+    if (e == cudaErrorNotReady) {
+        *out_done = 0;
+        return CK_OK;
+    }
+    if (e != cudaSuccess) {
+        set->pending = false;
+        return cuda_status(e, "ck_ctx_poll");
+    }
+    return ctx_finish(ctx, set);
+}
+
+int32_t ck_ctx_wait(int32_t ctx) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    t_status = CK_OK;
+    ScratchSet *set = ctx_set(ctx);
+    if (!set) return CK_ERR_INVALID_ARGUMENT;
+    if (!set->pending) return CK_OK;
+    const cudaError_t e = cudaEventSynchronize(set->done);
+    if (e != cudaSuccess) {
+        set->pending = false;
+        return cuda_status(e, "ck_ctx_wait");
+    }
+    return ctx_finish(ctx, set);
+}
+
 int32_t ck_sw_profile(int32_t enable) {
     std::lock_guard<std::mutex> lock(g_mutex);
     g_profile = enable != 0;
@@ -550,6 +720,7 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) return sw_set_wave(2, value);
     if (key == CK_CFG_WAVE_STREAM) return sw_set_wave(3, value);
     if (key == CK_CFG_WAVE_ROWS) return sw_set_wave(4, value);
+    if (key == CK_CFG_CTAS_PER_SM) return sw_set_ctas_per_sm(value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }
@@ -564,6 +735,7 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) { *value = sw_wave(2); return CK_OK; }
     if (key == CK_CFG_WAVE_STREAM) { *value = sw_wave(3); return CK_OK; }
     if (key == CK_CFG_WAVE_ROWS) { *value = sw_wave(4); return CK_OK; }
+    if (key == CK_CFG_CTAS_PER_SM) { *value = sw_ctas_per_sm(); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
 }

@@ -176,6 +176,19 @@ __device__ __forceinline__ int32_t entry_target(const int64_t *__restrict__ entr
     return targets ? __ldg(targets + h) : (int32_t)(entries[h] >> 32);
 }
 
+// Dense pair list of a search batch for the SW engine: pair q * K + c is
+// (seq0 + q, targets[q * K + c]) for the query's first n[q] candidates and
+// (empty, empty) after them (an empty sequence aligns to nothing).
+__global__ void search_pairs_kernel(int32_t nq, int32_t K, int32_t seq0, int32_t empty_idx,
+                                    const int32_t *__restrict__ n, const int32_t *__restrict__ targets,
+                                    int2 *__restrict__ pairs) {
+    const int64_t M = (int64_t)nq * K;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t q = (int32_t)(i / K), c = (int32_t)(i - (int64_t)q * K);
+        pairs[i] = c < __ldg(n + q) ? make_int2(seq0 + q, __ldg(targets + i)) : make_int2(empty_idx, empty_idx);
+    }
+}
+
 __global__ void compact_targets_kernel(const int64_t *__restrict__ entries, int64_t n,
                                        int32_t *__restrict__ targets) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1230,6 +1243,23 @@ extern "C" int32_t ck_kmer_targets_device(int32_t ctx, const int64_t *d_kmer_ent
         CK_CUDA(cudaGetLastError());
         return CK_OK;
     }, &a);
+}
+
+extern "C" int32_t ck_search_pairs_device(int32_t nq, int32_t max_cands, int32_t seq0, int32_t empty_idx,
+                                          const int32_t *d_n, const int32_t *d_targets, int32_t *d_pairs,
+                                          void *stream) {
+    std::lock_guard<std::mutex> lock(library_mutex());
+    reset_thread_status();
+    if (nq < 0 || max_cands < 0 || (nq > 0 && max_cands > 0 && (!d_n || !d_targets || !d_pairs))) {
+        set_error(CK_ERR_INVALID_ARGUMENT, "search pairs: bad arguments");
+        return CK_ERR_INVALID_ARGUMENT;
+    }
+    const int64_t M = (int64_t)nq * max_cands;
+    if (M == 0) return CK_OK;
+    search_pairs_kernel<<<grid_for(M, 256), 256, 0, (cudaStream_t)stream>>>(nq, max_cands, seq0, empty_idx, d_n,
+                                                                             d_targets, (int2 *)d_pairs);
+    CK_CUDA(cudaGetLastError());
+    return CK_OK;
 }
 
 extern "C" int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qflat_len,

@@ -72,7 +72,14 @@ __device__ __forceinline__ int32_t fadd(int32_t a, int32_t b, int32_t one) {
     asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(one), "r"(b));
     return d;
 }
-constexpr int INC_ENTRIES = N_CODES * N_CODES;           // 441
+// Row code of the rows of a pair's last strip below its last row.  Their
+// increments are so negative that the diagonal candidate always loses to
+// zero, so such a row only carries gap values down and along from the real
+// rows (each strictly below the score it came from): it can never hold the
+// pair's first maximum, and the last strip runs the unmasked column code.
+constexpr uint32_t PAD_CODE = N_CODES;
+constexpr int32_t PAD_INC = INT32_MIN + 1;  // H keys are >= 0, so H + PAD_INC never wraps
+constexpr int INC_ENTRIES = (N_CODES + 1) * N_CODES;     // 462: row code (0..21) x column code (0..20)
 constexpr size_t INC_SMEM = (size_t)INC_ENTRIES * 32 * 4;  // replicated per lane
 
 // ----------------------------------------------------------------- tables
@@ -81,7 +88,7 @@ __global__ void build_inc_kernel(const int8_t *sub, int32_t *inc) {
     if (t >= INC_ENTRIES) return;
     int a = t / N_CODES, b = t % N_CODES;
     int s = (a < 20 && b < 20) ? (int)sub[a * 20 + b] : -4;
-    inc[t] = s * key::KU + 2 * key::PU + (a == b ? 1 : 0);
+    inc[t] = a == (int)PAD_CODE ? PAD_INC : s * key::KU + 2 * key::PU + (a == b ? 1 : 0);
 }
 
 // Whether every residue code of sequence i is <= 20, memoised per call in
@@ -253,12 +260,15 @@ struct StripRegs {
     uint32_t bcol_n2;
 };
 
-// Structural variants of the strip kernel (picked by the autotuner):
-// bit 0 -- prefetch the window entry and residue 2 columns ahead instead of 1;
-// bit 1 -- run interior columns 4 at a time instead of 2.
+// Structural variants of the strip kernel (picked by the autotuner), all
+// prefetching the window entry and residue two columns ahead: bit 1 runs
+// interior columns in groups of 4 instead of 2 (one first-max vote per
+// group); bit 0 starts the groups at columns aligned to their size and
+// addresses a group's window slots and residues from two base pointers,
+// instead of computing each column's addresses on its own.
 template <int V> struct StripVariant {
-    static constexpr int PREFETCH = (V & 1) ? 2 : 1;
     static constexpr int UNROLL = (V & 2) ? 4 : 2;
+    static constexpr bool ALIGNED = (V & 1) != 0;
 };
 
 // Rows of a strip inside their band at a column, as a bit mask: row r
@@ -268,7 +278,7 @@ template <int V> struct StripVariant {
 __device__ __forceinline__ uint32_t band_rows(int32_t d, uint32_t w2, int32_t alive) {
     const int32_t lo = d - (int32_t)w2 > 0 ? d - (int32_t)w2 : 0;
     const int32_t hi = d < alive - 1 ? d : alive - 1;
-    return hi < lo ? 0u : (2u << hi) - (1u << lo);  // here 0 <= lo <= hi < alive <= 24
+    return hi < lo ? 0u : (2u << hi) - (1u << lo);  // 0 <= lo <= hi < alive <= 16 (wave kernel)
 }
 
 // Cells of rows [RB, RE) at one column, top to bottom.  (hu, eu) enter as
@@ -315,54 +325,215 @@ __device__ __forceinline__ void strip_cells(uint32_t bcol, int32_t &hu, int32_t 
     }
 }
 
-// First-max trackers (one per row, in shared memory) are touched only when
-// some lane's column maximum beats the best score its pair had when the
-// strip began -- the only way one of its rows can record a new first
-// maximum.
-template <int R>
-__device__ __forceinline__ void strip_track(const StripRegs<R> &S, int32_t gthr, int32_t *s_best) {
+// One DP cell of strip row r (all inputs inside the band).  (hu, eu) enter as
+// H and E of the row above at this column and leave as this row's; hdiag
+// enters as H of the row above at the previous column and leaves as this
+// row's H at the previous column (the next row's diagonal input).
+template <int R, int r>
+__device__ __forceinline__ void strip_cell(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
+                                           StripRegs<R> &S, const char *s_inc, int32_t one) {
     using namespace key;
-    int32_t cm = S.hc[0];
-#pragma unroll
-    for (int r = 1; r + 1 < R; r += 2) cm = __vimax3_s32(cm, S.hc[r], S.hc[r + 1]);
-    if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
-    if (__any_sync(__activemask(), cm > gthr)) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int32_t b = s_best[r * STRIP_THREADS];
-            if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
-        }
+    const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
+    const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
+    // E's extension term comes from E of the row above, known before that
+    // row's H: only H_up + OPEN_E and the max-of-three sit on the row-to-row
+    // dependency chain.  E's tie bit plays no part in H (E, F, diag and zero
+    // differ in priority), so it is set off the chain.
+    const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, EXT, one));
+    const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
+    const int32_t hn = __vimax3_s32(diagc, eR, fTn) & CLEAN;
+    hdiag = S.hc[r];
+    S.hc[r] = hn;
+    S.fT[r] = fTn;
+    hu = hn;
+    eu = eR | TBIT;
+}
+
+// Rows r .. R-1 of a column, all inside their band.
+template <int R, int r = 0>
+__device__ __forceinline__ void strip_cells_from(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
+                                                 StripRegs<R> &S, const char *s_inc, int32_t one) {
+    if constexpr (r < R) {
+        strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_cells_from<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, one);
     }
 }
 
-// A full column: every row computed (or skipped when outside its band),
-// window read and written, next columns' inputs prefetched.
-template <int R, bool MASKED, int PF>
-__device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R> &S,
-                                             const char *s_inc, int2 *win, int32_t wmask,
-                                             const uint8_t *B, int32_t lo0, uint32_t w2,
-                                             int32_t alive, int32_t gthr, int32_t *s_best,
-                                             int32_t one) {
-    const int2 bnd = S.bnd_n;
-    const uint32_t bcol = S.bcol_n;
-    int2 *slot = win + (size_t)(j & wmask) * 32;
-    const int32_t jn = j + PF < lb ? j + PF : lb;  // column whose residue is prefetched
-    if (PF == 2) {
+// A ramp or clipped column: only rows klo..khi lie inside their band.  A row
+// above klo has left it (it hands H = 0, E = -inf down and its last H as the
+// next row's diagonal input); a row below khi has not reached it (left
+// untouched, and the strip's bottom output is the out-of-band boundary).
+// The left ramp (klo = 0) is a prefix of the rows and the right ramp
+// (khi = R - 1) a suffix, so each needs one compare a row; a column that is
+// both (a band narrower than the strip) takes the two-sided test.  Every
+// row's cell appears once in the code.
+template <int R, int r = 0>
+__device__ __forceinline__ void strip_rows_prefix(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
+                                                  StripRegs<R> &S, const char *s_inc, int32_t khi, int32_t one) {
+    if constexpr (r < R) {
+        if (r <= khi) strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_rows_prefix<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, khi, one);
+    }
+}
+
+template <int R, int r = 0>
+__device__ __forceinline__ void strip_rows_suffix(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
+                                                  StripRegs<R> &S, const char *s_inc, int32_t klo, int32_t one) {
+    if constexpr (r < R) {
+        if (r >= klo) strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
+        else hdiag = S.hc[r];
+        strip_rows_suffix<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, klo, one);
+    }
+}
+
+template <int R, int r = 0>
+__device__ __forceinline__ void strip_rows_between(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
+                                                   StripRegs<R> &S, const char *s_inc, int32_t klo, int32_t khi,
+                                                   int32_t one) {
+    if constexpr (r < R) {
+        if (r < klo) hdiag = S.hc[r];
+        else if (r <= khi) strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_rows_between<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void strip_rows_masked(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
+                                                  StripRegs<R> &S, const char *s_inc, int32_t klo, int32_t khi,
+                                                  int32_t one) {
+    if (klo == 0) {
+        strip_rows_prefix<R>(bcol, hu, eu, hdiag, S, s_inc, khi, one);
+    } else {
+        hu = 0;  // the first row inside the band has the boundary above it
+        eu = key::NEG_E;
+        if (khi == R - 1) strip_rows_suffix<R>(bcol, hu, eu, hdiag, S, s_inc, klo, one);
+        else strip_rows_between<R>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
+    }
+    if (khi < R - 1) { hu = 0; eu = key::NEG_E; }  // the bottom row has not started
+}
+
+// First-max trackers (one per row, in shared memory) are touched only when
+// some lane holds a cell at or above its trigger threshold `tthr`: above the
+// pair's best when the strip began, and once this strip has set a best M, at
+// least M (an equal score in an earlier row still comes first in row-major
+// order; a lower one never can).  Only cells above the threshold read their
+// row's tracker; the strict '>' there keeps each row's first column.  The
+// check covers the U columns of `hs` (oldest first) at once, so that the
+// warp's vote and branch come once per U columns and the columns' row chains
+// can overlap in between.
+template <int R, int U>
+__device__ __forceinline__ void strip_track(const int32_t (&hs)[U][R], int32_t &tthr, int32_t *s_best) {
+    using namespace key;
+    int32_t cm = hs[0][0];
+#pragma unroll
+    for (int k = 1; k + 1 < U * R; k += 2) cm = __vimax3_s32(cm, hs[k / R][k % R], hs[(k + 1) / R][(k + 1) % R]);
+    if (((U * R) & 1) == 0) cm = max(cm, hs[U - 1][R - 1]);
+    if (__any_sync(__activemask(), cm > tthr)) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t v = hs[u][r];
+                if (v > tthr) {
+                    const int32_t b = s_best[r * STRIP_THREADS];
+                    if (v > (b | (KU - 1))) s_best[r * STRIP_THREADS] = v;
+                }
+            }
+        }
+        if (cm > tthr) tthr = (cm & ~(KU - 1)) - 1;
+    }
+}
+
+// The next column's inputs: the window entry (H, E of the row above the
+// strip) and the residue offset of column j, prefetched two columns ahead.
+template <int R>
+__device__ __forceinline__ void column_inputs(int32_t j, int32_t lb, StripRegs<R> &S, const int2 *win,
+                                              int32_t wmask, const uint8_t *B, int2 &bnd, uint32_t &bcol) {
+    bnd = S.bnd_n;
+    bcol = S.bcol_n;
+    const int32_t jn = j + 2 < lb ? j + 2 : lb;  // column whose residue is prefetched
+    S.bnd_n = S.bnd_n2;
+    S.bcol_n = S.bcol_n2;
+    S.bnd_n2 = win[(size_t)((j + 2) & wmask) * 32];
+    S.bcol_n2 = (uint32_t)__ldg(B + jn - 1) * 128u;
+}
+
+// U interior columns j .. j + U - 1 (every row inside its band), each
+// addressing its own window slots and residues, then one first-max check
+// over all of them.
+template <int R, int U>
+__device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripRegs<R> &S, const char *s_inc,
+                                                   int2 *win, int32_t wmask, const uint8_t *B, int32_t &tthr,
+                                                   int32_t *s_best, int32_t one) {
+    int32_t hs[U][R];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        int2 bnd;
+        uint32_t bcol;
+        column_inputs<R>(j + u, lb, S, win, wmask, B, bnd, bcol);
+        int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
+        S.hd0 = hu;
+        strip_cells_from<R>(bcol, hu, eu, hdiag, S, s_inc, one);
+        win[(size_t)((j + u) & wmask) * 32] = make_int2(hu, eu);
+#pragma unroll
+        for (int r = 0; r < R; ++r) hs[u][r] = S.hc[r];
+    }
+    strip_track<R, U>(hs, tthr, s_best);
+}
+
+// U interior columns j .. j + U - 1 with j a multiple of U, inputs prefetched
+// two columns ahead (columns j + U and j + U + 1 are loaded here).  W is a
+// power of two >= 32 and U divides it, so the slots of columns j .. j+U-1 are
+// consecutive, and so are those of j+U and j+U+1: two base addresses per
+// group, immediate offsets after them.  The caller runs a group only where
+// j + U + 1 <= lb, so the prefetched residues lie inside the sequence.
+template <int R, int U>
+__device__ __forceinline__ void strip_group(int32_t j, StripRegs<R> &S, const char *s_inc, int2 *win,
+                                            int32_t wmask, const uint8_t *B, int32_t &tthr, int32_t *s_best,
+                                            int32_t one) {
+    int2 *cur = win + (size_t)(j & wmask) * 32;
+    const int2 *nxt = win + (size_t)((j + U) & wmask) * 32;
+    const uint8_t *pb = B + j + 1;  // residue of column j + 2 (columns are 1-based)
+    int32_t hs[U][R];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int2 bnd = S.bnd_n;
+        const uint32_t bcol = S.bcol_n;
         S.bnd_n = S.bnd_n2;
         S.bcol_n = S.bcol_n2;
-        S.bnd_n2 = win[(size_t)((j + 2) & wmask) * 32];
-        S.bcol_n2 = (uint32_t)__ldg(B + jn - 1) * 128u;
-    } else {
-        S.bnd_n = win[(size_t)((j + 1) & wmask) * 32];
-        S.bcol_n = (uint32_t)__ldg(B + jn - 1) * 128u;
+        S.bnd_n2 = (u + 2 < U) ? cur[(u + 2) * 32] : nxt[(u + 2 - U) * 32];
+        S.bcol_n2 = (uint32_t)__ldg(pb + u) * 128u;
+        int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
+        S.hd0 = hu;
+        strip_cells_from<R>(bcol, hu, eu, hdiag, S, s_inc, one);
+        cur[u * 32] = make_int2(hu, eu);
+#pragma unroll
+        for (int r = 0; r < R; ++r) hs[u][r] = S.hc[r];
     }
-    int32_t hu = bnd.x, eu = bnd.y;
-    const int32_t hdiag = S.hd0;
+    strip_track<R, U>(hs, tthr, s_best);
+}
+
+// One column outside the aligned interior groups: a ramp or clipped column
+// (rows klo..khi inside their band) or an interior column at a group's edge.
+template <int R>
+__device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R> &S, const char *s_inc,
+                                             int2 *win, int32_t wmask, const uint8_t *B, int32_t lo0,
+                                             int32_t w2, int32_t &tthr, int32_t *s_best, int32_t one) {
+    int2 bnd;
+    uint32_t bcol;
+    column_inputs<R>(j, lb, S, win, wmask, B, bnd, bcol);
+    int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
     S.hd0 = hu;
-    strip_cells<R, 0, R, MASKED>(bcol, hu, eu, hdiag, S, s_inc, MASKED ? band_rows(j - lo0, w2, alive) : ~0u,
-                                 one);
-    *slot = make_int2(hu, eu);
-    strip_track<R>(S, gthr, s_best);
+    // rows r with lo0 + r <= j <= lo0 + r + 2w are inside their band
+    const int32_t d = j - lo0;
+    const int32_t klo = d - w2 > 0 ? d - w2 : 0;
+    const int32_t khi = d < R - 1 ? d : R - 1;
+    strip_rows_masked<R>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
+    win[(size_t)(j & wmask) * 32] = make_int2(hu, eu);
+    int32_t hs[1][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) hs[0][r] = S.hc[r];
+    strip_track<R, 1>(hs, tthr, s_best);
 }
 
 template <int R, int V>
@@ -376,7 +547,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
     const uint8_t *A = in.flat + in.offsets[g.a_idx];
     const uint8_t *B = in.flat + in.offsets[g.b_idx];
     const int32_t wmask = W - 1;
-    const uint32_t w2 = 2u * (uint32_t)w;
+    const int32_t w2 = 2 * w;
 
     for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E);
 
@@ -390,47 +561,47 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         if (J0 > lb) break;
         if (J1 < J0) continue;
 
-        const int32_t gthr = gbest | (KU - 1);
+        int32_t tthr = gbest | (KU - 1);
         const int32_t alive = la - i0 + 1 < R ? la - i0 + 1 : R;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             S.hc[r] = 0;
             S.fT[r] = NEG_F;
             s_best[r * STRIP_THREADS] = gbest;
-            const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : 0u;
+            // rows below the pair's last row (last strip only) read the pad code
+            const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : PAD_CODE;
             S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
         }
         S.hd0 = (J0 >= 2) ? win[(size_t)((J0 - 1) & wmask) * 32].x : 0;
         S.bnd_n = win[(size_t)(J0 & wmask) * 32];
         S.bcol_n = (uint32_t)__ldg(B + J0 - 1) * 128u;
-        if (StripVariant<V>::PREFETCH == 2) {
-            S.bnd_n2 = win[(size_t)((J0 + 1) & wmask) * 32];
-            S.bcol_n2 = (uint32_t)__ldg(B + (J0 + 1 < lb ? J0 + 1 : lb) - 1) * 128u;
-        }
+        S.bnd_n2 = win[(size_t)((J0 + 1) & wmask) * 32];
+        S.bcol_n2 = (uint32_t)__ldg(B + (J0 + 1 < lb ? J0 + 1 : lb) - 1) * 128u;
 
-        // Interior columns (every row alive and inside its band) run unmasked,
-        // two at a time; ramp and clipped columns run the masked step.  One
-        // loop keeps a single copy of each body in the instruction cache.
+        // Interior columns (every row inside its band) run unmasked in aligned
+        // groups of U; ramp and clipped columns, and interior columns at a
+        // group's edge, run one at a time.  One loop keeps a single copy of
+        // each body in the instruction cache.
         int32_t I0 = lo0 + R - 1;
         if (I0 < J0) I0 = J0;
         int32_t I1 = i0 + h + w;
         if (I1 > J1) I1 = J1;
-        if (alive < R) { I0 = J1 + 1; I1 = J1; }
-        constexpr int U = StripVariant<V>::UNROLL, PF = StripVariant<V>::PREFETCH;
+        constexpr int U = StripVariant<V>::UNROLL;
+        constexpr bool ALIGNED = StripVariant<V>::ALIGNED;
         for (int32_t j = J0; j <= J1;) {
-            if (j >= I0 && j + U - 1 <= I1) {
-#pragma unroll
-                for (int u = 0; u < U; ++u)
-                    strip_column<R, false, PF>(j + u, lb, S, s_inc, win, wmask, B, lo0, w2, alive, gthr,
-                                               s_best, one);
+            if (ALIGNED && j >= I0 && (j & (U - 1)) == 0 && j + U - 1 <= I1 && j + U + 1 <= lb) {
+                strip_group<R, U>(j, S, s_inc, win, wmask, B, tthr, s_best, one);
+                j += U;
+            } else if (!ALIGNED && j >= I0 && j + U - 1 <= I1) {
+                strip_group_percol<R, U>(j, lb, S, s_inc, win, wmask, B, tthr, s_best, one);
                 j += U;
             } else {
-                strip_column<R, true, PF>(j, lb, S, s_inc, win, wmask, B, lo0, w2, alive, gthr, s_best,
-                                          one);
+                strip_column<R>(j, lb, S, s_inc, win, wmask, B, lo0, w2, tthr, s_best, one);
                 j += 1;
             }
         }
         // rows merge in row order: strict '>' keeps the earliest row on ties
+        // (pad rows never hold a new best: their values stay below a real cell's)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int32_t b = s_best[r * STRIP_THREADS];
@@ -473,8 +644,8 @@ __device__ __noinline__ void wave_stream_any(int32_t rows, const SwIn &in, const
 // small call), then the rest 32 pairs per warp, one lane per pair, in
 // register strips of R rows.  Long pairs thus start first and the lane-per-
 // pair groups fill in around them.
-template <int R, int V>
-__global__ void __launch_bounds__(STRIP_THREADS, 2)
+template <int R, int V, int MINB>
+__global__ void __launch_bounds__(STRIP_THREADS, MINB)
 sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
@@ -949,6 +1120,9 @@ static int32_t pow2_at_least(int64_t x) {
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
 static int32_t g_rows_per_strip = 0;  // 0: by band width (8 up to w = 64, else 16)
 static int32_t g_variant = 1;
+// resident CTAs of 256 threads per SM for strips of up to 16 rows: 2 (at most
+// 128 registers a thread) or 1 (up to 255); 0 = 2.  Taller strips always run 1.
+static int32_t g_ctas_per_sm = 0;
 // every pair runs one warp per pair when a call has at most this many pairs;
 // in larger calls, long pairs do: rows >= max(min rows, the adaptive bound)
 static int32_t g_wave_all_below = 40960;
@@ -1010,8 +1184,8 @@ static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t 
                                int32_t *err, cudaStream_t st, SwCounters *ctr);
 
 int32_t sw_set_rows_per_strip(int32_t r) {
-    if (r != 0 && r != 8 && r != 16 && r != 24) {
-        set_error(CK_ERR_UNSUPPORTED, "rows per strip must be 0 (by band width), 8, 16 or 24");
+    if (r != 0 && r != 8 && r != 16 && r != 24 && r != 32) {
+        set_error(CK_ERR_UNSUPPORTED, "rows per strip must be 0 (by band width), 8, 16, 24 or 32");
         return CK_ERR_UNSUPPORTED;
     }
     g_rows_per_strip = r;
@@ -1019,17 +1193,31 @@ int32_t sw_set_rows_per_strip(int32_t r) {
 }
 int32_t sw_rows_per_strip() { return g_rows_per_strip; }
 
-template <int R, int V>
+int32_t sw_set_ctas_per_sm(int32_t v) {
+    if (v < 0 || v > 2) {
+        set_error(CK_ERR_UNSUPPORTED, "strip kernel CTAs per SM must be 0 (default), 1 or 2");
+        return CK_ERR_UNSUPPORTED;
+    }
+    g_ctas_per_sm = v;
+    return CK_OK;
+}
+int32_t sw_ctas_per_sm() { return g_ctas_per_sm; }
+
+// CTAs per SM the strip kernel of R rows runs at
+static int32_t strip_minb(int32_t rows) { return rows >= 24 ? 1 : (g_ctas_per_sm == 1 ? 1 : 2); }
+
+template <int R, int V, int MINB>
 static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *order,
                              const int32_t *counters, const int32_t *inc, int32_t wmax,
                              int32_t *ticket, int32_t *fallback, int32_t *fb_count,
                              int32_t *err, cudaStream_t st, SwCounters *ctr) {
     int32_t status = CK_OK;
-    auto kern = sw_strip_kernel<R, V>;
+    auto kern = sw_strip_kernel<R, V, MINB>;
     const size_t smem = strip_smem<R>();
     CK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, STRIP_THREADS, smem));
+    if (per_sm > MINB) per_sm = MINB;  // the CTAs per SM the setting asks for, even if more would fit
     if (per_sm < 1) per_sm = 1;
     const int32_t W = pow2_at_least(2 * (int64_t)wmax + 2 * R + 2);
     // one window of W columns per lane; keep the total under 8 GiB
@@ -1048,17 +1236,28 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     return CK_OK;
 }
 
+template <int R, int MINB>
+static int32_t launch_strips_m(const SwIn &in, const SwOut &out, const uint32_t *order,
+                               const int32_t *counters, const int32_t *inc, int32_t wmax,
+                               int32_t *ticket, int32_t *fallback, int32_t *fb_count,
+                               int32_t *err, cudaStream_t st, SwCounters *ctr) {
+    switch (g_variant) {
+        case 0: return launch_strips<R, 0, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 2: return launch_strips<R, 2, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 3: return launch_strips<R, 3, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        default: return launch_strips<R, 1, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+    }
+}
+
 template <int R>
 static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
                                const int32_t *counters, const int32_t *inc, int32_t wmax,
                                int32_t *ticket, int32_t *fallback, int32_t *fb_count,
                                int32_t *err, cudaStream_t st, SwCounters *ctr) {
-    switch (g_variant) {
-        case 1: return launch_strips<R, 1>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-        case 2: return launch_strips<R, 2>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-        case 3: return launch_strips<R, 3>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-        default: return launch_strips<R, 0>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-    }
+    if (R >= 24 || strip_minb(R) == 1)
+        return launch_strips_m<R, 1>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+    return launch_strips_m<(R >= 24 ? 16 : R), 2>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count,
+                                                   err, st, ctr);
 }
 
 int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int8_t *d_sub,
@@ -1105,22 +1304,25 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
         int32_t wmax = 0;
         CK_TRY(widest_band(in, st, &wmax));
         const uint32_t *order = dv.Current();
+        // narrow bands: a strip's ramps (R - 1 masked columns at each end) weigh
+        // against 2w + 1 interior columns, so fewer rows per strip win there
+        const int32_t rows = g_rows_per_strip ? g_rows_per_strip : (wmax <= 64 ? 8 : 16);
         wave_split_kernel<<<1, 32, 0, st>>>(dk.Current(), cnt, in.band_width, g_wave_all_below,
                                             g_wave_min_rows, g_wave_adaptive,
-                                            (int64_t)sm_count() * 2 * STRIP_THREADS);
+                                            (int64_t)sm_count() * strip_minb(rows) * STRIP_THREADS);
         CK_CUDA(cudaGetLastError());
         // profiling events bracket the alignment kernel
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
-        // narrow bands: a strip's ramps (R - 1 masked columns at each end) weigh
-        // against 2w + 1 interior columns, so fewer rows per strip win there
-        const int32_t rows = g_rows_per_strip ? g_rows_per_strip : (wmax <= 64 ? 8 : 16);
         switch (rows) {
             case 8:
                 CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;
             case 24:
                 CK_TRY(launch_strips_v<24>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                break;
+            case 32:
+                CK_TRY(launch_strips_v<32>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
                 break;
             default:
                 CK_TRY(launch_strips_v<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));

@@ -38,6 +38,7 @@ static __device__ __align__(256) int32_t g_noalloc_err[64];
 namespace {
 constexpr int MAX_DEV = 16;
 struct NoallocDev {
+    std::mutex lock;  // one call at a time per device: they share that device's arrays
     bool ready = false;
     int4 *ws = nullptr;
     int8_t *sub = nullptr;
@@ -45,20 +46,28 @@ struct NoallocDev {
     int sms = 0;
 };
 NoallocDev g_na[MAX_DEV];
-std::mutex g_na_mutex;
 }  // namespace
 
-// Device addresses of the static arrays, looked up once per device with that
-// device current.  The host-side names of __device__ arrays are stand-ins,
-// not device addresses, so they are never handed to a kernel directly.
-static int32_t noalloc_setup(NoallocDev **out) {
+// The current device's entry, or an error for an ordinal beyond the table.
+static int32_t noalloc_device(NoallocDev **out, int *ordinal) {
     int d = 0;
     CK_CUDA(cudaGetDevice(&d));
     if (d < 0 || d >= MAX_DEV) {
         set_error(CK_ERR_NO_DEVICE, "device ordinal out of range");
         return CK_ERR_NO_DEVICE;
     }
-    NoallocDev &s = g_na[d];
+    *out = &g_na[d];
+    *ordinal = d;
+    return CK_OK;
+}
+
+// Device addresses of the static arrays, looked up once per device with that
+// device current (the caller holds the device's lock).  The host-side names
+// of __device__ arrays are stand-ins, not device addresses, so they are never
+// handed to a kernel directly.  The addresses belong to the device's primary
+// context: after cudaDeviceReset in this process they are stale, and this
+// entry point is not to be used again on that device.
+static int32_t noalloc_setup(NoallocDev &s, int d) {
     if (!s.ready) {
         CK_CUDA(cudaGetSymbolAddress((void **)&s.ws, g_noalloc_ws));
         CK_CUDA(cudaGetSymbolAddress((void **)&s.sub, g_noalloc_sub));
@@ -66,7 +75,6 @@ static int32_t noalloc_setup(NoallocDev **out) {
         CK_CUDA(cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, d));
         s.ready = true;
     }
-    *out = &s;
     return CK_OK;
 }
 
@@ -80,7 +88,6 @@ extern "C" int32_t ck_sw_batch_device_noalloc(
     const int8_t *sub_matrix_host, float threshold, const int32_t *d_diag_hints, int32_t pass_rule,
     float *d_sims, int32_t *d_scores, int32_t *d_matches, int32_t *d_shorter, uint8_t *d_mask,
     void *stream) {
-    std::lock_guard<std::mutex> lock(g_na_mutex);
     if (M < 0 || flat_len < 0 || n_seqs < 0 || !sub_matrix_host ||
         (M > 0 && !d_pairs) || (n_seqs > 0 && (!d_offsets || !d_lengths)) || (flat_len > 0 && !d_flat)) {
         set_error(CK_ERR_INVALID_ARGUMENT, "noalloc: NULL pointer or negative size");
@@ -108,7 +115,14 @@ extern "C" int32_t ck_sw_batch_device_noalloc(
         return CK_ERR_UNSUPPORTED;
     }
     NoallocDev *dev = nullptr;
-    CK_TRY(noalloc_setup(&dev));
+    int ordinal = 0;
+    CK_TRY(noalloc_device(&dev, &ordinal));
+    // Calls on one device are serialised here and each returns only after its
+    // kernel has finished, so within this process two calls never use the
+    // device's arrays at the same time; calls on different devices run in
+    // parallel (each device has its own copy of the arrays).
+    std::lock_guard<std::mutex> lock(dev->lock);
+    CK_TRY(noalloc_setup(*dev, ordinal));
     if (M == 0) return CK_OK;
     const int64_t cap = (int64_t)dev->sms * 8 * NOALLOC_THREADS;
     if (threads > cap) threads = cap;

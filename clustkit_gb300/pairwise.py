@@ -190,6 +190,9 @@ def compute_pairwise_alignment(candidate_pairs, encoded_sequences, lengths, thre
 
     if device != "cpu":
         # clustkit's GPU branch (single device, "auto" or "0,1"): CuPy semantics.
+        # clustkit's "auto" times one CPU thread against its GPU path and, with
+        # CuPy present, lands on the GPU (pairwise.py:853-946); this library
+        # takes that outcome without timing anything.
         if "," in str(device):
             n_dev = len(str(device).split(","))
             m = len(candidate_pairs)

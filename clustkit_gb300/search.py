@@ -236,8 +236,6 @@ class _Slot:
         self.d_sims = torch.empty(Q * K, dtype=torch.float32, device=dev)
         self.d_scores = torch.empty(Q * K, dtype=torch.int32, device=dev)
         self.d_mask = torch.empty(Q * K, dtype=torch.uint8, device=dev)
-        self.d_slotq = torch.arange(Q, dtype=torch.int32, device=dev).repeat_interleave(K)
-        self.d_col = torch.arange(K, dtype=torch.int32, device=dev).repeat(Q)
         pin = lambda n, dt: torch.zeros(n, dtype=dt).pin_memory()
         self.h_res = pin(db.arena_residues, torch.uint8)
         self.h_off = pin(Q, torch.int64)
@@ -382,10 +380,8 @@ class _Slot:
         self.last_band = (int(sc.c_sw_band_width) if sc.use_c_sw else
                           int(sc.band_width) if sc.band_width is not None else db.band_width)
         # dense pair list: (query, target) or (empty, empty) past a query's candidates
-        q = self.d_slotq[:M]
-        valid = self.d_col[:M] < self.d_n[:nq].repeat_interleave(K)
-        self.d_pairs[:M, 0] = torch.where(valid, q + self.seq0, torch.full_like(q, db.empty_idx))
-        self.d_pairs[:M, 1] = torch.where(valid, self.d_targets[:M], torch.full_like(q, db.empty_idx))
+        _lib.check(lib.ck_search_pairs_device(nq, K, self.seq0, db.empty_idx, self.d_n.data_ptr(),
+                                              self.d_targets.data_ptr(), self.d_pairs.data_ptr(), st))
         _lib.check(lib.ck_sw_batch_device_ctx(
             ctx, self.d_pairs.data_ptr(), M, db.d_flat.data_ptr(), db.flat_len,
             db.d_offsets.data_ptr(), db.d_lengths.data_ptr(), db.n_all, self.last_band,
@@ -678,6 +674,19 @@ def search_kmer_index(db_index, query_dataset, threshold: float = 0.5, top_k: in
     return SearchResults(hits, nq, nd, n_cands, n_cands, time.perf_counter() - start)
 
 
+def batch_bytes(db, queries, max_cands: int) -> int:
+    """Device bytes a search batch of these queries occupies while it runs:
+    its residues and query table, the Phase-A hit counts (one int32 per
+    database sequence per query), the candidate list with its scores and
+    diagonals, the dense pair list and the SW outputs, and the batched SW
+    engine's per-pair sort and fallback scratch."""
+    nq = len(queries)
+    res = int(sum(int(np.asarray(q).size) for q in queries))
+    M = nq * int(max_cands)
+    return (res + nq * 12 + nq * db.n * 4 + M * (4 + 4 + 4) + M * 8 + M * (4 + 4 + 1)
+            + M * (4 * 4 + 4))
+
+
 @dataclass
 class _Request:
     query: np.ndarray
@@ -693,13 +702,25 @@ class SearchServer:
     library context and a pre-sized region of device memory -- is free, up to
     the slot's query and residue capacity; batches in different slots overlap
     on the device.  The number of slots is bounded by free device memory at
-    start-up.  Each request's future resolves to its list of SearchHit (query
-    index 0) when its batch completes; latency is recorded per request.
+    start-up.
+
+    Admission is also by device memory: a batch's footprint (``batch_bytes``:
+    its residues, its per-query Phase-A counts over the database, its
+    candidate and pair lists and the SW engine's per-pair scratch) is taken
+    from a byte budget while it runs and returned when it completes.  A batch
+    is formed only from queued requests that fit both the slot and what is
+    left of the budget; a request that does not fit waits (a deferral) until
+    running batches return their bytes, and one that cannot fit beside any
+    other runs alone.  ``mem_budget`` defaults to the device memory that is
+    free once the slots are allocated plus what the slots hold -- the slots
+    are then the binding limit -- and a smaller budget caps the concurrent
+    work by bytes.  Each request's future resolves to its list of SearchHit
+    (query index 0) when its batch completes; latency is recorded per request.
     """
 
     def __init__(self, db: DeviceDatabase, top_k: int = 10, max_cands: int = 500,
                  min_total_hits: int = 2, max_batch: int | None = None, use_graphs: bool = True,
-                 kmer_score_thresh: int = 13, **scoring):
+                 kmer_score_thresh: int = 13, mem_budget: int | None = None, **scoring):
         torch = _torch()
         self.db = db
         self.top_k = top_k
@@ -719,7 +740,7 @@ class SearchServer:
         n_slots = int(max(1, min(db.slots, (free // 2) // max(per_slot, 1))))
         self.slots = [_Slot(db, i, max_cands) for i in range(n_slots)]
         self.free = list(self.slots)
-        self.busy: list[tuple[_Slot, list[_Request]]] = []
+        self.busy: list[tuple[_Slot, list[_Request], int]] = []  # slot, requests, bytes held
         self.queue: collections.deque[_Request] = collections.deque()
         self.cv = threading.Condition()
         self.running = False
@@ -738,6 +759,16 @@ class SearchServer:
             s.launch(warm, min_total_hits, self.kmer_score_thresh, **self.scoring)
             s.event.synchronize()
             s.results(1)
+        self.per_slot_bytes = per_slot
+        if mem_budget is None:
+            mem_budget = int(torch.cuda.mem_get_info(db.dev)[0]) + n_slots * per_slot
+        self.mem_budget = int(mem_budget)
+        self.in_flight_bytes = 0
+        self.peak_in_flight_bytes = 0
+        self.deferrals = 0
+
+    def batch_bytes(self, queries) -> int:
+        return batch_bytes(self.db, queries, self.max_cands)
 
     def start(self):
         self.running = True
@@ -788,29 +819,41 @@ class SearchServer:
                     return
             progressed = False
             still = []
-            for slot, reqs in self.busy:
+            for slot, reqs, nbytes in self.busy:
                 if slot.event.query():
                     self._finish(slot, reqs)
                     self.free.append(slot)
+                    self.in_flight_bytes -= nbytes
                     progressed = True
                 else:
-                    still.append((slot, reqs))
+                    still.append((slot, reqs, nbytes))
             self.busy = still
             batch: list[_Request] = []
+            need = 0
             with self.cv:
                 if self.free and self.queue:
                     res = 0
-                    while (self.queue and len(batch) < self.max_batch and
-                           res + self.queue[0].query.size <= self.db.arena_residues):
+                    left = self.mem_budget - self.in_flight_bytes
+                    while self.queue and len(batch) < self.max_batch:
+                        q = self.queue[0].query
+                        if res + q.size > self.db.arena_residues:
+                            break
+                        grown = self.batch_bytes([r.query for r in batch] + [q])
+                        if grown > left and (batch or self.busy):
+                            self.deferrals += 1  # waits for running batches to return their bytes
+                            break
                         r = self.queue.popleft()
-                        res += r.query.size
+                        res += q.size
+                        need = grown
                         batch.append(r)
             if batch:
                 slot = self.free.pop()
                 try:
                     slot.launch([r.query for r in batch], self.min_total_hits, self.kmer_score_thresh,
                                 **self.scoring)
-                    self.busy.append((slot, batch))
+                    self.busy.append((slot, batch, need))
+                    self.in_flight_bytes += need
+                    self.peak_in_flight_bytes = max(self.peak_in_flight_bytes, self.in_flight_bytes)
                 except Exception as e:
                     for r in batch:
                         r.future.set_exception(e)
@@ -818,8 +861,7 @@ class SearchServer:
                 progressed = True
             if not progressed:
                 with self.cv:
-                    if not self.queue or not self.free:
-                        self.cv.wait(timeout=0.0002)
+                    self.cv.wait(timeout=0.0002)
 
     def latency_percentiles(self):
         a = np.array(self.latencies)

@@ -8,17 +8,24 @@ GB300 counterparts of "bin edges, band tiling and CTA shape":
   calls the pairs with at least ``wave_min_rows`` rows, raised (when
   ``wave_adaptive``) to where a pair's one-lane time would pass the call's
   expected time;
-* band tiling -- rows a lane keeps in registers per strip (8, 16, 24; the
-  library's default 0 picks 8 for half-widths up to 64, else 16);
-* strip variant -- prefetch distance (1 or 2 columns) and interior unroll
-  (2 or 4 columns), i.e. the shape of a lane's inner loop.
+* band tiling -- rows a lane keeps in registers per strip (8, 16, 24, 32;
+  the library's default 0 picks 8 for half-widths up to 64, else 16);
+* strip variant -- interior columns in groups of 2 or 4 (one first-maximum
+  vote per group), aligned with base-pointer addressing or not, i.e. the
+  shape of a lane's inner loop;
+* CTA shape -- resident 256-thread CTAs per SM for strips of up to 16 rows
+  (2 at <= 128 registers a thread, or 1 with up to 255; taller strips run 1),
+  which sets the warps per SM and the lanes' scratch windows in flight.
 
 ``autotune`` times candidates on the caller's own pairs (device-resident,
-CUDA events around the whole call, L2 flushed between runs) by coordinate
-descent -- bin edge, then tiling x variant, then the bin edge again -- and
-returns the fastest setting with the table of every trial.  Settings are
-process-wide (``apply``); every setting gives identical results, only the
-time changes.  Results are cached per (band width, length profile).
+CUDA events around the whole call, L2 flushed between runs, the median of
+``repeats`` runs) by coordinate descent -- bin edge, then tiling x variant x
+CTA shape, then the bin edge again.  The fastest candidate is then timed
+again against the default, alternating the two, and replaces the default only
+when it is at least ``min_gain`` (2 %) faster there, so a noisy trial never
+leaves a slower setting in place.  Settings are process-wide (``apply``);
+every setting gives identical results, only the time changes.  Results are
+cached per (band width, length profile).
 """
 from __future__ import annotations
 
@@ -33,17 +40,20 @@ from .cells import band_cells, effective_band
 KEYS = {
     "rows_per_strip": _lib.CFG_ROWS_PER_STRIP,
     "strip_variant": _lib.CFG_STRIP_VARIANT,
+    "ctas_per_sm": _lib.CFG_CTAS_PER_SM,
     "wave_min_rows": _lib.CFG_WAVE_MIN_ROWS,
     "wave_all_below": _lib.CFG_WAVE_ALL_BELOW,
     "wave_adaptive": _lib.CFG_WAVE_ADAPTIVE,
 }
 
-DEFAULT = {"rows_per_strip": 0, "strip_variant": 1, "wave_min_rows": 512, "wave_all_below": 40960,
-           "wave_adaptive": 1}
+DEFAULT = {"rows_per_strip": 0, "strip_variant": 1, "ctas_per_sm": 0, "wave_min_rows": 512,
+           "wave_all_below": 40960, "wave_adaptive": 1}
 
 # bin-edge candidates: (wave_min_rows, wave_adaptive); 1 << 30 = never by length
 BIN_EDGES = [(512, 1), (256, 1), (512, 0), (1024, 0), (2048, 0), (4096, 0), (1 << 30, 0)]
-TILINGS = [(r, v) for r in (8, 16, 24) for v in (0, 1, 2, 3)]
+# (rows per strip, strip variant, CTAs per SM); strips of 24 or 32 rows always run 1 CTA per SM
+TILINGS = ([(r, v, c) for r in (8, 16) for v in (0, 1, 2, 3) for c in (1, 2)] +
+           [(r, v, 1) for r in (24, 32) for v in (0, 1)])
 
 _cache: dict = {}
 
@@ -64,6 +74,7 @@ class TuneResult:
     gcups: float
     cells: int
     trials: list = field(default_factory=list)  # (config, ms)
+    confirm: dict = field(default_factory=dict)  # the winner re-timed against the default
 
 
 class _DeviceCall:
@@ -97,11 +108,12 @@ class _DeviceCall:
             o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), o[3].data_ptr(), o[4].data_ptr(),
             self.stream.cuda_stream))
 
-    def time_ms(self, repeats=2, warmup=1, engine=0) -> float:
+    def time_ms(self, repeats=5, warmup=1, engine=0) -> float:
+        """Median of `repeats` timed calls after `warmup` untimed ones."""
         torch = self.torch
         for _ in range(warmup):
             self.run(engine)
-        best = float("inf")
+        times = []
         for k in range(repeats):
             self.flush.fill_(k & 0xFF)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -109,9 +121,9 @@ class _DeviceCall:
             self.run(engine)
             b.record(self.stream)
             b.synchronize()
-            best = min(best, a.elapsed_time(b))
+            times.append(a.elapsed_time(b))
         _lib.check(self.lib.ck_sw_status_device(self.stream.cuda_stream))
-        return best
+        return float(np.median(times))
 
     def results(self):
         return {k: t.cpu().numpy() for k, t in zip(("sims", "scores", "matches", "shorter", "mask"), self.out)}
@@ -126,9 +138,22 @@ def profile_key(lengths, pairs, band_width):
     return (int(band_width), tuple(int(np.log2(max(x, 1))) for x in q), int(np.log2(max(len(p), 1))))
 
 
-def autotune(pairs, flat, offsets, lengths, band_width: int, repeats: int = 2,
-             use_cache: bool = True, apply_best: bool = True) -> TuneResult:
-    """Time the engine's settings on these pairs and return (and apply) the fastest."""
+def confirm(call, candidate: dict, base: dict, rounds: int = 3, repeats: int = 5) -> dict:
+    """Time the candidate and the base setting alternately (rounds x repeats
+    runs each, medians of the per-round medians) on the same call."""
+    t_c, t_b = [], []
+    for _ in range(rounds):
+        apply(base)
+        t_b.append(call.time_ms(repeats))
+        apply(candidate)
+        t_c.append(call.time_ms(repeats))
+    return {"candidate_ms": float(np.median(t_c)), "default_ms": float(np.median(t_b))}
+
+
+def autotune(pairs, flat, offsets, lengths, band_width: int, repeats: int = 5,
+             use_cache: bool = True, apply_best: bool = True, min_gain: float = 0.02) -> TuneResult:
+    """Time the engine's settings on these pairs and return (and apply) the
+    fastest, which must beat the default by ``min_gain`` on a re-time."""
     key = profile_key(lengths, pairs, band_width)
     if use_cache and key in _cache:
         res = _cache[key]
@@ -143,8 +168,9 @@ def autotune(pairs, flat, offsets, lengths, band_width: int, repeats: int = 2,
     cells = int(band_cells(la, lb, effective_band(la, lb, band_width)).sum())
     keep = current()
     trials = []
-    best = dict(keep)
+    best = dict(DEFAULT)
     best_ms = None
+    chk = {}
 
     def trial(cfg):
         nonlocal best, best_ms
@@ -159,16 +185,24 @@ def autotune(pairs, flat, offsets, lengths, band_width: int, repeats: int = 2,
         for mr, ad in BIN_EDGES:
             trial({**base, "wave_min_rows": mr, "wave_adaptive": ad})
         edge = {k: best[k] for k in ("wave_min_rows", "wave_adaptive")}
-        for r, v in TILINGS:
-            trial({**base, **edge, "rows_per_strip": r, "strip_variant": v})
-        tiling = {k: best[k] for k in ("rows_per_strip", "strip_variant")}
+        for r, v, c in TILINGS:
+            trial({**base, **edge, "rows_per_strip": r, "strip_variant": v, "ctas_per_sm": c})
+        tiling = {k: best[k] for k in ("rows_per_strip", "strip_variant", "ctas_per_sm")}
         for mr, ad in BIN_EDGES:
             cfg = {**base, **tiling, "wave_min_rows": mr, "wave_adaptive": ad}
             if not any(c == cfg for c, _ in trials):
                 trial(cfg)
+        if best != DEFAULT:
+            chk = confirm(call, best, DEFAULT)
+            if chk["candidate_ms"] > (1.0 - min_gain) * chk["default_ms"]:
+                best, best_ms = dict(DEFAULT), chk["default_ms"]
+                chk["kept"] = "default"
+            else:
+                best_ms = chk["candidate_ms"]
+                chk["kept"] = "candidate"
     finally:
         apply(keep)
-    res = TuneResult(best, best_ms, cells / (best_ms * 1e-3) / 1e9 if best_ms else 0.0, cells, trials)
+    res = TuneResult(best, best_ms, cells / (best_ms * 1e-3) / 1e9 if best_ms else 0.0, cells, trials, chk)
     _cache[key] = res
     if apply_best:
         apply(best)

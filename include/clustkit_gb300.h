@@ -130,10 +130,13 @@ int32_t ck_sw_batch_device(const int32_t *d_pairs, int64_t M, const uint8_t *d_f
  *   - Blocking: enqueues on `stream`, waits for it, and returns
  *     CK_ERR_OUT_OF_RANGE if a pair index or sequence extent was bad.
  *   - The first call on a device looks up the static arrays' device
- *     addresses; make that first call before any stream capture.
- *   - Every call shares the static arrays (which keep the last call's
- *     contents); calls that overlap on the GPU, e.g. from two streams or
- *     threads, race on them. */
+ *     addresses; make that first call before any stream capture.  Not for
+ *     use on a device after cudaDeviceReset in the same process.
+ *   - Every call on a device shares that device's static arrays (which keep
+ *     the last call's contents).  Calls on one device are serialised by a
+ *     lock held until the kernel has finished, so calls from several threads
+ *     or streams of this process never overlap on them; calls on different
+ *     devices do not wait for each other. */
 int32_t ck_sw_batch_device_noalloc(const int32_t *d_pairs, int64_t M, const uint8_t *d_flat,
                                    int64_t flat_len, const int64_t *d_offsets,
                                    const int32_t *d_lengths, int64_t n_seqs, int32_t band_width,
@@ -168,11 +171,13 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 /* Tunables of the batched engine, process-wide (the autotuner in
  * clustkit_gb300/tune.py picks them per workload):
  *   CK_CFG_ROWS_PER_STRIP  rows a lane keeps in registers per strip: 8, 16, 24,
- *                          or 0 (default) for 8 when the band half-width is
- *                          <= 64, else 16
- *   CK_CFG_STRIP_VARIANT   0..3: bit 0 prefetches the next columns' inputs two
- *                          columns ahead (else one), bit 1 runs interior
- *                          columns four at a time (else two)
+ *                          32, or 0 (default) for 8 when the band half-width
+ *                          is <= 64, else 16
+ *   CK_CFG_STRIP_VARIANT   0..3: bit 1 runs interior columns in groups of
+ *                          four (else two), with one first-maximum vote per
+ *                          group; bit 0 aligns the groups and addresses each
+ *                          group's window slots and residues from two base
+ *                          pointers (else each column its own)
  *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs to align (the
  *                          count is taken on the device, after empty and
  *                          skipped pairs) run every pair one warp per pair
@@ -194,7 +199,11 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *                          4, 8 or 16: at least that many
  *                          (key 7, a cluster-shared-memory form of the
  *                          similar-k-mer posting walk, is retired: it
- *                          measured 2.6x slower than the L2-atomic walk) */
+ *                          measured 2.6x slower than the L2-atomic walk)
+ *   CK_CFG_CTAS_PER_SM     resident 256-thread CTAs per SM of the strip
+ *                          kernel for strips of 8 or 16 rows: 2 (default, 0)
+ *                          at most 128 registers a thread, or 1 (up to 255);
+ *                          strips of 24 or 32 rows always run 1 */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
@@ -202,6 +211,7 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 #define CK_CFG_WAVE_ADAPTIVE 4
 #define CK_CFG_WAVE_STREAM 5
 #define CK_CFG_WAVE_ROWS 6
+#define CK_CFG_CTAS_PER_SM 8
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 
@@ -254,6 +264,42 @@ int32_t ck_sw_batch_device_ctx(int32_t ctx, const int32_t *d_pairs, int64_t M, c
                                const int32_t *d_diag_hints, int32_t pass_rule, int32_t engine,
                                float *d_sims, int32_t *d_scores, int32_t *d_matches,
                                int32_t *d_shorter, uint8_t *d_mask, void *stream);
+
+/* Resident database and asynchronous submit/poll on a context, for hosts
+ * that drive batches without a Python runtime.  Replaces, for such hosts,
+ * clustkit's synchronous ctypes call into batch_sw_align_c
+ * (clustkit/pairwise.py:50-58, :69-108 -> csrc/sw_align.c:182-266): the
+ * sequences go to the device once, then each batch is only its pairs.
+ *
+ * ck_ctx_upload_db copies flat / offsets / lengths (host buffers, clustkit's
+ * compact layout) into device memory owned by the context, replacing any
+ * earlier database; synchronous.
+ *
+ * ck_ctx_submit enqueues on `stream` (NULL: the default stream): the copy of
+ * the batch's pairs (and hints) to the device, the alignment against the
+ * resident database, and the copies of the outputs into the caller's host
+ * buffers (any of them NULL to skip), then returns without waiting.  One
+ * submission per context may be in flight; another submit or an upload
+ * before it completes returns CK_ERR_INVALID_ARGUMENT.  Every host buffer of
+ * the call must stay valid and unmodified until ck_ctx_poll reports it done.
+ * With page-locked host buffers (cudaHostAlloc / cudaHostRegister) the call
+ * returns at once; with pageable ones the CUDA runtime copies synchronously
+ * and the call returns when the outputs have landed.
+ *
+ * ck_ctx_poll sets *out_done to 0 while the submission runs; once it has
+ * finished (or when none is in flight) it sets 1 and returns the
+ * submission's status: CK_OK, or CK_ERR_OUT_OF_RANGE when a pair index or a
+ * sequence extent was outside the database.  ck_ctx_wait blocks until the
+ * submission has finished and returns the same status.
+ * Results are those of ck_sw_batch with the same arguments. */
+int32_t ck_ctx_upload_db(int32_t ctx, const uint8_t *flat, int64_t flat_len, const int64_t *offsets,
+                         const int32_t *lengths, int64_t n_seqs);
+int32_t ck_ctx_submit(int32_t ctx, const int32_t *pairs, int64_t M, int32_t band_width,
+                      const int8_t *sub_matrix, float threshold, const int32_t *diag_hints,
+                      int32_t pass_rule, int32_t engine, float *out_sims, int32_t *out_scores,
+                      int32_t *out_matches, int32_t *out_shorter, uint8_t *out_mask, void *stream);
+int32_t ck_ctx_poll(int32_t ctx, int32_t *out_done);
+int32_t ck_ctx_wait(int32_t ctx);
 
 /* ------------------------------------------------------ search: k-mer index
  * CSR inverted index in clustkit's layout (clustkit/kmer_index.py:117-166),
@@ -376,6 +422,18 @@ int32_t ck_connected_components_device(int32_t ctx, const int32_t *d_pairs, int6
                                        int32_t *d_labels, int64_t *out_n_components, int32_t *out_rounds,
                                        void *stream);
 
+/* The dense pair list of a search batch, for ck_sw_batch_device_ctx: entry
+ * q * max_cands + c of d_pairs (int32 [nq * max_cands][2]) becomes
+ * (seq0 + q, d_targets[q * max_cands + c]) for the query's first d_n[q]
+ * candidates and (empty_idx, empty_idx) after them -- empty_idx names a
+ * sequence of length 0, which aligns to nothing.  The candidate lists are
+ * the ones the search scorers write (d_targets int32 [nq][max_cands], d_n
+ * int32 [nq]).  Replaces the per-query loop of clustkit/kmer_index.py:
+ * 2230-2266 that gathers (query, target) pairs for the SW call.
+ * Asynchronous on `stream`. */
+int32_t ck_search_pairs_device(int32_t nq, int32_t max_cands, int32_t seq0, int32_t empty_idx,
+                               const int32_t *d_n, const int32_t *d_targets, int32_t *d_pairs,
+                               void *stream);
 /* Phase-A k-mer scoring of a query batch (clustkit/kmer_index.py:470-534 with
  * the per-query cap of :858-902): hits per database sequence from the query's
  * valid k-mers with frequency <= freq_thresh, saturating at 32767; targets with
@@ -406,6 +464,16 @@ int32_t ck_search_phase_a_device(int32_t ctx, const uint8_t *d_qflat, int64_t qf
  * 3 = __viaddmax_s16x2 (2 lane-ops per instruction), 4 = 3-input logic op,
  * 5 = 32-bit multiply-add.  Writes lane-ops/s. */
 int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s);
+/* DP cells per second of three forms of the Smith-Waterman cell, each run as
+ * the strip kernel runs it (16 rows a lane, register state, increments from
+ * shared memory) but without the kernel's window, residue stream and
+ * first-maximum tracking: form 0 = the exact int32 packed key this library
+ * uses; 1 = int16x2 score only (two pairs a lane; no match count, so not
+ * usable for clustkit's identity); 2 = int16x2 with match counts carried in
+ * a second int16x2 register and picked by compare masks (what exact tracking
+ * at two pairs a lane costs).  A measurement of the cell arithmetic, no
+ * counterpart in clustkit. */
+int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s);
 
 #ifdef __cplusplus
 }

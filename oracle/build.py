@@ -32,8 +32,13 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-# Location of the reference checkout; only this build script reads it.
-REF_SRC = Path(os.environ.get("CLUSTKIT_REFERENCE", "/root/reference")) / "clustkit" / "csrc" / "sw_align.c"
+# Root of the clustkit reference checkout: the CLUSTKIT_REFERENCE environment
+# variable, else the location where the build container mounts it.  This
+# recipe and tests/golden/make_golden.py (which takes it from here) are the
+# only readers; nothing at run time needs the checkout, and without it the
+# reference-built checkers are simply not produced.
+REF_ROOT = Path(os.environ.get("CLUSTKIT_REFERENCE", "/root/reference"))
+REF_SRC = REF_ROOT / "clustkit" / "csrc" / "sw_align.c"
 
 CFLAGS = ["-O3", "-fopenmp", "-shared", "-fPIC", "-std=c11"]
 

@@ -1,7 +1,8 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout where the clustkit reference is mounted (path in
-CLUSTKIT_REFERENCE, default /root/reference):
+Run where the clustkit reference checkout is available (its root is
+oracle/build.py's REF_ROOT: the CLUSTKIT_REFERENCE environment variable, else
+the build container's mount point):
 
     python tests/golden/make_golden.py
 
@@ -41,7 +42,11 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REF_ROOT = Path(os.environ.get("CLUSTKIT_REFERENCE", "/root/reference"))
+sys.path.insert(0, str(REPO))
+from oracle.build import REF_ROOT  # noqa: E402
+
+if not (REF_ROOT / "clustkit" / "pairwise.py").exists():
+    raise SystemExit(f"clustkit reference checkout not found at {REF_ROOT}; set CLUSTKIT_REFERENCE")
 
 
 # --------------------------------------------------------------------------- numba stand-in

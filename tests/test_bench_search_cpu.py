@@ -42,3 +42,25 @@ def test_search_summary_ratios():
     assert summ["similar"]["server_vs_host_cores"] == 880.0 / 44.0
     assert "host_cores_qps" not in summ["c_path"]
     assert summ["c_path"]["server_low_rate"]["p99_ms"] == 2.0
+
+
+def test_exact_mode_host_chain_is_phase_a_then_unhinted_sw():
+    """The exact-5-mer host baseline's scorer call (the C scorer with Phase B
+    off) gives clustkit's Phase A survivors, and the chain runs end to end."""
+    import types
+
+    import bench
+    import oracle
+    s = synth.generate_families(60, 5, median=150, lo=40, hi=300, seed=32)
+    off, ent, fr = so.build_kmer_index(s.flat, s.offsets, s.lengths, 5)
+    ft = so.compute_freq_threshold(fr, s.n, 99.5)
+    qs = [s.seq(i).copy() for i in (1, 9, 44, 120)]
+    lens = np.array([len(q) for q in qs], np.int32)
+    got = oracle.kmer_candidates_batch(np.concatenate(qs), np.concatenate([[0], np.cumsum(lens[:-1])]), lens,
+                                       5, 20, off, ent, fr, ft, s.n, 2, 0, 10, 20, 10000)
+    for q, (ids, sc, dg) in zip(qs, got):
+        want = so.phase_a(q, 5, 20, off, ent, fr, ft, s.n, 2, 20)
+        assert np.array_equal(ids, want[0]) and np.array_equal(sc, want[1]) and not dg.any()
+    db = types.SimpleNamespace(index_arrays=lambda: (off, ent, fr), freq_thresh=ft, band_width=40)
+    base = bench.search_cpu_baseline(db, s, qs * 8, target_s=0.01, mode="exact")
+    assert base["value"] > 0 and base["unit"] == "queries/s" and "470-534" in base["source"]

@@ -225,6 +225,36 @@ def test_server_results_same_alone_and_in_mix(ck, monkeypatch, use_graphs, thres
 
 
 @pytest.mark.gpu
+def test_server_memory_budget_defers_and_keeps_results(ck):
+    """A device-memory budget smaller than two full batches: the server never
+    holds more than the budget in flight, defers requests until running
+    batches return their bytes, and every query's hits are the same as when
+    it is searched alone."""
+    from clustkit_gb300.search import DeviceDatabase, SearchServer, batch_bytes, search_batch
+    db_set = synth.generate_families(400, 10, median=200, lo=40, hi=600, seed=94)
+    db = DeviceDatabase(db_set.flat, db_set.offsets, db_set.lengths, arena_slots=3, arena_queries=16,
+                        arena_residues=16 * 600)
+    rng = np.random.default_rng(7)
+    qs = [db_set.seq(int(i)).copy() for i in rng.choice(db_set.n, 48, replace=False)]
+    alone = [search_batch(db, [q], top_k=10, kmer_score_thresh=0)[0] for q in qs]
+    budget = int(1.5 * batch_bytes(db, qs[:8], 500))  # room for one full batch, not two
+    server = SearchServer(db, top_k=10, max_batch=8, use_graphs=False, kmer_score_thresh=0,
+                          mem_budget=budget).start()
+    try:
+        futs = [server.submit(q) for q in qs]
+        mixed = [f.result(timeout=120) for f in futs]
+    finally:
+        server.stop()
+    assert len(server.slots) >= 2  # slots alone would let batches overlap
+    assert server.deferrals > 0
+    assert 0 < server.peak_in_flight_bytes <= budget
+    assert server.in_flight_bytes == 0
+    for a, b in zip(alone, mixed):
+        assert [(h.target, h.identity, h.score, h.rank) for h in a] == \
+            [(h.target, h.identity, h.score, h.rank) for h in b]
+
+
+@pytest.mark.gpu
 def test_frozen_context_refuses_to_grow(ck):
     """A frozen context (its buffers may sit in a captured graph) keeps
     working at the sizes it has and fails, instead of reallocating, beyond."""

@@ -45,3 +45,14 @@ def test_ranking_pass_matches_lexsort(monkeypatch):
         want = _lexsort_hits(nq, K, n, tg.reshape(nq, K), sims.reshape(nq, K), scores.reshape(nq, K),
                              mask.reshape(nq, K), lens, lh, top_k)
         assert [[(h.target, h.identity, h.score, h.rank) for h in g] for g in got] == want, trial
+
+
+def test_batch_bytes_grows_with_queries_residues_and_candidates():
+    from clustkit_gb300.search import batch_bytes
+    db = types.SimpleNamespace(n=1000)
+    q = [np.zeros(300, np.uint8)] * 4
+    b4 = batch_bytes(db, q, 500)
+    assert batch_bytes(db, q * 2, 500) == 2 * b4
+    assert batch_bytes(db, q, 500) < batch_bytes(db, q, 600)
+    assert batch_bytes(db, [np.zeros(301, np.uint8)] + q[1:], 500) == b4 + 1
+    assert batch_bytes(db, [], 500) == 0

@@ -72,16 +72,19 @@ def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist, route):
     assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
 
 
-@pytest.mark.parametrize("rows,variant", [(8, 0), (16, 0), (24, 0), (16, 1), (16, 2), (16, 3), (8, 3),
-                                          (24, 3)])
+@pytest.mark.parametrize("rows,variant,ctas", [(8, 1, 2), (16, 1, 2), (24, 1, 1), (16, 3, 2), (8, 3, 2),
+                                               (24, 3, 1), (16, 1, 1), (16, 3, 1), (8, 1, 1), (32, 1, 1),
+                                               (32, 3, 1), (16, 0, 2), (16, 2, 2), (8, 0, 1), (32, 0, 1),
+                                               (24, 2, 1)])
 @pytest.mark.parametrize("bw", [3, 32, 100, 0])
-def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
-    from clustkit_gb300._lib import (CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, CFG_WAVE_ALL_BELOW,
-                                     CFG_WAVE_MIN_ROWS, get_config, set_config)
-    keep = (get_config(CFG_ROWS_PER_STRIP), get_config(CFG_STRIP_VARIANT))
+def test_rows_per_strip_settings(ck, golden, rows, variant, ctas, bw):
+    from clustkit_gb300._lib import (CFG_CTAS_PER_SM, CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, get_config,
+                                     set_config)
+    keys = (CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, CFG_CTAS_PER_SM)
+    keep = [get_config(k) for k in keys]
     try:
-        set_config(CFG_ROWS_PER_STRIP, rows)
-        set_config(CFG_STRIP_VARIANT, variant)
+        for k, v in zip(keys, (rows, variant, ctas)):
+            set_config(k, v)
         with wave_config(all_below=0, min_rows=1 << 30):  # strip kernel only
             g = golden("sw_golden.npz")
             r = batch_sw(g["pairs"], g["flat"], g["offsets"], g["lengths"], bw, BLOSUM62)
@@ -93,8 +96,8 @@ def test_rows_per_strip_settings(ck, golden, rows, variant, bw):
                   oracle.sw_batch(pairs, s.flat, s.offsets, s.lengths, bw, BLOSUM62))
             assert ck.sw_counters()["batched"] > 0
     finally:
-        set_config(CFG_ROWS_PER_STRIP, keep[0])
-        set_config(CFG_STRIP_VARIANT, keep[1])
+        for k, v in zip(keys, keep):
+            set_config(k, v)
 
 
 @contextlib.contextmanager

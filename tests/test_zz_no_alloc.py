@@ -23,11 +23,12 @@ from clustkit_gb300.pairwise import ENGINE_BATCHED, PASS_CPU
 pytestmark = pytest.mark.gpu
 
 
-def _device_run(lib, torch, fn_name, data, pairs, bw, threshold, noalloc):
+def _device_run(lib, torch, data, pairs, bw, threshold, noalloc, hints=None):
     dev = torch.device("cuda:0")
     s = data
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     d_pairs, d_flat, d_off, d_len = T(pairs), T(s.flat), T(s.offsets), T(s.lengths)
+    d_hints = None if hints is None else T(hints)
     M = len(pairs)
     out = {k: torch.full((M,), 7, dtype=dt, device=dev) for k, dt in
            (("sims", torch.float32), ("scores", torch.int32), ("matches", torch.int32),
@@ -35,9 +36,11 @@ def _device_run(lib, torch, fn_name, data, pairs, bw, threshold, noalloc):
     sub = np.ascontiguousarray(BLOSUM62)
     stream = torch.cuda.current_stream().cuda_stream
     common = (d_pairs.data_ptr(), M, d_flat.data_ptr(), len(s.flat), d_off.data_ptr(), d_len.data_ptr(),
-              s.n, bw, sub.ctypes.data, float(threshold), None, PASS_CPU)
+              s.n, bw, sub.ctypes.data, float(threshold), None if d_hints is None else d_hints.data_ptr(),
+              PASS_CPU)
     outs = (out["sims"].data_ptr(), out["scores"].data_ptr(), out["matches"].data_ptr(),
             out["shorter"].data_ptr(), out["mask"].data_ptr(), stream)
+    torch.cuda.synchronize()
     if noalloc:
         st = lib.ck_sw_batch_device_noalloc(*common, *outs)
         assert st == 0, lib.ck_last_error()
@@ -49,19 +52,66 @@ def _device_run(lib, torch, fn_name, data, pairs, bw, threshold, noalloc):
     return {k: v.cpu().numpy() for k, v in out.items()}
 
 
+def _hints(data, pairs, seed):
+    """Diagonal hints across the whole range, some beyond +-shorter (clamped to 0)."""
+    rng = np.random.default_rng(seed)
+    sh = np.minimum(data.lengths[pairs[:, 0]], data.lengths[pairs[:, 1]])
+    h = (rng.integers(-3000, 3000, len(pairs)) % (2 * sh + 41) - sh - 20).astype(np.int32)
+    h[rng.random(len(pairs)) < 0.3] = 0
+    return h
+
+
 def test_noalloc_matches_device_entry_point_twice(ck):
+    """The allocation-free entry point first (before the allocating one in each
+    case), then the regular device entry point on the same inputs: equal
+    outputs, on calls in a row with different shapes, with and without
+    diagonal hints, up to the widest band the static workspace takes."""
     torch = pytest.importorskip("torch")
     lib = ck.load()
     cases = [
-        (synth.generate_families(30, 8, median=300, lo=30, hi=900, seed=71), 100, 0.3, 6000),
-        (synth.generate_families(25, 6, median=150, lo=20, hi=500, seed=72), 16, 0.5, 4000),
+        (synth.generate_families(30, 8, median=300, lo=30, hi=900, seed=71), 100, 0.3, 6000, False),
+        (synth.generate_families(25, 6, median=150, lo=20, hi=500, seed=72), 16, 0.5, 4000, False),
+        (synth.generate_families(20, 6, median=250, lo=20, hi=700, seed=73), 32, 0.3, 3000, True),
+        (synth.generate_families(4, 3, median=600, lo=100, hi=1500, seed=74), 8191, 0.3, 40, False),
     ]
-    for data, bw, t, n_pairs in cases:  # two calls in a row, different shapes
+    for data, bw, t, n_pairs, hinted in cases:
         pairs = synth.mixed_pairs(data, n_pairs, seed=bw)
-        want = _device_run(lib, torch, "ck_sw_batch_device", data, pairs, bw, t, noalloc=False)
-        got = _device_run(lib, torch, "ck_sw_batch_device_noalloc", data, pairs, bw, t, noalloc=True)
+        hints = _hints(data, pairs, bw) if hinted else None
+        got = _device_run(lib, torch, data, pairs, bw, t, noalloc=True, hints=hints)
+        want = _device_run(lib, torch, data, pairs, bw, t, noalloc=False, hints=hints)
         for k in want:
-            assert np.array_equal(got[k], want[k]), k
+            assert np.array_equal(got[k], want[k]), (bw, k)
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged(ck):
+    """After one call (which may load the library's module and with it the
+    static arrays), further calls take no device memory: cudaMemGetInfo's free
+    bytes are the same before and after."""
+    torch = pytest.importorskip("torch")
+    lib = ck.load()
+    data = synth.generate_families(20, 8, median=300, lo=30, hi=900, seed=75)
+    pairs = synth.mixed_pairs(data, 5000, seed=3)
+    dev = torch.device("cuda:0")
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_pairs, d_flat, d_off, d_len = T(pairs), T(data.flat), T(data.offsets), T(data.lengths)
+    outs = [torch.empty(len(pairs), dtype=dt, device=dev)
+            for dt in (torch.float32, torch.int32, torch.int32, torch.int32, torch.uint8)]
+    sub = np.ascontiguousarray(BLOSUM62)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        st = lib.ck_sw_batch_device_noalloc(d_pairs.data_ptr(), len(pairs), d_flat.data_ptr(), len(data.flat),
+                                            d_off.data_ptr(), d_len.data_ptr(), data.n, 100, sub.ctypes.data,
+                                            0.3, None, PASS_CPU, *[o.data_ptr() for o in outs], stream)
+        assert st == 0, lib.ck_last_error()
+
+    call()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(dev)[0] == free0
 
 
 def test_noalloc_rejects_sizes_beyond_its_workspace(ck):
