@@ -1120,7 +1120,7 @@ def main():
                     help="search leg: only full batches per mode (a warm-up and a few), for profiler launch lists")
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24/32); 0 = library default")
     ap.add_argument("--ctas", type=int, default=0, help="strip kernel CTAs per SM (1/2); 0 = library default")
-    ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default")
+    ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default (by strip height)")
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
     ap.add_argument("--search", choices=["auto", "on", "off", "only"], default="auto",
                     help="search/serving leg (auto: on for the full workload, off with --quick)")

@@ -254,10 +254,8 @@ struct StripRegs {
     int32_t fT[R];     // F key (tie bit set) of row r at the last column done
     uint32_t arow[R];  // byte offset of row r's residue block in the increment table
     int32_t hd0;       // H(i0 - 1, j - 1): diagonal input of the strip's first row
-    int2 bnd_n;        // window entry (row i0 - 1) prefetched for the next column
-    uint32_t bcol_n;   // residue offset of the next column's b, prefetched
-    int2 bnd_n2;       // the same, two columns ahead (prefetch distance 2)
-    uint32_t bcol_n2;
+    int2 bq[4];        // window entries (row i0 - 1) of the next P columns, prefetched
+    uint32_t cq[4];    // residue offsets of the same columns' b
 };
 
 // Structural variants of the strip kernel (picked by the autotuner), all
@@ -269,6 +267,7 @@ struct StripRegs {
 template <int V> struct StripVariant {
     static constexpr int UNROLL = (V & 2) ? 4 : 2;
     static constexpr bool ALIGNED = (V & 1) != 0;
+    static constexpr int PREFETCH = ALIGNED ? 4 : 2;  // columns ahead
 };
 
 // Rows of a strip inside their band at a column, as a bit mask: row r
@@ -445,23 +444,27 @@ __device__ __forceinline__ void strip_track(const int32_t (&hs)[U][R], int32_t &
 }
 
 // The next column's inputs: the window entry (H, E of the row above the
-// strip) and the residue offset of column j, prefetched two columns ahead.
-template <int R>
+// strip) and the residue offset of column j, from the P-deep prefetch queue;
+// column j + P is loaded behind them (its residue clamped to the sequence).
+template <int R, int P>
 __device__ __forceinline__ void column_inputs(int32_t j, int32_t lb, StripRegs<R> &S, const int2 *win,
                                               int32_t wmask, const uint8_t *B, int2 &bnd, uint32_t &bcol) {
-    bnd = S.bnd_n;
-    bcol = S.bcol_n;
-    const int32_t jn = j + 2 < lb ? j + 2 : lb;  // column whose residue is prefetched
-    S.bnd_n = S.bnd_n2;
-    S.bcol_n = S.bcol_n2;
-    S.bnd_n2 = win[(size_t)((j + 2) & wmask) * 32];
-    S.bcol_n2 = (uint32_t)__ldg(B + jn - 1) * 128u;
+    bnd = S.bq[0];
+    bcol = S.cq[0];
+#pragma unroll
+    for (int k = 0; k + 1 < P; ++k) {
+        S.bq[k] = S.bq[k + 1];
+        S.cq[k] = S.cq[k + 1];
+    }
+    const int32_t jn = j + P < lb ? j + P : lb;  // column whose residue is prefetched
+    S.bq[P - 1] = win[(size_t)((j + P) & wmask) * 32];
+    S.cq[P - 1] = (uint32_t)__ldg(B + jn - 1) * 128u;
 }
 
 // U interior columns j .. j + U - 1 (every row inside its band), each
 // addressing its own window slots and residues, then one first-max check
 // over all of them.
-template <int R, int U>
+template <int R, int U, int P>
 __device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripRegs<R> &S, const char *s_inc,
                                                    int2 *win, int32_t wmask, const uint8_t *B, int32_t &tthr,
                                                    int32_t *s_best, int32_t one) {
@@ -470,7 +473,7 @@ __device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripR
     for (int u = 0; u < U; ++u) {
         int2 bnd;
         uint32_t bcol;
-        column_inputs<R>(j + u, lb, S, win, wmask, B, bnd, bcol);
+        column_inputs<R, P>(j + u, lb, S, win, wmask, B, bnd, bcol);
         int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
         S.hd0 = hu;
         strip_cells_from<R>(bcol, hu, eu, hdiag, S, s_inc, one);
@@ -482,27 +485,31 @@ __device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripR
 }
 
 // U interior columns j .. j + U - 1 with j a multiple of U, inputs prefetched
-// two columns ahead (columns j + U and j + U + 1 are loaded here).  W is a
-// power of two >= 32 and U divides it, so the slots of columns j .. j+U-1 are
-// consecutive, and so are those of j+U and j+U+1: two base addresses per
-// group, immediate offsets after them.  The caller runs a group only where
-// j + U + 1 <= lb, so the prefetched residues lie inside the sequence.
-template <int R, int U>
+// P columns ahead.  W is a power of two >= 32 and U divides it, so every run
+// of U columns that starts at a multiple of U has consecutive slots: one base
+// address per run, immediate offsets after it.  The caller runs a group only
+// where j + U - 1 + P <= lb, so the prefetched residues lie inside the
+// sequence.
+template <int R, int U, int P>
 __device__ __forceinline__ void strip_group(int32_t j, StripRegs<R> &S, const char *s_inc, int2 *win,
                                             int32_t wmask, const uint8_t *B, int32_t &tthr, int32_t *s_best,
                                             int32_t one) {
     int2 *cur = win + (size_t)(j & wmask) * 32;
-    const int2 *nxt = win + (size_t)((j + U) & wmask) * 32;
-    const uint8_t *pb = B + j + 1;  // residue of column j + 2 (columns are 1-based)
+    const uint8_t *pb = B + j + P - 1;  // residue of column j + P (columns are 1-based)
     int32_t hs[U][R];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        const int2 bnd = S.bnd_n;
-        const uint32_t bcol = S.bcol_n;
-        S.bnd_n = S.bnd_n2;
-        S.bcol_n = S.bcol_n2;
-        S.bnd_n2 = (u + 2 < U) ? cur[(u + 2) * 32] : nxt[(u + 2 - U) * 32];
-        S.bcol_n2 = (uint32_t)__ldg(pb + u) * 128u;
+        const int2 bnd = S.bq[0];
+        const uint32_t bcol = S.cq[0];
+#pragma unroll
+        for (int k = 0; k + 1 < P; ++k) {
+            S.bq[k] = S.bq[k + 1];
+            S.cq[k] = S.cq[k + 1];
+        }
+        const int c = u + P;  // column j + c is loaded: run c / U of the group's window, offset c % U
+        const int2 *run = win + (size_t)((j + (c / U) * U) & wmask) * 32;
+        S.bq[P - 1] = run[(c % U) * 32];
+        S.cq[P - 1] = (uint32_t)__ldg(pb + u) * 128u;
         int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
         S.hd0 = hu;
         strip_cells_from<R>(bcol, hu, eu, hdiag, S, s_inc, one);
@@ -515,13 +522,13 @@ __device__ __forceinline__ void strip_group(int32_t j, StripRegs<R> &S, const ch
 
 // One column outside the aligned interior groups: a ramp or clipped column
 // (rows klo..khi inside their band) or an interior column at a group's edge.
-template <int R>
+template <int R, int P>
 __device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R> &S, const char *s_inc,
                                              int2 *win, int32_t wmask, const uint8_t *B, int32_t lo0,
                                              int32_t w2, int32_t &tthr, int32_t *s_best, int32_t one) {
     int2 bnd;
     uint32_t bcol;
-    column_inputs<R>(j, lb, S, win, wmask, B, bnd, bcol);
+    column_inputs<R, P>(j, lb, S, win, wmask, B, bnd, bcol);
     int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
     S.hd0 = hu;
     // rows r with lo0 + r <= j <= lo0 + r + 2w are inside their band
@@ -573,10 +580,12 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
             S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
         }
         S.hd0 = (J0 >= 2) ? win[(size_t)((J0 - 1) & wmask) * 32].x : 0;
-        S.bnd_n = win[(size_t)(J0 & wmask) * 32];
-        S.bcol_n = (uint32_t)__ldg(B + J0 - 1) * 128u;
-        S.bnd_n2 = win[(size_t)((J0 + 1) & wmask) * 32];
-        S.bcol_n2 = (uint32_t)__ldg(B + (J0 + 1 < lb ? J0 + 1 : lb) - 1) * 128u;
+        constexpr int P = StripVariant<V>::PREFETCH;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            S.bq[k] = win[(size_t)((J0 + k) & wmask) * 32];
+            S.cq[k] = (uint32_t)__ldg(B + (J0 + k < lb ? J0 + k : lb) - 1) * 128u;
+        }
 
         // Interior columns (every row inside its band) run unmasked in aligned
         // groups of U; ramp and clipped columns, and interior columns at a
@@ -589,14 +598,14 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         constexpr int U = StripVariant<V>::UNROLL;
         constexpr bool ALIGNED = StripVariant<V>::ALIGNED;
         for (int32_t j = J0; j <= J1;) {
-            if (ALIGNED && j >= I0 && (j & (U - 1)) == 0 && j + U - 1 <= I1 && j + U + 1 <= lb) {
-                strip_group<R, U>(j, S, s_inc, win, wmask, B, tthr, s_best, one);
+            if (ALIGNED && j >= I0 && (j & (U - 1)) == 0 && j + U - 1 <= I1 && j + U - 1 + P <= lb) {
+                strip_group<R, U, P>(j, S, s_inc, win, wmask, B, tthr, s_best, one);
                 j += U;
             } else if (!ALIGNED && j >= I0 && j + U - 1 <= I1) {
-                strip_group_percol<R, U>(j, lb, S, s_inc, win, wmask, B, tthr, s_best, one);
+                strip_group_percol<R, U, P>(j, lb, S, s_inc, win, wmask, B, tthr, s_best, one);
                 j += U;
             } else {
-                strip_column<R>(j, lb, S, s_inc, win, wmask, B, lo0, w2, tthr, s_best, one);
+                strip_column<R, P>(j, lb, S, s_inc, win, wmask, B, lo0, w2, tthr, s_best, one);
                 j += 1;
             }
         }
@@ -1119,7 +1128,9 @@ static int32_t pow2_at_least(int64_t x) {
 
 // Tunables (set by ck_sw_set_config, chosen by the autotuner).
 static int32_t g_rows_per_strip = 0;  // 0: by band width (8 up to w = 64, else 16)
-static int32_t g_variant = 1;
+// -1 (default): by strip height -- groups of 4 columns at 8 rows (3), of 2
+// above (1); 0..3 as set (see StripVariant)
+static int32_t g_variant = -1;
 // resident CTAs of 256 threads per SM for strips of up to 16 rows: 2 (at most
 // 128 registers a thread) or 1 (up to 255); 0 = 2.  Taller strips always run 1.
 static int32_t g_ctas_per_sm = 0;
@@ -1168,8 +1179,8 @@ int32_t sw_wave(int32_t key) {
 }
 
 int32_t sw_set_variant(int32_t v) {
-    if (v < 0 || v > 3) {
-        set_error(CK_ERR_UNSUPPORTED, "strip kernel variant must be 0..3");
+    if (v < -1 || v > 3) {
+        set_error(CK_ERR_UNSUPPORTED, "strip kernel variant must be -1 (by strip height) or 0..3");
         return CK_ERR_UNSUPPORTED;
     }
     g_variant = v;
@@ -1241,7 +1252,7 @@ static int32_t launch_strips_m(const SwIn &in, const SwOut &out, const uint32_t 
                                const int32_t *counters, const int32_t *inc, int32_t wmax,
                                int32_t *ticket, int32_t *fallback, int32_t *fb_count,
                                int32_t *err, cudaStream_t st, SwCounters *ctr) {
-    switch (g_variant) {
+    switch (g_variant >= 0 ? g_variant : (R <= 8 ? 3 : 1)) {
         case 0: return launch_strips<R, 0, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
         case 2: return launch_strips<R, 2, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
         case 3: return launch_strips<R, 3, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);

@@ -11,8 +11,9 @@ GB300 counterparts of "bin edges, band tiling and CTA shape":
 * band tiling -- rows a lane keeps in registers per strip (8, 16, 24, 32;
   the library's default 0 picks 8 for half-widths up to 64, else 16);
 * strip variant -- interior columns in groups of 2 or 4 (one first-maximum
-  vote per group), aligned with base-pointer addressing or not, i.e. the
-  shape of a lane's inner loop;
+  vote per group), aligned with base-pointer addressing and a 4-column
+  prefetch or not, i.e. the shape of a lane's inner loop (the library's
+  default -1 takes groups of 4 at 8 rows per strip, else 2);
 * CTA shape -- resident 256-thread CTAs per SM for strips of up to 16 rows
   (2 at <= 128 registers a thread, or 1 with up to 255; taller strips run 1),
   which sets the warps per SM and the lanes' scratch windows in flight.
@@ -46,7 +47,7 @@ KEYS = {
     "wave_adaptive": _lib.CFG_WAVE_ADAPTIVE,
 }
 
-DEFAULT = {"rows_per_strip": 0, "strip_variant": 1, "ctas_per_sm": 0, "wave_min_rows": 512,
+DEFAULT = {"rows_per_strip": 0, "strip_variant": -1, "ctas_per_sm": 0, "wave_min_rows": 512,
            "wave_all_below": 40960, "wave_adaptive": 1}
 
 # bin-edge candidates: (wave_min_rows, wave_adaptive); 1 << 30 = never by length

@@ -175,9 +175,11 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *                          is <= 64, else 16
  *   CK_CFG_STRIP_VARIANT   0..3: bit 1 runs interior columns in groups of
  *                          four (else two), with one first-maximum vote per
- *                          group; bit 0 aligns the groups and addresses each
- *                          group's window slots and residues from two base
- *                          pointers (else each column its own)
+ *                          group; bit 0 aligns the groups, addresses each
+ *                          group's window slots and residues from one base
+ *                          pointer per run and prefetches four columns ahead
+ *                          (else each column its own addresses, two ahead);
+ *                          -1 (default): 3 for strips of 8 rows, else 1
  *   CK_CFG_WAVE_ALL_BELOW  calls with at most this many pairs to align (the
  *                          count is taken on the device, after empty and
  *                          skipped pairs) run every pair one warp per pair

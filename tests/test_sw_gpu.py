@@ -344,6 +344,27 @@ def test_autotuner_settings_agree(ck):
         tune.apply(keep)
 
 
+def test_autotuner_never_returns_a_slower_setting(ck):
+    """On a fixed input the tuner either keeps the default or returns a setting
+    that its own alternating re-time found at least 2 % faster; an independent
+    re-time (medians of 5 calls, alternating, three rounds) then finds the
+    returned setting no slower than the default, within 5 % for timing noise."""
+    from clustkit_gb300 import tune
+    s = synth.generate_families(200, 10, median=0, lo=30, hi=4000, seed=9, length_dist="pareto")
+    pairs = synth.mixed_pairs(s, 200_000, seed=4, min_ratio=0.5)
+    keep = tune.current()
+    try:
+        res = tune.autotune(pairs, s.flat, s.offsets, s.lengths, 32, use_cache=False, apply_best=False)
+        if res.config != tune.DEFAULT:
+            assert res.confirm["kept"] == "candidate"
+            assert res.confirm["candidate_ms"] <= 0.98 * res.confirm["default_ms"]
+        call = tune._DeviceCall(pairs, s.flat, s.offsets, s.lengths, 32)
+        again = tune.confirm(call, res.config, tune.DEFAULT)
+        assert again["candidate_ms"] <= 1.05 * again["default_ms"], (res.config, res.confirm, again)
+    finally:
+        tune.apply(keep)
+
+
 @pytest.mark.parametrize("bw", [238, 100, 20])
 def test_streamed_wave_many_small_pairs(ck, bw):
     """Thousands of short and mixed pairs through the streamed warp-per-pair
