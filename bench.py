@@ -495,7 +495,8 @@ def run_ours(args, world, rank, local):
     p_int32 = rates["viaddmax_s32"]
     # cell arithmetic alone, in the exact int32 form and two int16x2 forms
     cell_forms = {}
-    for form, name in ((0, "int32_exact_key"), (1, "int16x2_score_only"), (2, "int16x2_match_select")):
+    for form, name in ((0, "int32_exact_key"), (1, "int16x2_score_only"), (2, "int16x2_match_select"),
+                       (3, "int32_exact_key_skewed_halves")):
         _lib.check(lib.ck_probe_cell_rate(form, peak.ctypes.data))
         cell_forms[name] = float(peak[0]) / 1e9
     kernel_s = float(np.mean(kt)) / 1e3 if kt and min(kt) > 0 else t_batched / args.steps

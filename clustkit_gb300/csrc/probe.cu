@@ -51,14 +51,18 @@ __global__ void __launch_bounds__(1024) probe_kernel(int32_t iters, int32_t seed
 //      update is one DPX op: 5 DPX + 1 PRMT + 2 LDS per cell pair;
 //   2  int16x2 with the match count carried in a second int16x2 register:
 //      each max picks its winner's count through a compare mask and a
-//      select, as exact tracking at two pairs per lane would need.
+//      select, as exact tracking at two pairs per lane would need;
+//   3  form 0 with the strip's lower 8 rows one column behind the upper 8:
+//      the lower half's top row takes the upper half's bottom row as it stood
+//      a column earlier, so a column holds two independent 8-row chains.
 // Each reports DP cells per second (forms 1 and 2: two cells per lane op).
 // Every table index is (arow + bcol) >> 2 with arow <= 31 * 128 and bcol <=
 // 31 * 4, so below 1024, and t ^ 16 stays below 1024 too.
 template <int FORM>
 __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_t seed, int32_t *sink) {
     __shared__ int32_t tab[32 * 32];
-    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) tab[t] = ((t * 7 + seed) % 23 - 11) << (FORM == 0 ? 16 : 0);
+    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x)
+        tab[t] = ((t * 7 + seed) % 23 - 11) << ((FORM == 0 || FORM == 3) ? 16 : 0);
     __syncthreads();
     constexpr int R = 16;
     const int lane = threadIdx.x & 31;
@@ -67,12 +71,13 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         hc[r] = 0;
-        fT[r] = FORM == 0 ? -(16 << 16) : (int32_t)0x80408040u;
+        fT[r] = (FORM == 0 || FORM == 3) ? -(16 << 16) : (int32_t)0x80408040u;
         mh[r] = 0;
         mf[r] = 0;
         arow[r] = (uint32_t)(((r * 5 + seed + threadIdx.x) & 31) * 32 * 4);
     }
-    int32_t hd0 = 0, e_in = FORM == 0 ? -(16 << 16) : (int32_t)0x80408040u, acc = 0;
+    int32_t hd0 = 0, e_in = (FORM == 0 || FORM == 3) ? -(16 << 16) : (int32_t)0x80408040u, acc = 0;
+    int32_t h_mid = 0, e_mid = -(16 << 16), h_mid_prev = 0;  // form 3: the upper half's bottom row, delayed
     for (int32_t j = 0; j < cols; ++j) {
         const uint32_t bcol = (uint32_t)(((j * 13 + lane) & 31) * 4);
         const uint32_t offj = (uint32_t)(((j - 10) & 0xffff) * 0x10001u);
@@ -81,8 +86,19 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
         hd0 = hu;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
+            if (FORM == 3 && r == R / 2) {
+                // lower half one column behind: its top row reads the upper half's
+                // bottom row as it stood after the previous column, not this one
+                const int32_t h_now = hu, e_now = eu;
+                hu = h_mid;
+                eu = e_mid;
+                hdiag = h_mid_prev;
+                h_mid_prev = h_mid;
+                h_mid = h_now;
+                e_mid = e_now;
+            }
             const uint32_t t = (arow[r] + bcol) >> 2;
-            if (FORM == 0) {
+            if (FORM == 0 || FORM == 3) {
                 const int32_t inc = tab[t];
                 const int32_t diagc = __viaddmax_s32(hdiag, inc, 3 << 14);
                 const int32_t eR = __viaddmax_s32(hu, (-11 << 16) + (1 << 14), eu + (-1 << 16));
@@ -139,7 +155,7 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
 using namespace ck;
 
 extern "C" int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s) {
-    if (!out_cells_per_s || form < 0 || form > 2) {
+    if (!out_cells_per_s || form < 0 || form > 3) {
         set_error(CK_ERR_INVALID_ARGUMENT, "cell probe: bad argument");
         return CK_ERR_INVALID_ARGUMENT;
     }
@@ -157,7 +173,8 @@ extern "C" int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s) {
         switch (form) {
             case 0: cell_probe_kernel<0><<<blocks, threads>>>(cols, rep + 3, sink); break;
             case 1: cell_probe_kernel<1><<<blocks, threads>>>(cols, rep + 3, sink); break;
-            default: cell_probe_kernel<2><<<blocks, threads>>>(cols, rep + 3, sink); break;
+            case 2: cell_probe_kernel<2><<<blocks, threads>>>(cols, rep + 3, sink); break;
+            default: cell_probe_kernel<3><<<blocks, threads>>>(cols, rep + 3, sink); break;
         }
         CK_CUDA(cudaGetLastError());
         CK_CUDA(cudaEventRecord(e1, 0));
@@ -168,7 +185,7 @@ extern "C" int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const double cells = (double)blocks * threads * cols * 16.0 * (form == 0 ? 1.0 : 2.0);
+    const double cells = (double)blocks * threads * cols * 16.0 * ((form == 0 || form == 3) ? 1.0 : 2.0);
     *out_cells_per_s = cells / (best_ms * 1e-3);
     return CK_OK;
 }

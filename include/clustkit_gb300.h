@@ -473,8 +473,9 @@ int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s);
  * uses; 1 = int16x2 score only (two pairs a lane; no match count, so not
  * usable for clustkit's identity); 2 = int16x2 with match counts carried in
  * a second int16x2 register and picked by compare masks (what exact tracking
- * at two pairs a lane costs).  A measurement of the cell arithmetic, no
- * counterpart in clustkit. */
+ * at two pairs a lane costs); 3 = form 0 with the strip's lower half one
+ * column behind its upper half (two independent row chains a column).  A
+ * measurement of the cell arithmetic, no counterpart in clustkit. */
 int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s);
 
 #ifdef __cplusplus
