@@ -32,7 +32,11 @@
 //     H    = max(diag, E, F)                 (__vimax3_s32)
 // and H's priority/tie bits are cleared before it feeds other cells.
 // The first row-major cell holding the best score is tracked per row (strict
-// '>' along the row) and the rows are merged in row order after each strip.
+// '>' along the row) and the rows are merged in row order after each strip;
+// a warp vote once per group of interior columns decides whether any lane's
+// cells reached its threshold, so most columns never touch the trackers.
+// Rows of a pair's last strip below its last row read a pad code (their
+// diagonal always loses to zero), so every strip runs the same column code.
 // Scores use the key's top 16 bits; a pair whose best score comes within 24
 // of 32767 is re-run on the plain kernel, so no overflow reaches the output.
 #include <cub/device/device_radix_sort.cuh>
@@ -258,12 +262,12 @@ struct StripRegs {
     uint32_t cq[4];    // residue offsets of the same columns' b
 };
 
-// Structural variants of the strip kernel (picked by the autotuner), all
-// prefetching the window entry and residue two columns ahead: bit 1 runs
-// interior columns in groups of 4 instead of 2 (one first-max vote per
-// group); bit 0 starts the groups at columns aligned to their size and
-// addresses a group's window slots and residues from two base pointers,
-// instead of computing each column's addresses on its own.
+// Structural variants of the strip kernel (picked by the autotuner): bit 1
+// runs interior columns in groups of 4 instead of 2 (one first-max vote per
+// group); bit 0 starts the groups at columns aligned to their size,
+// addresses each run of a group's window slots from one base pointer and
+// prefetches window entries and residues four columns ahead, instead of
+// computing each column's addresses on its own and prefetching two ahead.
 template <int V> struct StripVariant {
     static constexpr int UNROLL = (V & 2) ? 4 : 2;
     static constexpr bool ALIGNED = (V & 1) != 0;
