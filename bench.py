@@ -375,6 +375,8 @@ def run_ours(args, world, rank, local):
         _lib.set_config(_lib.CFG_STRIP_VARIANT, args.variant)
     if args.ctas:
         _lib.set_config(_lib.CFG_CTAS_PER_SM, args.ctas)
+    if args.strip_key:
+        _lib.set_config(_lib.CFG_STRIP_KEY, args.strip_key)
     s, pairs, n_cand = build_workload(use_gpu=True, quick=args.quick)
     pairs = shard(pairs, world, rank)
     M = len(pairs)
@@ -432,6 +434,18 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     lib.ck_sw_profile(0)
     res_b = {k: v.cpu().numpy() for k, v in out.items()}
+    # the same step with the other key form of the strip kernel (compact key for
+    # pairs of <= 2047 rows, or the wide key for every pair): speed and results
+    key_now = _lib.get_config(_lib.CFG_STRIP_KEY)
+    _lib.set_config(_lib.CFG_STRIP_KEY, 1 - key_now)
+    t_other, _ = timed(ENGINE_BATCHED, 3, 1)
+    other_same = all(np.array_equal(res_b[k], v.cpu().numpy()) for k, v in out.items())
+    _lib.set_config(_lib.CFG_STRIP_KEY, key_now)
+    gc_this = cells / (t_batched / args.steps) / 1e9
+    gc_other = cells / (t_other / 3) / 1e9
+    key_forms = {"compact_gcups": round(gc_other if key_now else gc_this, 1),
+                 "wide_gcups": round(gc_this if key_now else gc_other, 1),
+                 "results_identical": bool(other_same), "in_use": "wide" if key_now else "compact"}
     sweep = {}
     if args.sweep:
         keys = (_lib.CFG_ROWS_PER_STRIP, _lib.CFG_STRIP_VARIANT, _lib.CFG_CTAS_PER_SM)
@@ -496,7 +510,7 @@ def run_ours(args, world, rank, local):
     # cell arithmetic alone, in the exact int32 form and two int16x2 forms
     cell_forms = {}
     for form, name in ((0, "int32_exact_key"), (1, "int16x2_score_only"), (2, "int16x2_match_select"),
-                       (3, "int32_exact_key_skewed_halves")):
+                       (3, "int32_exact_key_skewed_halves"), (4, "int32_compact_key_ext_counter")):
         _lib.check(lib.ck_probe_cell_rate(form, peak.ctypes.data))
         cell_forms[name] = float(peak[0]) / 1e9
     kernel_s = float(np.mean(kt)) / 1e3 if kt and min(kt) > 0 else t_batched / args.steps
@@ -551,6 +565,7 @@ def run_ours(args, world, rank, local):
         "reference_cupy_path": gpu_ref,
         "rows_per_strip": _lib.get_config(_lib.CFG_ROWS_PER_STRIP),
         "strip_variant": _lib.get_config(_lib.CFG_STRIP_VARIANT),
+        "strip_key_forms": key_forms,
         "sweep_gcups": sweep or None,
         "clocks": clk,
         "gpu_launches": int(launches),
@@ -1121,6 +1136,8 @@ def main():
                     help="search leg: only full batches per mode (a warm-up and a few), for profiler launch lists")
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24/32); 0 = library default")
     ap.add_argument("--ctas", type=int, default=0, help="strip kernel CTAs per SM (1/2); 0 = library default")
+    ap.add_argument("--strip-key", type=int, default=0, choices=[0, 1],
+                    help="1: the strip kernel's wide key for every pair (default 0: compact where rows fit)")
     ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default (by strip height)")
     ap.add_argument("--sweep", action="store_true", help="also time every rows-per-strip x variant setting")
     ap.add_argument("--search", choices=["auto", "on", "off", "only"], default="auto",

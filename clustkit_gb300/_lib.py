@@ -32,6 +32,7 @@ CFG_WAVE_ADAPTIVE = 4
 CFG_WAVE_STREAM = 5
 CFG_WAVE_ROWS = 6
 CFG_CTAS_PER_SM = 8
+CFG_STRIP_KEY = 9
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32

@@ -166,6 +166,8 @@ int32_t sw_set_rows_per_strip(int32_t r);
 int32_t sw_rows_per_strip();
 int32_t sw_set_ctas_per_sm(int32_t v);
 int32_t sw_ctas_per_sm();
+int32_t sw_set_wide_key(int32_t v);
+int32_t sw_wide_key();
 int32_t sw_set_variant(int32_t v);
 int32_t sw_variant();
 int32_t sw_set_wave(int32_t key, int32_t v);  // key 0: min rows, 1: all-pairs batch limit, 2: adaptive, 3: stream, 4: streamed strip rows

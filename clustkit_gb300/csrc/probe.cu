@@ -54,7 +54,11 @@ __global__ void __launch_bounds__(1024) probe_kernel(int32_t iters, int32_t seed
 //      select, as exact tracking at two pairs per lane would need;
 //   3  form 0 with the strip's lower 8 rows one column behind the upper 8:
 //      the lower half's top row takes the upper half's bottom row as it stood
-//      a column earlier, so a column holds two independent 8-row chains.
+//      a column earlier, so a column holds two independent 8-row chains;
+//   4  a compact key: 11-bit match count and a 3-bit extension counter (each
+//      gap extension adds 1, so it wins ties against an opening) in place of
+//      the tie bit, cleared every 4 rows (E) and every 2 columns (F) instead
+//      of a tie bit set after every max.
 // Each reports DP cells per second (forms 1 and 2: two cells per lane op).
 // Every table index is (arow + bcol) >> 2 with arow <= 31 * 128 and bcol <=
 // 31 * 4, so below 1024, and t ^ 16 stays below 1024 too.
@@ -62,7 +66,7 @@ template <int FORM>
 __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_t seed, int32_t *sink) {
     __shared__ int32_t tab[32 * 32];
     for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x)
-        tab[t] = ((t * 7 + seed) % 23 - 11) << ((FORM == 0 || FORM == 3) ? 16 : 0);
+        tab[t] = ((t * 7 + seed) % 23 - 11) << ((FORM == 0 || FORM >= 3) ? 16 : 0);
     __syncthreads();
     constexpr int R = 16;
     const int lane = threadIdx.x & 31;
@@ -71,12 +75,12 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         hc[r] = 0;
-        fT[r] = (FORM == 0 || FORM == 3) ? -(16 << 16) : (int32_t)0x80408040u;
+        fT[r] = (FORM == 0 || FORM >= 3) ? -(16 << 16) : (int32_t)0x80408040u;
         mh[r] = 0;
         mf[r] = 0;
         arow[r] = (uint32_t)(((r * 5 + seed + threadIdx.x) & 31) * 32 * 4);
     }
-    int32_t hd0 = 0, e_in = (FORM == 0 || FORM == 3) ? -(16 << 16) : (int32_t)0x80408040u, acc = 0;
+    int32_t hd0 = 0, e_in = (FORM == 0 || FORM >= 3) ? -(16 << 16) : (int32_t)0x80408040u, acc = 0;
     int32_t h_mid = 0, e_mid = -(16 << 16), h_mid_prev = 0;  // form 3: the upper half's bottom row, delayed
     for (int32_t j = 0; j < cols; ++j) {
         const uint32_t bcol = (uint32_t)(((j * 13 + lane) & 31) * 4);
@@ -98,7 +102,22 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
                 e_mid = e_now;
             }
             const uint32_t t = (arow[r] + bcol) >> 2;
-            if (FORM == 0 || FORM == 3) {
+            if (FORM == 4) {
+                // compact key: 11-bit match count, a 3-bit extension counter in
+                // bits 11..13 instead of a tie bit; E's counter cleared every 4
+                // rows, F's every 2 columns, H cleaned as before
+                constexpr int32_t CM = 7 << 11;
+                const int32_t inc = tab[t];
+                const int32_t diagc = __viaddmax_s32(hdiag, inc, 3 << 14);
+                const int32_t eR = __viaddmax_s32(hu, (-11 << 16) + (1 << 14), eu + (-1 << 16) + (1 << 11));
+                const int32_t fTn = __viaddmax_s32(fT[r], (-1 << 16) + (1 << 11), hc[r] + (-11 << 16));
+                const int32_t hn = __vimax3_s32(diagc, eR, fTn) & ~(CM | (3 << 14));
+                hdiag = hc[r];
+                hc[r] = hn;
+                fT[r] = fTn;
+                hu = hn;
+                eu = (r & 3) == 3 ? (eR & ~CM) : eR;
+            } else if (FORM == 0 || FORM == 3) {
                 const int32_t inc = tab[t];
                 const int32_t diagc = __viaddmax_s32(hdiag, inc, 3 << 14);
                 const int32_t eR = __viaddmax_s32(hu, (-11 << 16) + (1 << 14), eu + (-1 << 16));
@@ -146,6 +165,10 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
         }
         e_in = eu;
         acc ^= hu ^ mu;
+        if (FORM == 4 && (j & 1)) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) fT[r] &= ~(7 << 11);
+        }
     }
     if (acc == 0x7fffabcd) sink[0] = acc;  // keeps the chains live
 }
@@ -155,7 +178,7 @@ __global__ void __launch_bounds__(256, 2) cell_probe_kernel(int32_t cols, int32_
 using namespace ck;
 
 extern "C" int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s) {
-    if (!out_cells_per_s || form < 0 || form > 3) {
+    if (!out_cells_per_s || form < 0 || form > 4) {
         set_error(CK_ERR_INVALID_ARGUMENT, "cell probe: bad argument");
         return CK_ERR_INVALID_ARGUMENT;
     }
@@ -174,7 +197,8 @@ extern "C" int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s) {
             case 0: cell_probe_kernel<0><<<blocks, threads>>>(cols, rep + 3, sink); break;
             case 1: cell_probe_kernel<1><<<blocks, threads>>>(cols, rep + 3, sink); break;
             case 2: cell_probe_kernel<2><<<blocks, threads>>>(cols, rep + 3, sink); break;
-            default: cell_probe_kernel<3><<<blocks, threads>>>(cols, rep + 3, sink); break;
+            case 3: cell_probe_kernel<3><<<blocks, threads>>>(cols, rep + 3, sink); break;
+            default: cell_probe_kernel<4><<<blocks, threads>>>(cols, rep + 3, sink); break;
         }
         CK_CUDA(cudaGetLastError());
         CK_CUDA(cudaEventRecord(e1, 0));
@@ -185,7 +209,7 @@ extern "C" int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const double cells = (double)blocks * threads * cols * 16.0 * ((form == 0 || form == 3) ? 1.0 : 2.0);
+    const double cells = (double)blocks * threads * cols * 16.0 * ((form == 1 || form == 2) ? 2.0 : 1.0);
     *out_cells_per_s = cells / (best_ms * 1e-3);
     return CK_OK;
 }

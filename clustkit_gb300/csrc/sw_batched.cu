@@ -63,6 +63,35 @@ constexpr int32_t SCORE_LIMIT = 32767 - 24;
 constexpr int32_t MATCH_MASK = (1 << 13) - 1;
 }  // namespace key
 
+// The two key forms of the strip kernel.  Wide (above): 13 bits of match
+// count, and a tie bit set on every stored E and F so that a gap extension
+// beats a gap opening of the same score.  Compact, for pairs of at most 2047
+// rows: 11 bits of match count and, in bits 11..13, a counter that every gap
+// extension increments.  An opening starts from a clean H (counter 0) and an
+// extension from E or F plus one (counter >= 1), so extension still wins
+// every tie.  E's counter is cleared every 4 rows and F's after every group
+// of at most 4 columns, before it could carry into the priority bits: a few
+// logic ops per group instead of two per cell.
+struct KeyWide {
+    static constexpr bool COMPACT = false;
+    static constexpr int32_t CTR = 0;
+    static constexpr int32_t CLEAN = key::CLEAN;
+    static constexpr int32_t EXT = key::EXT;
+    static constexpr int32_t NEG_E = key::NEG_E;
+    static constexpr int32_t NEG_F = key::NEG_F;
+    static constexpr int32_t MATCH_MASK = key::MATCH_MASK;
+};
+struct KeyCompact {
+    static constexpr bool COMPACT = true;
+    static constexpr int32_t CTR = 7 << 11;
+    static constexpr int32_t CLEAN = ~(CTR | 3 * key::PU);
+    static constexpr int32_t EXT = key::EXT + (1 << 11);
+    static constexpr int32_t NEG_E = -16 * key::KU + 1 * key::PU;
+    static constexpr int32_t NEG_F = -16 * key::KU;
+    static constexpr int32_t MATCH_MASK = (1 << 11) - 1;
+    static constexpr int32_t ROWS_MAX = (1 << 11) - 1;
+};
+
 constexpr int STRIP_THREADS = 256;
 // per warp, the streamed warp-per-pair phase's pair slots in shared memory
 constexpr size_t WAVE_SLOT_BYTES = 72;  // sizeof(WaveSlot), checked where it is defined
@@ -332,7 +361,7 @@ __device__ __forceinline__ void strip_cells(uint32_t bcol, int32_t &hu, int32_t 
 // H and E of the row above at this column and leave as this row's; hdiag
 // enters as H of the row above at the previous column and leaves as this
 // row's H at the previous column (the next row's diagonal input).
-template <int R, int r>
+template <int R, int r, class K>
 __device__ __forceinline__ void strip_cell(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
                                            StripRegs<R> &S, const char *s_inc, int32_t one) {
     using namespace key;
@@ -340,25 +369,37 @@ __device__ __forceinline__ void strip_cell(uint32_t bcol, int32_t &hu, int32_t &
     const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
     // E's extension term comes from E of the row above, known before that
     // row's H: only H_up + OPEN_E and the max-of-three sit on the row-to-row
-    // dependency chain.  E's tie bit plays no part in H (E, F, diag and zero
+    // dependency chain.  E's tie mark plays no part in H (E, F, diag and zero
     // differ in priority), so it is set off the chain.
-    const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, EXT, one));
-    const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
-    const int32_t hn = __vimax3_s32(diagc, eR, fTn) & CLEAN;
+    const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, K::EXT, one));
+    int32_t fTn = __viaddmax_s32(S.fT[r], K::EXT, fadd(S.hc[r], OPEN_F, one));
+    if constexpr (!K::COMPACT) fTn |= TBIT;
+    const int32_t hn = __vimax3_s32(diagc, eR, fTn) & K::CLEAN;
     hdiag = S.hc[r];
     S.hc[r] = hn;
     S.fT[r] = fTn;
     hu = hn;
-    eu = eR | TBIT;
+    if constexpr (K::COMPACT) eu = (r & 3) == 3 ? (eR & ~K::CTR) : eR;
+    else eu = eR | TBIT;
 }
 
 // Rows r .. R-1 of a column, all inside their band.
-template <int R, int r = 0>
+template <int R, class K, int r = 0>
 __device__ __forceinline__ void strip_cells_from(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
                                                  StripRegs<R> &S, const char *s_inc, int32_t one) {
     if constexpr (r < R) {
-        strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
-        strip_cells_from<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_cell<R, r, K>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_cells_from<R, K, r + 1>(bcol, hu, eu, hdiag, S, s_inc, one);
+    }
+}
+
+// Compact key: clear the F counters of the strip's rows after a group of
+// columns (at most 4 extensions since the last clear).
+template <int R, class K>
+__device__ __forceinline__ void strip_clear_f(StripRegs<R> &S) {
+    if constexpr (K::COMPACT) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) S.fT[r] &= ~K::CTR;
     }
 }
 
@@ -370,49 +411,49 @@ __device__ __forceinline__ void strip_cells_from(uint32_t bcol, int32_t &hu, int
 // (khi = R - 1) a suffix, so each needs one compare a row; a column that is
 // both (a band narrower than the strip) takes the two-sided test.  Every
 // row's cell appears once in the code.
-template <int R, int r = 0>
+template <int R, class K, int r = 0>
 __device__ __forceinline__ void strip_rows_prefix(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
                                                   StripRegs<R> &S, const char *s_inc, int32_t khi, int32_t one) {
     if constexpr (r < R) {
-        if (r <= khi) strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
-        strip_rows_prefix<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, khi, one);
+        if (r <= khi) strip_cell<R, r, K>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_rows_prefix<R, K, r + 1>(bcol, hu, eu, hdiag, S, s_inc, khi, one);
     }
 }
 
-template <int R, int r = 0>
+template <int R, class K, int r = 0>
 __device__ __forceinline__ void strip_rows_suffix(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
                                                   StripRegs<R> &S, const char *s_inc, int32_t klo, int32_t one) {
     if constexpr (r < R) {
-        if (r >= klo) strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
+        if (r >= klo) strip_cell<R, r, K>(bcol, hu, eu, hdiag, S, s_inc, one);
         else hdiag = S.hc[r];
-        strip_rows_suffix<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, klo, one);
+        strip_rows_suffix<R, K, r + 1>(bcol, hu, eu, hdiag, S, s_inc, klo, one);
     }
 }
 
-template <int R, int r = 0>
+template <int R, class K, int r = 0>
 __device__ __forceinline__ void strip_rows_between(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
                                                    StripRegs<R> &S, const char *s_inc, int32_t klo, int32_t khi,
                                                    int32_t one) {
     if constexpr (r < R) {
         if (r < klo) hdiag = S.hc[r];
-        else if (r <= khi) strip_cell<R, r>(bcol, hu, eu, hdiag, S, s_inc, one);
-        strip_rows_between<R, r + 1>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
+        else if (r <= khi) strip_cell<R, r, K>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_rows_between<R, K, r + 1>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
     }
 }
 
-template <int R>
+template <int R, class K>
 __device__ __forceinline__ void strip_rows_masked(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t &hdiag,
                                                   StripRegs<R> &S, const char *s_inc, int32_t klo, int32_t khi,
                                                   int32_t one) {
     if (klo == 0) {
-        strip_rows_prefix<R>(bcol, hu, eu, hdiag, S, s_inc, khi, one);
+        strip_rows_prefix<R, K>(bcol, hu, eu, hdiag, S, s_inc, khi, one);
     } else {
         hu = 0;  // the first row inside the band has the boundary above it
-        eu = key::NEG_E;
-        if (khi == R - 1) strip_rows_suffix<R>(bcol, hu, eu, hdiag, S, s_inc, klo, one);
-        else strip_rows_between<R>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
+        eu = K::NEG_E;
+        if (khi == R - 1) strip_rows_suffix<R, K>(bcol, hu, eu, hdiag, S, s_inc, klo, one);
+        else strip_rows_between<R, K>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
     }
-    if (khi < R - 1) { hu = 0; eu = key::NEG_E; }  // the bottom row has not started
+    if (khi < R - 1) { hu = 0; eu = K::NEG_E; }  // the bottom row has not started
 }
 
 // First-max trackers (one per row, in shared memory) are touched only when
@@ -468,7 +509,7 @@ __device__ __forceinline__ void column_inputs(int32_t j, int32_t lb, StripRegs<R
 // U interior columns j .. j + U - 1 (every row inside its band), each
 // addressing its own window slots and residues, then one first-max check
 // over all of them.
-template <int R, int U, int P>
+template <int R, int U, int P, class K>
 __device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripRegs<R> &S, const char *s_inc,
                                                    int2 *win, int32_t wmask, const uint8_t *B, int32_t &tthr,
                                                    int32_t *s_best, int32_t one) {
@@ -480,11 +521,12 @@ __device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripR
         column_inputs<R, P>(j + u, lb, S, win, wmask, B, bnd, bcol);
         int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
         S.hd0 = hu;
-        strip_cells_from<R>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_cells_from<R, K>(bcol, hu, eu, hdiag, S, s_inc, one);
         win[(size_t)((j + u) & wmask) * 32] = make_int2(hu, eu);
 #pragma unroll
         for (int r = 0; r < R; ++r) hs[u][r] = S.hc[r];
     }
+    strip_clear_f<R, K>(S);
     strip_track<R, U>(hs, tthr, s_best);
 }
 
@@ -494,7 +536,7 @@ __device__ __forceinline__ void strip_group_percol(int32_t j, int32_t lb, StripR
 // address per run, immediate offsets after it.  The caller runs a group only
 // where j + U - 1 + P <= lb, so the prefetched residues lie inside the
 // sequence.
-template <int R, int U, int P>
+template <int R, int U, int P, class K>
 __device__ __forceinline__ void strip_group(int32_t j, StripRegs<R> &S, const char *s_inc, int2 *win,
                                             int32_t wmask, const uint8_t *B, int32_t &tthr, int32_t *s_best,
                                             int32_t one) {
@@ -516,17 +558,18 @@ __device__ __forceinline__ void strip_group(int32_t j, StripRegs<R> &S, const ch
         S.cq[P - 1] = (uint32_t)__ldg(pb + u) * 128u;
         int32_t hu = bnd.x, eu = bnd.y, hdiag = S.hd0;
         S.hd0 = hu;
-        strip_cells_from<R>(bcol, hu, eu, hdiag, S, s_inc, one);
+        strip_cells_from<R, K>(bcol, hu, eu, hdiag, S, s_inc, one);
         cur[u * 32] = make_int2(hu, eu);
 #pragma unroll
         for (int r = 0; r < R; ++r) hs[u][r] = S.hc[r];
     }
+    strip_clear_f<R, K>(S);
     strip_track<R, U>(hs, tthr, s_best);
 }
 
 // One column outside the aligned interior groups: a ramp or clipped column
 // (rows klo..khi inside their band) or an interior column at a group's edge.
-template <int R, int P>
+template <int R, int P, class K>
 __device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R> &S, const char *s_inc,
                                              int2 *win, int32_t wmask, const uint8_t *B, int32_t lo0,
                                              int32_t w2, int32_t &tthr, int32_t *s_best, int32_t one) {
@@ -539,28 +582,28 @@ __device__ __forceinline__ void strip_column(int32_t j, int32_t lb, StripRegs<R>
     const int32_t d = j - lo0;
     const int32_t klo = d - w2 > 0 ? d - w2 : 0;
     const int32_t khi = d < R - 1 ? d : R - 1;
-    strip_rows_masked<R>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
+    strip_rows_masked<R, K>(bcol, hu, eu, hdiag, S, s_inc, klo, khi, one);
     win[(size_t)(j & wmask) * 32] = make_int2(hu, eu);
+    strip_clear_f<R, K>(S);
     int32_t hs[1][R];
 #pragma unroll
     for (int r = 0; r < R; ++r) hs[0][r] = S.hc[r];
     strip_track<R, 1>(hs, tthr, s_best);
 }
 
-template <int R, int V>
-__device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
-                                  int32_t *s_best, int2 *win, int32_t W, int32_t lane,
-                                  int32_t *fallback, int32_t *fallback_count, int32_t *err,
-                                  int32_t one) {
+template <int R, int V, class K>
+__device__ __forceinline__ void align_pair_strips_k(const SwIn &in, const SwOut &out, int64_t p,
+                                                    const PairGeom &g, const char *s_inc, int32_t *s_best,
+                                                    int2 *win, int32_t W, int32_t lane, int32_t *fallback,
+                                                    int32_t *fallback_count, int32_t one) {
     using namespace key;
-    PairGeom g = pair_geometry(in, p, err);
     const int32_t la = g.la, lb = g.lb, w = g.w, h = g.h;
     const uint8_t *A = in.flat + in.offsets[g.a_idx];
     const uint8_t *B = in.flat + in.offsets[g.b_idx];
     const int32_t wmask = W - 1;
     const int32_t w2 = 2 * w;
 
-    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, NEG_E);
+    for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, K::NEG_E);
 
     int32_t gbest = 0;
     StripRegs<R> S;
@@ -577,7 +620,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             S.hc[r] = 0;
-            S.fT[r] = NEG_F;
+            S.fT[r] = K::NEG_F;
             s_best[r * STRIP_THREADS] = gbest;
             // rows below the pair's last row (last strip only) read the pad code
             const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : PAD_CODE;
@@ -603,13 +646,13 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         constexpr bool ALIGNED = StripVariant<V>::ALIGNED;
         for (int32_t j = J0; j <= J1;) {
             if (ALIGNED && j >= I0 && (j & (U - 1)) == 0 && j + U - 1 <= I1 && j + U - 1 + P <= lb) {
-                strip_group<R, U, P>(j, S, s_inc, win, wmask, B, tthr, s_best, one);
+                strip_group<R, U, P, K>(j, S, s_inc, win, wmask, B, tthr, s_best, one);
                 j += U;
             } else if (!ALIGNED && j >= I0 && j + U - 1 <= I1) {
-                strip_group_percol<R, U, P>(j, lb, S, s_inc, win, wmask, B, tthr, s_best, one);
+                strip_group_percol<R, U, P, K>(j, lb, S, s_inc, win, wmask, B, tthr, s_best, one);
                 j += U;
             } else {
-                strip_column<R, P>(j, lb, S, s_inc, win, wmask, B, lo0, w2, tthr, s_best, one);
+                strip_column<R, P, K>(j, lb, S, s_inc, win, wmask, B, lo0, w2, tthr, s_best, one);
                 j += 1;
             }
         }
@@ -623,7 +666,7 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         // the columns right of this strip's band read as out-of-band for the next strip
         const int32_t fill_end = J1 + R < lb ? J1 + R : lb;
         for (int32_t j = J1 + 1; j <= fill_end; ++j)
-            win[(size_t)(j & wmask) * 32] = make_int2(0, NEG_E);
+            win[(size_t)(j & wmask) * 32] = make_int2(0, K::NEG_E);
     }
     const int32_t score = gbest >> 16;
     if (score >= SCORE_LIMIT) {
@@ -632,7 +675,24 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
         atomicAdd(fallback_count + 2, 1);  // re-run counter
         return;
     }
-    write_result(out, in, p, score, gbest & MATCH_MASK, la, la, lb);
+    write_result(out, in, p, score, gbest & K::MATCH_MASK, la, la, lb);
+}
+
+// One pair, one lane: the compact key when its rows fit (and wide_key is 0),
+// else the wide one.  Only a group of 32 sorted pairs that straddles 2047
+// rows runs both forms.
+template <int R, int V>
+__device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, const char *s_inc,
+                                  int32_t *s_best, int2 *win, int32_t W, int32_t lane,
+                                  int32_t *fallback, int32_t *fallback_count, int32_t *err,
+                                  int32_t one, int32_t wide_key) {
+    const PairGeom g = pair_geometry(in, p, err);
+    if (!wide_key && g.la <= KeyCompact::ROWS_MAX)
+        align_pair_strips_k<R, V, KeyCompact>(in, out, p, g, s_inc, s_best, win, W, lane, fallback,
+                                              fallback_count, one);
+    else
+        align_pair_strips_k<R, V, KeyWide>(in, out, p, g, s_inc, s_best, win, W, lane, fallback,
+                                           fallback_count, one);
 }
 
 // increment table + per-row first-max trackers (16 rows for the warp-per-pair phase)
@@ -664,7 +724,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
                 int32_t *__restrict__ wave_ticket, int32_t *__restrict__ fallback,
                 int32_t *__restrict__ fallback_count, int32_t *err, int32_t one, int32_t wave_rows,
-                int32_t wave_rows_force) {
+                int32_t wave_rows_force, int32_t wide_key) {
     extern __shared__ int32_t s_inc[];
     if (counters[0] <= 0) return;
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
@@ -709,7 +769,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
         const int32_t q = grp * 32 + lane;
         if (q < n_elig)
             align_pair_strips<R, V>(in, out, (int64_t)order[q], (const char *)s_inc, s_best, win, W, lane,
-                                 fallback, fallback_count, err, one);
+                                 fallback, fallback_count, err, one, wide_key);
     }
 }
 
@@ -1138,6 +1198,9 @@ static int32_t g_variant = -1;
 // resident CTAs of 256 threads per SM for strips of up to 16 rows: 2 (at most
 // 128 registers a thread) or 1 (up to 255); 0 = 2.  Taller strips always run 1.
 static int32_t g_ctas_per_sm = 0;
+// 1: the wide key for every pair of the strip kernel (measurement); 0
+// (default): the compact key for pairs of at most 2047 rows
+static int32_t g_wide_key = 0;
 // every pair runs one warp per pair when a call has at most this many pairs;
 // in larger calls, long pairs do: rows >= max(min rows, the adaptive bound)
 static int32_t g_wave_all_below = 40960;
@@ -1218,6 +1281,16 @@ int32_t sw_set_ctas_per_sm(int32_t v) {
 }
 int32_t sw_ctas_per_sm() { return g_ctas_per_sm; }
 
+int32_t sw_set_wide_key(int32_t v) {
+    if (v != 0 && v != 1) {
+        set_error(CK_ERR_UNSUPPORTED, "strip key form must be 0 (compact where rows fit) or 1 (wide)");
+        return CK_ERR_UNSUPPORTED;
+    }
+    g_wide_key = v;
+    return CK_OK;
+}
+int32_t sw_wide_key() { return g_wide_key; }
+
 // CTAs per SM the strip kernel of R rows runs at
 static int32_t strip_minb(int32_t rows) { return rows >= 24 ? 1 : (g_ctas_per_sm == 1 ? 1 : 2); }
 
@@ -1245,7 +1318,7 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     if (!window) return status;
     kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
                                               ticket + 5, fallback, fb_count, err, 1, wave_rows_for(wmax),
-                                              g_wave_stream == 2 ? 1 : 0);
+                                              g_wave_stream == 2 ? 1 : 0, g_wide_key);
     CK_CUDA(cudaGetLastError());
     if (ctr) ctr->launches += 1;
     return CK_OK;

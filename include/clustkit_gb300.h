@@ -205,7 +205,13 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_CTAS_PER_SM     resident 256-thread CTAs per SM of the strip
  *                          kernel for strips of 8 or 16 rows: 2 (default, 0)
  *                          at most 128 registers a thread, or 1 (up to 255);
- *                          strips of 24 or 32 rows always run 1 */
+ *                          strips of 24 or 32 rows always run 1
+ *   CK_CFG_STRIP_KEY       0 (default): the strip kernel packs pairs of at
+ *                          most 2047 rows in the compact key (11-bit match
+ *                          count, a gap-extension counter in place of a tie
+ *                          bit: fewer logic ops a cell), longer ones in the
+ *                          wide key (13-bit match count); 1: the wide key for
+ *                          every pair.  Results are the same either way. */
 #define CK_CFG_ROWS_PER_STRIP 0
 #define CK_CFG_STRIP_VARIANT 1
 #define CK_CFG_WAVE_MIN_ROWS 2
@@ -214,6 +220,7 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 #define CK_CFG_WAVE_STREAM 5
 #define CK_CFG_WAVE_ROWS 6
 #define CK_CFG_CTAS_PER_SM 8
+#define CK_CFG_STRIP_KEY 9
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 
@@ -474,7 +481,9 @@ int32_t ck_probe_int_rate(int32_t which, double *out_ops_per_s);
  * usable for clustkit's identity); 2 = int16x2 with match counts carried in
  * a second int16x2 register and picked by compare masks (what exact tracking
  * at two pairs a lane costs); 3 = form 0 with the strip's lower half one
- * column behind its upper half (two independent row chains a column).  A
+ * column behind its upper half (two independent row chains a column); 4 = a
+ * compact key with an 11-bit match count and a 3-bit gap-extension counter
+ * cleared every few cells in place of a tie bit set at every cell.  A
  * measurement of the cell arithmetic, no counterpart in clustkit. */
 int32_t ck_probe_cell_rate(int32_t form, double *out_cells_per_s);
 

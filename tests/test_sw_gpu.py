@@ -100,6 +100,72 @@ def test_rows_per_strip_settings(ck, golden, rows, variant, ctas, bw):
             set_config(k, v)
 
 
+def _key_form_set(seed):
+    """Sequences that stress the strip kernel's two key forms: lengths either
+    side of 2047 rows, two-letter low-complexity sequences (many equal-score
+    paths, so the gap-extension tie rule decides matches), and copies of
+    sequences with long inserted runs (gaps of up to 40 in either sequence,
+    far past the compact key's counter clears)."""
+    rng = np.random.default_rng(seed)
+    fam = synth.generate_families(6, 6, median=2040, lo=1900, hi=2200, seed=seed)
+    seqs = [fam.seq(i) for i in range(fam.n)]
+    for _ in range(24):
+        seqs.append(rng.choice(np.array([0, 7], dtype=np.uint8), int(rng.integers(300, 2300))))
+    for k in range(24):
+        base = seqs[k % 12].copy() if k < 12 else rng.integers(0, 20, 600).astype(np.uint8)
+        out, pos = [], 0
+        for cut in np.sort(rng.choice(base.size, 6, replace=False)):
+            out += [base[pos:cut], rng.integers(0, 20, int(rng.integers(5, 41))).astype(np.uint8)]
+            pos = cut
+        out.append(base[pos:])
+        seqs.append(np.concatenate(out))
+        seqs.append(base)
+    lengths = np.array([x.size for x in seqs], dtype=np.int32)
+    offsets = np.zeros(lengths.size, dtype=np.int64)
+    offsets[1:] = np.cumsum(lengths[:-1])
+    flat = np.concatenate(seqs).astype(np.uint8)
+    n = lengths.size
+    pairs = np.concatenate([np.stack([np.arange(36, 84, 2), np.arange(37, 84, 2)], 1),   # insert vs base
+                            np.stack([np.arange(12, 36), np.roll(np.arange(12, 36), 1)], 1),  # low complexity
+                            rng.integers(0, 36, (80, 2)),  # long family sequences
+                            rng.integers(0, n, (120, 2))]).astype(np.int32)
+    return flat, offsets, lengths, pairs
+
+
+@pytest.mark.parametrize("rows,variant", [(16, 1), (8, 3), (16, 0), (32, 1)])
+@pytest.mark.parametrize("bw", [3, 40, 300])
+def test_strip_key_forms_agree(ck, rows, variant, bw):
+    """The compact key (pairs of at most 2047 rows) and the wide key give the
+    oracle's results on the same pairs, including pairs on both sides of 2047
+    rows in one group of 32."""
+    from clustkit_gb300._lib import (CFG_ROWS_PER_STRIP, CFG_STRIP_KEY, CFG_STRIP_VARIANT, get_config,
+                                     set_config)
+    flat, offsets, lengths, pairs = _key_form_set(rows + bw)
+    sh = np.minimum(lengths[pairs[:, 0]], lengths[pairs[:, 1]])
+    assert (sh > 2047).any() and (sh <= 2047).any()
+    ref = oracle.sw_batch(pairs, flat, offsets, lengths, bw, BLOSUM62)
+    keys = (CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, CFG_STRIP_KEY)
+    keep = [get_config(k) for k in keys]
+    try:
+        set_config(CFG_ROWS_PER_STRIP, rows)
+        set_config(CFG_STRIP_VARIANT, variant)
+        with wave_config(all_below=0, min_rows=1 << 30):  # strip kernel only
+            for wide in (0, 1):
+                set_config(CFG_STRIP_KEY, wide)
+                _same(batch_sw(pairs, flat, offsets, lengths, bw, BLOSUM62), ref)
+    finally:
+        for k, v in zip(keys, keep):
+            set_config(k, v)
+
+
+def test_strip_key_setting_rejects_other_values(ck):
+    from clustkit_gb300._lib import CFG_STRIP_KEY, get_config, set_config
+    assert get_config(CFG_STRIP_KEY) == 0
+    with pytest.raises(Exception):
+        set_config(CFG_STRIP_KEY, 2)
+    assert get_config(CFG_STRIP_KEY) == 0
+
+
 @contextlib.contextmanager
 def wave_config(all_below, min_rows, adaptive=0, stream=1, rows=0):
     """Route pairs between the warp-per-pair and the lane-per-pair kernels."""
