@@ -132,7 +132,7 @@ def _key_form_set(seed):
     return flat, offsets, lengths, pairs
 
 
-@pytest.mark.parametrize("rows,variant", [(16, 1), (8, 3), (16, 0), (32, 1)])
+@pytest.mark.parametrize("rows,variant", [(16, 1), (8, 3), (16, 0), (32, 1), (8, 2), (24, 3)])
 @pytest.mark.parametrize("bw", [3, 40, 300])
 def test_strip_key_forms_agree(ck, rows, variant, bw):
     """The compact key (pairs of at most 2047 rows) and the wide key give the
