@@ -373,8 +373,8 @@ def run_ours(args, world, rank, local):
         _lib.set_config(_lib.CFG_ROWS_PER_STRIP, args.rows)
     if args.variant >= 0:
         _lib.set_config(_lib.CFG_STRIP_VARIANT, args.variant)
-    if args.ctas:
-        _lib.set_config(_lib.CFG_CTAS_PER_SM, args.ctas)
+    if args.threads:
+        _lib.set_config(_lib.CFG_STRIP_THREADS, args.threads)
     if args.strip_key:
         _lib.set_config(_lib.CFG_STRIP_KEY, args.strip_key)
     s, pairs, n_cand = build_workload(use_gpu=True, quick=args.quick)
@@ -448,15 +448,15 @@ def run_ours(args, world, rank, local):
                  "results_identical": bool(other_same), "in_use": "wide" if key_now else "compact"}
     sweep = {}
     if args.sweep:
-        keys = (_lib.CFG_ROWS_PER_STRIP, _lib.CFG_STRIP_VARIANT, _lib.CFG_CTAS_PER_SM)
+        keys = (_lib.CFG_ROWS_PER_STRIP, _lib.CFG_STRIP_VARIANT, _lib.CFG_STRIP_THREADS)
         keep = [_lib.get_config(k) for k in keys]
         for rows in (8, 16, 24, 32):
-            for ctas in ((2, 1) if rows <= 16 else (1,)):
+            for nt in ((512, 640, 768) if rows == 8 else (0,)):
                 for var in range(4):
-                    for k, v in zip(keys, (rows, var, ctas)):
+                    for k, v in zip(keys, (rows, var, nt)):
                         _lib.set_config(k, v)
                     t_r, _ = timed(ENGINE_BATCHED, 3, 1)
-                    sweep[f"R{rows}_V{var}_C{ctas}"] = round(cells / (t_r / 3) / 1e9, 1)
+                    sweep[f"R{rows}_V{var}_T{nt or (512 if rows == 16 else 256)}"] = round(cells / (t_r / 3) / 1e9, 1)
         for k, v in zip(keys, keep):
             _lib.set_config(k, v)
     # ---- plain engine (the plain GPU form), same pairs
@@ -1135,7 +1135,8 @@ def main():
     ap.add_argument("--search-batches-only", action="store_true",
                     help="search leg: only full batches per mode (a warm-up and a few), for profiler launch lists")
     ap.add_argument("--rows", type=int, default=0, help="rows per strip (8/16/24/32); 0 = library default")
-    ap.add_argument("--ctas", type=int, default=0, help="strip kernel CTAs per SM (1/2); 0 = library default")
+    ap.add_argument("--threads", type=int, default=0,
+                    help="strip kernel CTA threads for 8-row strips (512/640/768); 0 = library default")
     ap.add_argument("--strip-key", type=int, default=0, choices=[0, 1],
                     help="1: the strip kernel's wide key for every pair (default 0: compact where rows fit)")
     ap.add_argument("--variant", type=int, default=-1, help="strip kernel variant 0..3; -1 = library default (by strip height)")

@@ -31,8 +31,8 @@ CFG_WAVE_ALL_BELOW = 3
 CFG_WAVE_ADAPTIVE = 4
 CFG_WAVE_STREAM = 5
 CFG_WAVE_ROWS = 6
-CFG_CTAS_PER_SM = 8
 CFG_STRIP_KEY = 9
+CFG_STRIP_THREADS = 10
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32

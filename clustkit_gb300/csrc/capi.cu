@@ -720,7 +720,7 @@ int32_t ck_sw_set_config(int32_t key, int32_t value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) return sw_set_wave(2, value);
     if (key == CK_CFG_WAVE_STREAM) return sw_set_wave(3, value);
     if (key == CK_CFG_WAVE_ROWS) return sw_set_wave(4, value);
-    if (key == CK_CFG_CTAS_PER_SM) return sw_set_ctas_per_sm(value);
+    if (key == CK_CFG_STRIP_THREADS) return sw_set_strip_threads(value);
     if (key == CK_CFG_STRIP_KEY) return sw_set_wide_key(value);
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;
@@ -736,7 +736,7 @@ int32_t ck_sw_get_config(int32_t key, int32_t *value) {
     if (key == CK_CFG_WAVE_ADAPTIVE) { *value = sw_wave(2); return CK_OK; }
     if (key == CK_CFG_WAVE_STREAM) { *value = sw_wave(3); return CK_OK; }
     if (key == CK_CFG_WAVE_ROWS) { *value = sw_wave(4); return CK_OK; }
-    if (key == CK_CFG_CTAS_PER_SM) { *value = sw_ctas_per_sm(); return CK_OK; }
+    if (key == CK_CFG_STRIP_THREADS) { *value = sw_strip_threads(); return CK_OK; }
     if (key == CK_CFG_STRIP_KEY) { *value = sw_wide_key(); return CK_OK; }
     set_error(CK_ERR_INVALID_ARGUMENT, "unknown config key");
     return CK_ERR_INVALID_ARGUMENT;

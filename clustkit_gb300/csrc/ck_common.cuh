@@ -164,8 +164,8 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
                           int32_t *d_err, cudaStream_t st, SwCounters *ctr, bool read_counters);
 int32_t sw_set_rows_per_strip(int32_t r);
 int32_t sw_rows_per_strip();
-int32_t sw_set_ctas_per_sm(int32_t v);
-int32_t sw_ctas_per_sm();
+int32_t sw_set_strip_threads(int32_t v);
+int32_t sw_strip_threads();
 int32_t sw_set_wide_key(int32_t v);
 int32_t sw_wide_key();
 int32_t sw_set_variant(int32_t v);

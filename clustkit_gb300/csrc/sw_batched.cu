@@ -69,9 +69,11 @@ constexpr int32_t MATCH_MASK = (1 << 13) - 1;
 // rows: 11 bits of match count and, in bits 11..13, a counter that every gap
 // extension increments.  An opening starts from a clean H (counter 0) and an
 // extension from E or F plus one (counter >= 1), so extension still wins
-// every tie.  E's counter is cleared every 4 rows and F's after every group
-// of at most 4 columns, before it could carry into the priority bits: a few
-// logic ops per group instead of two per cell.
+// every tie.  E's counter is cleared at strip rows 5, 11, 17, ... and the
+// strip's last row (at most 6 extensions between clears, the window carrying
+// the count from one strip's last row into the next strip's first), F's after
+// every group of at most 4 columns, before either could carry into the
+// priority bits: a few logic ops per group instead of two per cell.
 struct KeyWide {
     static constexpr bool COMPACT = false;
     static constexpr int32_t CTR = 0;
@@ -92,7 +94,13 @@ struct KeyCompact {
     static constexpr int32_t ROWS_MAX = (1 << 11) - 1;
 };
 
-constexpr int STRIP_THREADS = 256;
+// Threads of the strip kernel's one persistent CTA per SM: 512 (16 warps at
+// up to 128 registers) for strips of 8 or 16 rows, 640 or 768 (20 or 24
+// warps at 96 or 80 registers) for 8-row strips, 256 (8 warps, up to 255
+// registers) for 24 or 32 rows.  One CTA per SM holds one increment table,
+// so the warps a CTA adds cost no table copy.  Each warp keeps its strip
+// rows' first-maximum trackers in a block of its own (row r of lane l at
+// r * 32 + l), so the layout does not depend on the CTA's size.
 // per warp, the streamed warp-per-pair phase's pair slots in shared memory
 constexpr size_t WAVE_SLOT_BYTES = 72;  // sizeof(WaveSlot), checked where it is defined
 constexpr int WAVE_SLOTS_PER_WARP = 16;
@@ -379,7 +387,7 @@ __device__ __forceinline__ void strip_cell(uint32_t bcol, int32_t &hu, int32_t &
     S.hc[r] = hn;
     S.fT[r] = fTn;
     hu = hn;
-    if constexpr (K::COMPACT) eu = (r & 3) == 3 ? (eR & ~K::CTR) : eR;
+    if constexpr (K::COMPACT) eu = (r % 6 == 5 || r == R - 1) ? (eR & ~K::CTR) : eR;
     else eu = eR | TBIT;
 }
 
@@ -479,8 +487,8 @@ __device__ __forceinline__ void strip_track(const int32_t (&hs)[U][R], int32_t &
             for (int u = 0; u < U; ++u) {
                 const int32_t v = hs[u][r];
                 if (v > tthr) {
-                    const int32_t b = s_best[r * STRIP_THREADS];
-                    if (v > (b | (KU - 1))) s_best[r * STRIP_THREADS] = v;
+                    const int32_t b = s_best[r * 32];
+                    if (v > (b | (KU - 1))) s_best[r * 32] = v;
                 }
             }
         }
@@ -621,7 +629,7 @@ __device__ __forceinline__ void align_pair_strips_k(const SwIn &in, const SwOut 
         for (int r = 0; r < R; ++r) {
             S.hc[r] = 0;
             S.fT[r] = K::NEG_F;
-            s_best[r * STRIP_THREADS] = gbest;
+            s_best[r * 32] = gbest;
             // rows below the pair's last row (last strip only) read the pad code
             const uint32_t code = (r < alive) ? (uint32_t)A[i0 + r - 1] : PAD_CODE;
             S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
@@ -660,7 +668,7 @@ __device__ __forceinline__ void align_pair_strips_k(const SwIn &in, const SwOut 
         // (pad rows never hold a new best: their values stay below a real cell's)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const int32_t b = s_best[r * STRIP_THREADS];
+            const int32_t b = s_best[r * 32];
             if (b > (gbest | (KU - 1))) gbest = b;
         }
         // the columns right of this strip's band read as out-of-band for the next strip
@@ -695,11 +703,14 @@ __device__ void align_pair_strips(const SwIn &in, const SwOut &out, int64_t p, c
                                            fallback_count, one);
 }
 
-// increment table + per-row first-max trackers (16 rows for the warp-per-pair phase)
+// increment table + per-row first-max trackers (16 rows for the warp-per-pair
+// phase) + the warp-per-pair slots, for a CTA of NT threads
 template <int R>
+constexpr int track_rows() { return R > 16 ? R : 16; }
+template <int R, int NT>
 __host__ __device__ constexpr size_t strip_smem() {
-    return INC_SMEM + (size_t)(R > 16 ? R : 16) * STRIP_THREADS * sizeof(int32_t) +
-           (size_t)(STRIP_THREADS / 32) * WAVE_SLOTS_PER_WARP * WAVE_SLOT_BYTES;
+    return INC_SMEM + (size_t)track_rows<R>() * NT * sizeof(int32_t) +
+           (size_t)(NT / 32) * WAVE_SLOTS_PER_WARP * WAVE_SLOT_BYTES;
 }
 
 __device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &out, int64_t p,
@@ -717,8 +728,8 @@ __device__ __noinline__ void wave_stream_any(int32_t rows, const SwIn &in, const
 // small call), then the rest 32 pairs per warp, one lane per pair, in
 // register strips of R rows.  Long pairs thus start first and the lane-per-
 // pair groups fill in around them.
-template <int R, int V, int MINB>
-__global__ void __launch_bounds__(STRIP_THREADS, MINB)
+template <int R, int V, int NT>
+__global__ void __launch_bounds__(NT, 1)
 sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
                 const int32_t *__restrict__ counters, const int32_t *__restrict__ inc_global,
                 int2 *__restrict__ window, int32_t W, int32_t *__restrict__ ticket,
@@ -729,7 +740,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
     if (counters[0] <= 0) return;
     for (int t = threadIdx.x; t < INC_ENTRIES * 32; t += blockDim.x) s_inc[t] = inc_global[t >> 5];
     __syncthreads();
-    int32_t *s_best = s_inc + INC_ENTRIES * 32 + threadIdx.x;
+    int32_t *s_best = s_inc + INC_ENTRIES * 32 + (threadIdx.x >> 5) * (track_rows<R>() * 32) + (threadIdx.x & 31);
     const int32_t lane = threadIdx.x & 31;
     const int32_t n_wave = counters[6];
     // stream the pairs' strips through each warp when there are more pairs than
@@ -738,7 +749,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
     const int32_t n_warps = (int32_t)((gridDim.x * blockDim.x) >> 5);
     if (wave_rows > 0 && (wave_rows_force || n_wave > n_warps)) {
         // slots behind the increment table and the per-row trackers
-        char *slot_base = (char *)(s_inc + INC_ENTRIES * 32 + (R > 16 ? R : 16) * STRIP_THREADS);
+        char *slot_base = (char *)(s_inc + INC_ENTRIES * 32 + track_rows<R>() * NT);
         WaveSlot *slots = (WaveSlot *)(slot_base + (size_t)(threadIdx.x >> 5) * WAVE_SLOTS_PER_WARP *
                                                        WAVE_SLOT_BYTES);
         if (n_wave > 0)
@@ -842,7 +853,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             for (int r = 0; r < R; ++r) {
                 S.hc[r] = 0;
                 S.fT[r] = NEG_F;
-                s_best[r * STRIP_THREADS] = 0;
+                s_best[r * 32] = 0;
                 const uint32_t code = (r < alive && s < n_strips) ? (uint32_t)A[i0 + r - 1] : 0u;
                 S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
             }
@@ -850,7 +861,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
         auto merge = [&]() {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const int32_t b = s_best[r * STRIP_THREADS];
+                const int32_t b = s_best[r * 32];
                 if (r < alive && b > (lbest | (KU - 1))) { lbest = b; lrow = i0 + r; }
             }
         };
@@ -891,8 +902,8 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             if (__any_sync(0xffffffffu, (cm >> 16) >= gs)) {
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    const int32_t b = s_best[r * STRIP_THREADS];
-                    if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
+                    const int32_t b = s_best[r * 32];
+                    if (S.hc[r] > (b | (KU - 1))) s_best[r * 32] = S.hc[r];
                 }
                 const int32_t m = __reduce_max_sync(0xffffffffu, cm >> 16);
                 if (m > gs) gs = m;
@@ -1085,7 +1096,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             for (int r = 0; r < R; ++r) {
                 S.hc[r] = 0;
                 S.fT[r] = NEG_F;
-                s_best[r * STRIP_THREADS] = 0;
+                s_best[r * 32] = 0;
                 const uint32_t code = r < alive ? (uint32_t)A[i0 + r - 1] : 0u;
                 S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
             }
@@ -1127,8 +1138,8 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             if (has) {
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    const int32_t b = s_best[r * STRIP_THREADS];
-                    if (S.hc[r] > (b | (KU - 1))) s_best[r * STRIP_THREADS] = S.hc[r];
+                    const int32_t b = s_best[r * 32];
+                    if (S.hc[r] > (b | (KU - 1))) s_best[r * 32] = S.hc[r];
                 }
                 if (cm > 0) atomicMax(&slots[cur_slot].gs, cm >> 16);
             }
@@ -1138,7 +1149,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             int32_t bk = 0, br = 0;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const int32_t b = s_best[r * STRIP_THREADS];
+                const int32_t b = s_best[r * 32];
                 if (r < alive && b > (bk | (KU - 1))) { bk = b; br = i0 + r; }
             }
             WaveSlot &sl = slots[cur_slot];
@@ -1195,9 +1206,10 @@ static int32_t g_rows_per_strip = 0;  // 0: by band width (8 up to w = 64, else 
 // -1 (default): by strip height -- groups of 4 columns at 8 rows (3), of 2
 // above (1); 0..3 as set (see StripVariant)
 static int32_t g_variant = -1;
-// resident CTAs of 256 threads per SM for strips of up to 16 rows: 2 (at most
-// 128 registers a thread) or 1 (up to 255); 0 = 2.  Taller strips always run 1.
-static int32_t g_ctas_per_sm = 0;
+// threads of the strip kernel's CTA for 8-row strips: 512, 640 or 768; 0 =
+// by call (640, or 512 when every pair may run one warp per pair, whose code
+// would spill at 96 registers).  16-row strips run 512, taller ones 256.
+static int32_t g_strip_threads = 0;
 // 1: the wide key for every pair of the strip kernel (measurement); 0
 // (default): the compact key for pairs of at most 2047 rows
 static int32_t g_wide_key = 0;
@@ -1255,11 +1267,6 @@ int32_t sw_set_variant(int32_t v) {
 }
 int32_t sw_variant() { return g_variant; }
 
-template <int R>
-static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
-                               const int32_t *counters, const int32_t *inc, int32_t wmax,
-                               int32_t *ticket, int32_t *fallback, int32_t *fb_count,
-                               int32_t *err, cudaStream_t st, SwCounters *ctr);
 
 int32_t sw_set_rows_per_strip(int32_t r) {
     if (r != 0 && r != 8 && r != 16 && r != 24 && r != 32) {
@@ -1271,15 +1278,15 @@ int32_t sw_set_rows_per_strip(int32_t r) {
 }
 int32_t sw_rows_per_strip() { return g_rows_per_strip; }
 
-int32_t sw_set_ctas_per_sm(int32_t v) {
-    if (v < 0 || v > 2) {
-        set_error(CK_ERR_UNSUPPORTED, "strip kernel CTAs per SM must be 0 (default), 1 or 2");
+int32_t sw_set_strip_threads(int32_t v) {
+    if (v != 0 && v != 512 && v != 640 && v != 768) {
+        set_error(CK_ERR_UNSUPPORTED, "strip kernel threads per CTA must be 0 (default), 512, 640 or 768");
         return CK_ERR_UNSUPPORTED;
     }
-    g_ctas_per_sm = v;
+    g_strip_threads = v;
     return CK_OK;
 }
-int32_t sw_ctas_per_sm() { return g_ctas_per_sm; }
+int32_t sw_strip_threads() { return g_strip_threads; }
 
 int32_t sw_set_wide_key(int32_t v) {
     if (v != 0 && v != 1) {
@@ -1291,32 +1298,40 @@ int32_t sw_set_wide_key(int32_t v) {
 }
 int32_t sw_wide_key() { return g_wide_key; }
 
-// CTAs per SM the strip kernel of R rows runs at
-static int32_t strip_minb(int32_t rows) { return rows >= 24 ? 1 : (g_ctas_per_sm == 1 ? 1 : 2); }
+// threads of the strip kernel's CTA (one per SM) for strips of `rows` rows
+// in a call of M pairs
+static int32_t strip_threads(int32_t rows, int64_t M) {
+    if (rows >= 24) return 256;
+    if (rows == 16) return 512;
+    if (g_strip_threads) return g_strip_threads;
+    return M <= (int64_t)g_wave_all_below ? 512 : 640;
+}
 
-template <int R, int V, int MINB>
+template <int R, int V, int NT>
 static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *order,
                              const int32_t *counters, const int32_t *inc, int32_t wmax,
                              int32_t *ticket, int32_t *fallback, int32_t *fb_count,
                              int32_t *err, cudaStream_t st, SwCounters *ctr) {
     int32_t status = CK_OK;
-    auto kern = sw_strip_kernel<R, V, MINB>;
-    const size_t smem = strip_smem<R>();
+    auto kern = sw_strip_kernel<R, V, NT>;
+    const size_t smem = strip_smem<R, NT>();
     CK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, STRIP_THREADS, smem));
-    if (per_sm > MINB) per_sm = MINB;  // the CTAs per SM the setting asks for, even if more would fit
-    if (per_sm < 1) per_sm = 1;
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (per_sm < 1) {
+        set_error(CK_ERR_UNSUPPORTED, "strip kernel CTA does not fit an SM");
+        return CK_ERR_UNSUPPORTED;
+    }
     const int32_t W = pow2_at_least(2 * (int64_t)wmax + 2 * R + 2);
     // one window of W columns per lane; keep the total under 8 GiB
-    const size_t per_block = (size_t)STRIP_THREADS * (size_t)W * sizeof(int2);
-    int blocks = sm_count() * per_sm;
+    const size_t per_block = (size_t)NT * (size_t)W * sizeof(int2);
+    int blocks = sm_count();  // one persistent CTA per SM
     const size_t cap = (size_t)8 << 30;
     if ((size_t)blocks * per_block > cap) blocks = (int)(cap / per_block);
     if (blocks < 1) blocks = 1;
     int2 *window = (int2 *)scratch(SLOT_WINDOW, (size_t)blocks * per_block, &status);
     if (!window) return status;
-    kern<<<blocks, STRIP_THREADS, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
+    kern<<<blocks, NT, smem, st>>>(in, out, order, counters, inc, window, W, ticket,
                                               ticket + 5, fallback, fb_count, err, 1, wave_rows_for(wmax),
                                               g_wave_stream == 2 ? 1 : 0, g_wide_key);
     CK_CUDA(cudaGetLastError());
@@ -1324,28 +1339,37 @@ static int32_t launch_strips(const SwIn &in, const SwOut &out, const uint32_t *o
     return CK_OK;
 }
 
-template <int R, int MINB>
+template <int R, int NT>
 static int32_t launch_strips_m(const SwIn &in, const SwOut &out, const uint32_t *order,
                                const int32_t *counters, const int32_t *inc, int32_t wmax,
                                int32_t *ticket, int32_t *fallback, int32_t *fb_count,
                                int32_t *err, cudaStream_t st, SwCounters *ctr) {
     switch (g_variant >= 0 ? g_variant : (R <= 8 ? 3 : 1)) {
-        case 0: return launch_strips<R, 0, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-        case 2: return launch_strips<R, 2, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-        case 3: return launch_strips<R, 3, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-        default: return launch_strips<R, 1, MINB>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 0: return launch_strips<R, 0, NT>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 2: return launch_strips<R, 2, NT>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        case 3: return launch_strips<R, 3, NT>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        default: return launch_strips<R, 1, NT>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
     }
 }
 
+// strips of R rows in CTAs of nt threads (strip_threads: 512/640/768 for 8 rows,
+// 512 for 16, 256 for 24 and 32)
 template <int R>
 static int32_t launch_strips_v(const SwIn &in, const SwOut &out, const uint32_t *order,
                                const int32_t *counters, const int32_t *inc, int32_t wmax,
                                int32_t *ticket, int32_t *fallback, int32_t *fb_count,
-                               int32_t *err, cudaStream_t st, SwCounters *ctr) {
-    if (R >= 24 || strip_minb(R) == 1)
-        return launch_strips_m<R, 1>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
-    return launch_strips_m<(R >= 24 ? 16 : R), 2>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count,
-                                                   err, st, ctr);
+                               int32_t *err, cudaStream_t st, SwCounters *ctr, int32_t nt) {
+    if constexpr (R >= 24) {
+        return launch_strips_m<R, 256>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+    } else if constexpr (R == 8) {
+        if (nt == 768)
+            return launch_strips_m<R, 768>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        if (nt == 640)
+            return launch_strips_m<R, 640>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+        return launch_strips_m<R, 512>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+    } else {
+        return launch_strips_m<R, 512>(in, out, order, counters, inc, wmax, ticket, fallback, fb_count, err, st, ctr);
+    }
 }
 
 int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int8_t *d_sub,
@@ -1395,25 +1419,25 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
         // narrow bands: a strip's ramps (R - 1 masked columns at each end) weigh
         // against 2w + 1 interior columns, so fewer rows per strip win there
         const int32_t rows = g_rows_per_strip ? g_rows_per_strip : (wmax <= 64 ? 8 : 16);
+        const int32_t nt = strip_threads(rows, M);
         wave_split_kernel<<<1, 32, 0, st>>>(dk.Current(), cnt, in.band_width, g_wave_all_below,
-                                            g_wave_min_rows, g_wave_adaptive,
-                                            (int64_t)sm_count() * strip_minb(rows) * STRIP_THREADS);
+                                            g_wave_min_rows, g_wave_adaptive, (int64_t)sm_count() * nt);
         CK_CUDA(cudaGetLastError());
         // profiling events bracket the alignment kernel
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         if (profile_events(&ev0, &ev1)) CK_CUDA(cudaEventRecord(ev0, st));
         switch (rows) {
             case 8:
-                CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<8>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr, nt));
                 break;
             case 24:
-                CK_TRY(launch_strips_v<24>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<24>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr, nt));
                 break;
             case 32:
-                CK_TRY(launch_strips_v<32>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<32>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr, nt));
                 break;
             default:
-                CK_TRY(launch_strips_v<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr));
+                CK_TRY(launch_strips_v<16>(in, out, order, cnt, inc, wmax, cnt + 2, fb, cnt + 1, d_err, st, ctr, nt));
                 break;
         }
         if (ev1) CK_CUDA(cudaEventRecord(ev1, st));

@@ -41,20 +41,22 @@ from .cells import band_cells, effective_band
 KEYS = {
     "rows_per_strip": _lib.CFG_ROWS_PER_STRIP,
     "strip_variant": _lib.CFG_STRIP_VARIANT,
-    "ctas_per_sm": _lib.CFG_CTAS_PER_SM,
+    "strip_threads": _lib.CFG_STRIP_THREADS,
     "wave_min_rows": _lib.CFG_WAVE_MIN_ROWS,
     "wave_all_below": _lib.CFG_WAVE_ALL_BELOW,
     "wave_adaptive": _lib.CFG_WAVE_ADAPTIVE,
 }
 
-DEFAULT = {"rows_per_strip": 0, "strip_variant": -1, "ctas_per_sm": 0, "wave_min_rows": 512,
+DEFAULT = {"rows_per_strip": 0, "strip_variant": -1, "strip_threads": 0, "wave_min_rows": 512,
            "wave_all_below": 40960, "wave_adaptive": 1}
 
 # bin-edge candidates: (wave_min_rows, wave_adaptive); 1 << 30 = never by length
 BIN_EDGES = [(512, 1), (256, 1), (512, 0), (1024, 0), (2048, 0), (4096, 0), (1 << 30, 0)]
-# (rows per strip, strip variant, CTAs per SM); strips of 24 or 32 rows always run 1 CTA per SM
-TILINGS = ([(r, v, c) for r in (8, 16) for v in (0, 1, 2, 3) for c in (1, 2)] +
-           [(r, v, 1) for r in (24, 32) for v in (0, 1)])
+# (rows per strip, strip variant, threads of the strip kernel's CTA); 0 = the
+# library's choice (the only one for 16, 24 and 32 rows)
+TILINGS = ([(8, v, t) for v in (0, 1, 2, 3) for t in (512, 640, 768)] +
+           [(16, v, 0) for v in (0, 1, 2, 3)] +
+           [(r, v, 0) for r in (24, 32) for v in (0, 1)])
 
 _cache: dict = {}
 
@@ -187,8 +189,8 @@ def autotune(pairs, flat, offsets, lengths, band_width: int, repeats: int = 5,
             trial({**base, "wave_min_rows": mr, "wave_adaptive": ad})
         edge = {k: best[k] for k in ("wave_min_rows", "wave_adaptive")}
         for r, v, c in TILINGS:
-            trial({**base, **edge, "rows_per_strip": r, "strip_variant": v, "ctas_per_sm": c})
-        tiling = {k: best[k] for k in ("rows_per_strip", "strip_variant", "ctas_per_sm")}
+            trial({**base, **edge, "rows_per_strip": r, "strip_variant": v, "strip_threads": c})
+        tiling = {k: best[k] for k in ("rows_per_strip", "strip_variant", "strip_threads")}
         for mr, ad in BIN_EDGES:
             cfg = {**base, **tiling, "wave_min_rows": mr, "wave_adaptive": ad}
             if not any(c == cfg for c, _ in trials):

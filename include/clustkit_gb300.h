@@ -202,10 +202,15 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *                          (key 7, a cluster-shared-memory form of the
  *                          similar-k-mer posting walk, is retired: it
  *                          measured 2.6x slower than the L2-atomic walk)
- *   CK_CFG_CTAS_PER_SM     resident 256-thread CTAs per SM of the strip
- *                          kernel for strips of 8 or 16 rows: 2 (default, 0)
- *                          at most 128 registers a thread, or 1 (up to 255);
- *                          strips of 24 or 32 rows always run 1
+ *   CK_CFG_STRIP_THREADS   threads of the strip kernel's one persistent CTA
+ *                          per SM for strips of 8 rows: 512 (16 warps, up to
+ *                          128 registers), 640 (20 warps, 96) or 768 (24, 80);
+ *                          0 (default): 640, or 512 in calls with at most
+ *                          CK_CFG_WAVE_ALL_BELOW pairs (the warp-per-pair code
+ *                          spills at 96 registers).  Strips of 16 rows always
+ *                          run 512 threads, of 24 or 32 rows 256.  (Key 8,
+ *                          CTAs of 256 threads per SM, is retired: one CTA of
+ *                          512 threads measured at least as fast in every case.)
  *   CK_CFG_STRIP_KEY       0 (default): the strip kernel packs pairs of at
  *                          most 2047 rows in the compact key (11-bit match
  *                          count, a gap-extension counter in place of a tie
@@ -219,8 +224,8 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
 #define CK_CFG_WAVE_ADAPTIVE 4
 #define CK_CFG_WAVE_STREAM 5
 #define CK_CFG_WAVE_ROWS 6
-#define CK_CFG_CTAS_PER_SM 8
 #define CK_CFG_STRIP_KEY 9
+#define CK_CFG_STRIP_THREADS 10
 int32_t ck_sw_set_config(int32_t key, int32_t value);
 int32_t ck_sw_get_config(int32_t key, int32_t *value);
 

@@ -12,8 +12,9 @@ ties) and carries the winner's match count.  Two forms of the tie mark:
 
 * wide: 13-bit match count and a tie bit (2^13) set on every stored E and F;
 * compact (pairs of <= 2047 rows): 11-bit match count and a 3-bit counter at
-  bits 11..13 that every gap extension increments; E's counter is cleared
-  every 4 rows, F's every (at most) 4 columns.
+  bits 11..13 that every gap extension increments; E's counter is cleared at
+  strip rows 5, 11, 17, ... and each strip's last row (strips of R rows), F's
+  every (at most) 4 columns.
 
 This restates that arithmetic in numpy, row by row over many pairs of one
 shape at once, and checks score and first-maximum match count against the
@@ -55,9 +56,10 @@ def _inc_table():
     return t
 
 
-def model_keys(A, B, w, hint, form):
+def model_keys(A, B, w, hint, form, R=16):
     """Best score and first-max match count of each pair (rows A[p] against
-    columns B[p], all of one shape), by the kernel's key arithmetic."""
+    columns B[p], all of one shape), by the kernel's key arithmetic with
+    strips of R rows (the E counter clears)."""
     f_ = FORMS[form]
     P, la = A.shape
     lb = B.shape[1]
@@ -87,7 +89,8 @@ def model_keys(A, B, w, hint, form):
             h = np.maximum(np.maximum(diag, e), f) & f_["clean"]
             if f_["counter"]:
                 max_ctr = max(max_ctr, int(((e >> 11) & 7).max()), int(((f >> 11) & 7).max()))
-                e_st = e & ~CTR if i % 4 == 0 else e  # strip row (i - 1) % R, R a multiple of 4
+                r = (i - 1) % R  # the strip row
+                e_st = e & ~CTR if (r % 6 == 5 or r == R - 1) else e
             else:
                 e_st = e | TBIT if f_["tie_bit"] else e
             upd = (h >> 16) > (best >> 16)  # strict '>' in row-major order: the first maximum
@@ -149,12 +152,21 @@ def test_key_forms_match_oracle(la, lb, bw, hint):
     ref_s, ref_m = _oracle(A, B, bw, hint)
     longer = max(la, lb)
     w = longer if (bw <= 0 or longer <= 50) else bw
-    for form in ("wide", "compact"):
-        s, m, max_ctr = model_keys(A, B, w, hint, form)
-        assert np.array_equal(s, ref_s), form
-        assert np.array_equal(m, ref_m), form
+    for form, R in (("wide", 16), ("compact", 8), ("compact", 16), ("compact", 24), ("compact", 32)):
+        s, m, max_ctr = model_keys(A, B, w, hint, form, R)
+        assert np.array_equal(s, ref_s), (form, R)
+        assert np.array_equal(m, ref_m), (form, R)
         if form == "compact":
-            assert 1 <= max_ctr <= 4  # extensions happened; never near a carry into the priority bits
+            assert 1 <= max_ctr <= 6  # extensions happened; never a carry into the priority bits
+
+
+@pytest.mark.parametrize("R", [8, 16, 24, 32])
+def test_e_counter_clears_bound_the_count(R):
+    """At most 6 extensions between two E clears, counted across strip
+    boundaries (the window carries the last row's E into the next strip)."""
+    clears = [r for r in range(R) if r % 6 == 5 or r == R - 1]
+    gaps = [b - a for a, b in zip(clears, clears[1:])] + [clears[0] + R - clears[-1]]
+    assert max(gaps) <= 6 and clears[-1] == R - 1
 
 
 def test_tie_mark_matters():

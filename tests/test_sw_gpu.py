@@ -72,18 +72,18 @@ def test_random_families_vs_oracle(ck, engine, bw, median, hi, dist, route):
     assert np.array_equal(r["mask"], ref["sims"] >= np.float32(0.3))
 
 
-@pytest.mark.parametrize("rows,variant,ctas", [(8, 1, 2), (16, 1, 2), (24, 1, 1), (16, 3, 2), (8, 3, 2),
-                                               (24, 3, 1), (16, 1, 1), (16, 3, 1), (8, 1, 1), (32, 1, 1),
-                                               (32, 3, 1), (16, 0, 2), (16, 2, 2), (8, 0, 1), (32, 0, 1),
-                                               (24, 2, 1)])
+@pytest.mark.parametrize("rows,variant,threads", [(8, 1, 640), (16, 1, 0), (24, 1, 0), (16, 3, 0), (8, 3, 640),
+                                                  (24, 3, 0), (8, 3, 512), (8, 3, 768), (8, 1, 512), (32, 1, 0),
+                                                  (32, 3, 0), (16, 0, 0), (16, 2, 0), (8, 0, 768), (32, 0, 0),
+                                                  (24, 2, 0), (8, 2, 640), (8, 0, 512), (8, 1, 768)])
 @pytest.mark.parametrize("bw", [3, 32, 100, 0])
-def test_rows_per_strip_settings(ck, golden, rows, variant, ctas, bw):
-    from clustkit_gb300._lib import (CFG_CTAS_PER_SM, CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, get_config,
+def test_rows_per_strip_settings(ck, golden, rows, variant, threads, bw):
+    from clustkit_gb300._lib import (CFG_ROWS_PER_STRIP, CFG_STRIP_THREADS, CFG_STRIP_VARIANT, get_config,
                                      set_config)
-    keys = (CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, CFG_CTAS_PER_SM)
+    keys = (CFG_ROWS_PER_STRIP, CFG_STRIP_VARIANT, CFG_STRIP_THREADS)
     keep = [get_config(k) for k in keys]
     try:
-        for k, v in zip(keys, (rows, variant, ctas)):
+        for k, v in zip(keys, (rows, variant, threads)):
             set_config(k, v)
         with wave_config(all_below=0, min_rows=1 << 30):  # strip kernel only
             g = golden("sw_golden.npz")

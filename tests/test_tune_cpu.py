@@ -17,9 +17,9 @@ def test_candidate_sets_cover_the_tunables():
     assert set(tune.DEFAULT) == set(tune.KEYS)
     assert {r for r, _, _ in tune.TILINGS} == {8, 16, 24, 32}
     assert {v for _, v, _ in tune.TILINGS} == {0, 1, 2, 3}
-    assert {c for _, _, c in tune.TILINGS} == {1, 2}
-    # taller strips only exist at one CTA per SM
-    assert all(c == 1 for r, _, c in tune.TILINGS if r > 16)
+    assert {t for _, _, t in tune.TILINGS} == {0, 512, 640, 768}
+    # the CTA's threads are a choice for 8-row strips only
+    assert all(t == 0 for r, _, t in tune.TILINGS if r > 8)
     assert (tune.DEFAULT["wave_min_rows"], tune.DEFAULT["wave_adaptive"]) in tune.BIN_EDGES
 
 
