@@ -266,6 +266,7 @@ __global__ void wave_split_kernel(const uint32_t *__restrict__ sorted_keys, int3
     counters[6] = 0;
     if (n_elig <= 0) return;
     const int32_t max_rows = (int32_t)(sorted_keys[0] >> 13);
+    counters[8] = max_rows;  // the warp-per-pair phase's key form depends on it
     const bool all_capable = (band_width >= 1 && 2 * band_width < 31 * 16 + 32) || max_rows <= 512;
     if (!all_capable) return;
     if (n_elig <= all_below) { counters[6] = n_elig; return; }
@@ -324,12 +325,14 @@ __device__ __forceinline__ uint32_t band_rows(int32_t d, uint32_t w2, int32_t al
 // Cells of rows [RB, RE) at one column, top to bottom.  (hu, eu) enter as
 // H and E of row RB - 1 at column j, hdiag as H of row RB - 1 at column
 // j - 1; they leave as the values of row RE - 1.  Stored keys: H clean
-// (score * 2^16 + matches), E and F with the tie bit set.
+// (score * 2^16 + matches), E and F with the tie bit set (wide key) or their
+// extension counters (compact key: E's cleared here at the strip rows the
+// lane-per-pair kernel clears them, F's by the caller every 4 columns).
 //     diag = max(Hdiag + inc, ZERO)
 //     E    = max(E_up - 2^16, H_up + OPEN_E) | tie
 //     F    = max(F_left - 2^16, H_left + OPEN_F) | tie
 //     H    = max(diag, E, F) & CLEAN
-template <int R, int RB, int RE, bool MASKED>
+template <int R, int RB, int RE, bool MASKED, class K>
 __device__ __forceinline__ void strip_cells(uint32_t bcol, int32_t &hu, int32_t &eu, int32_t hdiag,
                                             StripRegs<R> &S, const char *s_inc, uint32_t rmask, int32_t one) {
     using namespace key;
@@ -347,20 +350,21 @@ __device__ __forceinline__ void strip_cells(uint32_t bcol, int32_t &hu, int32_t 
             // that row's H: only H_up + OPEN_E and the max-of-three sit on the
             // row-to-row dependency chain.  E's tie bit plays no part in H
             // (E, F, diag and zero differ in priority), so it is set off the chain.
-            const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, EXT, one));
-            const int32_t fTn = __viaddmax_s32(S.fT[r], EXT, fadd(S.hc[r], OPEN_F, one)) | TBIT;
-            const int32_t hn = __vimax3_s32(diagc, eR, fTn) & CLEAN;
-            const int32_t eT = eR | TBIT;
+            const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, K::EXT, one));
+            int32_t fTn = __viaddmax_s32(S.fT[r], K::EXT, fadd(S.hc[r], OPEN_F, one));
+            if constexpr (!K::COMPACT) fTn |= TBIT;
+            const int32_t hn = __vimax3_s32(diagc, eR, fTn) & K::CLEAN;
             hdiag = S.hc[r];
             S.hc[r] = hn;
             S.fT[r] = fTn;
             hu = hn;
-            eu = eT;
+            if constexpr (K::COMPACT) eu = (r % 6 == 5 || r == R - 1) ? (eR & ~K::CTR) : eR;
+            else eu = eR | TBIT;
         } else {
             hdiag = S.hc[r];
             S.hc[r] = 0;
             hu = 0;
-            eu = NEG_E;
+            eu = K::NEG_E;
         }
     }
 }
@@ -716,12 +720,12 @@ __host__ __device__ constexpr size_t strip_smem() {
 __device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &out, int64_t p,
                                                  const char *s_inc, int32_t *s_best, int32_t lane,
                                                  int32_t *fallback, int32_t *fallback_count,
-                                                 int32_t *err, int32_t one);
+                                                 int32_t *err, int32_t one, int32_t wide_key);
 struct WaveSlot;
 __device__ __noinline__ void wave_stream_any(int32_t rows, const SwIn &in, const SwOut &out, const uint32_t *order,
                                              int32_t n_wave, int32_t *ticket, const char *s_inc, int32_t *s_best,
                                              WaveSlot *slots, int32_t lane, int32_t *fallback,
-                                             int32_t *fallback_count, int32_t *err, int32_t one);
+                                             int32_t *fallback_count, int32_t *err, int32_t one, int32_t compact);
 
 // Persistent alignment kernel.  Its warps first take the leading
 // counters[6] sorted pairs one warp per pair (long pairs, or every pair of a
@@ -752,9 +756,12 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
         char *slot_base = (char *)(s_inc + INC_ENTRIES * 32 + track_rows<R>() * NT);
         WaveSlot *slots = (WaveSlot *)(slot_base + (size_t)(threadIdx.x >> 5) * WAVE_SLOTS_PER_WARP *
                                                        WAVE_SLOT_BYTES);
+        // the compact key when every pair of the call (so every warp-per-pair
+        // pair) has at most 2047 rows
         if (n_wave > 0)
             wave_stream_any(wave_rows, in, out, order, n_wave, wave_ticket, (const char *)s_inc, s_best, slots,
-                            lane, fallback, fallback_count, err, one);
+                            lane, fallback, fallback_count, err, one,
+                            !wide_key && counters[8] <= KeyCompact::ROWS_MAX);
     } else {
         for (;;) {
             __syncwarp();
@@ -763,7 +770,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
             q = __shfl_sync(0xffffffffu, q, 0);
             if (q >= n_wave) break;
             align_pair_wave_any(in, out, (int64_t)order[q], (const char *)s_inc, s_best, lane, fallback,
-                                fallback_count, err, one);
+                                fallback_count, err, one, wide_key);
         }
     }
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -804,7 +811,7 @@ sw_strip_kernel(SwIn in, SwOut out, const uint32_t *__restrict__ order,
 // of a strip its rows merge into the lane's best in row order (strict '>');
 // at the end of the pair the lanes agree on the best score, then on the
 // lowest row holding it -- clustkit's first cell in row-major order.
-template <int R>
+template <int R, class K>
 __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, const PairGeom &g,
                                 const char *s_inc, int32_t *s_best, int32_t lane, int32_t *fallback,
                                 int32_t *fallback_count, int32_t one) {
@@ -852,7 +859,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 S.hc[r] = 0;
-                S.fT[r] = NEG_F;
+                S.fT[r] = K::NEG_F;
                 s_best[r * 32] = 0;
                 const uint32_t code = (r < alive && s < n_strips) ? (uint32_t)A[i0 + r - 1] : 0u;
                 S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
@@ -866,7 +873,7 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             }
         };
         setup();
-        int32_t hout = 0, eout = NEG_E, hprev = 0, gs = 1;
+        int32_t hout = 0, eout = K::NEG_E, hprev = 0, gs = 1;
         for (int32_t T = T_first; T <= T_last; ++T) {
             if (T == next_switch) {
                 merge();
@@ -882,13 +889,13 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
             const int32_t top = s * R + h + w;  // last in-band column of the row above
             const int32_t hdiag = (s == 0 || j - 1 > top) ? 0 : hprev;
             hprev = hin;
-            if (s == 0 || j > top) { hin = 0; ein = NEG_E; }
+            if (s == 0 || j > top) { hin = 0; ein = K::NEG_E; }
             int32_t cm = 0;
             if (j >= J0 && j <= J1) {
                 const uint32_t bcol = bcol_n;
                 if (j < J1) bcol_n = (uint32_t)__ldg(B + j) * 128u;  // column j + 1
                 int32_t hu = hin, eu = ein;
-                strip_cells<R, 0, R, true>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2, alive), one);
+                strip_cells<R, 0, R, true, K>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2, alive), one);
                 hout = hu;
                 eout = eu;
                 cm = S.hc[0];
@@ -897,7 +904,13 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
                 if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
             } else {
                 hout = 0;
-                eout = NEG_E;
+                eout = K::NEG_E;
+            }
+            if constexpr (K::COMPACT) {
+                if ((T & 3) == 3) {  // at most 4 F extensions between clears (T is warp-uniform)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) S.fT[r] &= ~K::CTR;
+                }
             }
             if (__any_sync(0xffffffffu, (cm >> 16) >= gs)) {
 #pragma unroll
@@ -923,20 +936,31 @@ __device__ void align_pair_wave(const SwIn &in, const SwOut &out, int64_t p, con
         atomicAdd(fallback_count + 2, 1);  // re-run counter
         return;
     }
-    write_result(out, in, p, best, best > 0 ? (lbest & MATCH_MASK) : 0, la, la, lb);
+    write_result(out, in, p, best, best > 0 ? (lbest & K::MATCH_MASK) : 0, la, la, lb);
 }
 
 // One sorted wave pair, at the rows per strip its shape allows.
+template <class K>
+__device__ __forceinline__ void align_pair_wave_k(const SwIn &in, const SwOut &out, int64_t p, const PairGeom &g,
+                                                  const char *s_inc, int32_t *s_best, int32_t lane,
+                                                  int32_t *fallback, int32_t *fallback_count, int32_t one) {
+    switch (wave_rows_per_strip(g.la, g.w)) {
+        case 4: align_pair_wave<4, K>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
+        case 8: align_pair_wave<8, K>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
+        default: align_pair_wave<16, K>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
+    }
+}
+
+// the compact key for a pair of at most 2047 rows (unless wide_key)
 __device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &out, int64_t p,
                                                  const char *s_inc, int32_t *s_best, int32_t lane,
                                                  int32_t *fallback, int32_t *fallback_count,
-                                                 int32_t *err, int32_t one) {
+                                                 int32_t *err, int32_t one, int32_t wide_key) {
     const PairGeom g = pair_geometry(in, p, err);
-    switch (wave_rows_per_strip(g.la, g.w)) {
-        case 4: align_pair_wave<4>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
-        case 8: align_pair_wave<8>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
-        default: align_pair_wave<16>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one); break;
-    }
+    if (!wide_key && g.la <= KeyCompact::ROWS_MAX)
+        align_pair_wave_k<KeyCompact>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one);
+    else
+        align_pair_wave_k<KeyWide>(in, out, p, g, s_inc, s_best, lane, fallback, fallback_count, one);
 }
 
 // ----------------------------------------------------------------- streamed warp-per-pair
@@ -999,7 +1023,7 @@ __device__ __forceinline__ int32_t strip_te(const WaveSlot &sl, int32_t s) {
     return te > t0 ? te : t0;  // a strip whose band lies left of column 1 ends where it starts
 }
 
-template <int R>
+template <int R, class K>
 __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *order, int32_t n_wave,
                             int32_t *ticket, const char *s_inc, int32_t *s_best, WaveSlot *slots, int32_t lane,
                             int32_t *fallback, int32_t *fallback_count, int32_t *err, int32_t one) {
@@ -1017,7 +1041,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
     uint32_t bcol_n = 0;  // residue offset of its next column, loaded a step ahead
     int32_t pend_slot = -1, pend_s = 0, pend_t0 = 0;
     int32_t F = -1;
-    int32_t hout = 0, eout = NEG_E, hprev = 0;
+    int32_t hout = 0, eout = K::NEG_E, hprev = 0;
     const uint8_t *B = nullptr;
     StripRegs<R> S;
     for (;;) {
@@ -1095,7 +1119,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 S.hc[r] = 0;
-                S.fT[r] = NEG_F;
+                S.fT[r] = K::NEG_F;
                 s_best[r * 32] = 0;
                 const uint32_t code = r < alive ? (uint32_t)A[i0 + r - 1] : 0u;
                 S.arow[r] = (code * (uint32_t)N_CODES * 32u + (uint32_t)lane) * 4u;
@@ -1111,12 +1135,12 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             j = T + jb;
             const int32_t hdiag = (cur_s == 0 || j - 1 > top || j - 1 < 1) ? 0 : hprev;
             hprev = hin;
-            if (cur_s == 0 || j > top) { hin = 0; ein = NEG_E; }
+            if (cur_s == 0 || j > top) { hin = 0; ein = K::NEG_E; }
             if (j >= J0 && j <= J1) {
                 const uint32_t bcol = bcol_n;
                 if (j < J1) bcol_n = (uint32_t)__ldg(B + j) * 128u;  // column j + 1
                 int32_t hu = hin, eu = ein;
-                strip_cells<R, 0, R, true>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2s, alive), one);
+                strip_cells<R, 0, R, true, K>(bcol, hu, eu, hdiag, S, s_inc, band_rows(j - lo0, w2s, alive), one);
                 hout = hu;
                 eout = eu;
                 cm = S.hc[0];
@@ -1125,12 +1149,18 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
                 if ((R & 1) == 0) cm = max(cm, S.hc[R - 1]);
             } else {
                 hout = 0;
-                eout = NEG_E;
+                eout = K::NEG_E;
             }
         } else {
             hprev = hin;
             hout = 0;
-            eout = NEG_E;
+            eout = K::NEG_E;
+        }
+        if constexpr (K::COMPACT) {
+            if ((T & 3) == 3) {  // at most 4 F extensions between clears (T is warp-uniform)
+#pragma unroll
+                for (int r = 0; r < R; ++r) S.fT[r] &= ~K::CTR;
+            }
         }
         // ---- first-maximum trackers: per-pair running best score
         const bool trig = has && (cm >> 16) >= slots[cur_slot].gs;
@@ -1156,7 +1186,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             if (bk > 0)
                 atomicMax(&sl.acc, ((unsigned long long)(uint32_t)(bk >> 16) << 27) |
                                        ((unsigned long long)(uint32_t)(16383 - br) << 13) |
-                                       (unsigned long long)(uint32_t)(bk & MATCH_MASK));
+                                       (unsigned long long)(uint32_t)(bk & K::MATCH_MASK));
             if (cur_s == sl.S - 1) {
                 __threadfence_block();
                 const unsigned long long acc = atomicAdd(&sl.acc, 0ull);
@@ -1183,15 +1213,28 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
     }
 }
 
+template <class K>
+__device__ __forceinline__ void wave_stream_k(int32_t rows, const SwIn &in, const SwOut &out, const uint32_t *order,
+                                              int32_t n_wave, int32_t *ticket, const char *s_inc, int32_t *s_best,
+                                              WaveSlot *slots, int32_t lane, int32_t *fallback,
+                                              int32_t *fallback_count, int32_t *err, int32_t one) {
+    switch (rows) {
+        case 4: wave_stream<4, K>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
+        case 8: wave_stream<8, K>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
+        default: wave_stream<16, K>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
+    }
+}
+
 __device__ __noinline__ void wave_stream_any(int32_t rows, const SwIn &in, const SwOut &out, const uint32_t *order,
                                              int32_t n_wave, int32_t *ticket, const char *s_inc, int32_t *s_best,
                                              WaveSlot *slots, int32_t lane, int32_t *fallback,
-                                             int32_t *fallback_count, int32_t *err, int32_t one) {
-    switch (rows) {
-        case 4: wave_stream<4>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
-        case 8: wave_stream<8>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
-        default: wave_stream<16>(in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback, fallback_count, err, one); break;
-    }
+                                             int32_t *fallback_count, int32_t *err, int32_t one, int32_t compact) {
+    if (compact)
+        wave_stream_k<KeyCompact>(rows, in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback,
+                                  fallback_count, err, one);
+    else
+        wave_stream_k<KeyWide>(rows, in, out, order, n_wave, ticket, s_inc, s_best, slots, lane, fallback,
+                               fallback_count, err, one);
 }
 
 // ----------------------------------------------------------------- driver
@@ -1207,8 +1250,7 @@ static int32_t g_rows_per_strip = 0;  // 0: by band width (8 up to w = 64, else 
 // above (1); 0..3 as set (see StripVariant)
 static int32_t g_variant = -1;
 // threads of the strip kernel's CTA for 8-row strips: 512, 640 or 768; 0 =
-// by call (640, or 512 when every pair may run one warp per pair, whose code
-// would spill at 96 registers).  16-row strips run 512, taller ones 256.
+// 640.  16-row strips run 512, taller ones 256.
 static int32_t g_strip_threads = 0;
 // 1: the wide key for every pair of the strip kernel (measurement); 0
 // (default): the compact key for pairs of at most 2047 rows
@@ -1299,12 +1341,10 @@ int32_t sw_set_wide_key(int32_t v) {
 int32_t sw_wide_key() { return g_wide_key; }
 
 // threads of the strip kernel's CTA (one per SM) for strips of `rows` rows
-// in a call of M pairs
-static int32_t strip_threads(int32_t rows, int64_t M) {
+static int32_t strip_threads(int32_t rows) {
     if (rows >= 24) return 256;
     if (rows == 16) return 512;
-    if (g_strip_threads) return g_strip_threads;
-    return M <= (int64_t)g_wave_all_below ? 512 : 640;
+    return g_strip_threads ? g_strip_threads : 640;
 }
 
 template <int R, int V, int NT>
@@ -1418,8 +1458,19 @@ int32_t sw_batched_launch(const SwIn &in, const SwOut &out, int64_t M, const int
         const uint32_t *order = dv.Current();
         // narrow bands: a strip's ramps (R - 1 masked columns at each end) weigh
         // against 2w + 1 interior columns, so fewer rows per strip win there
-        const int32_t rows = g_rows_per_strip ? g_rows_per_strip : (wmax <= 64 ? 8 : 16);
-        const int32_t nt = strip_threads(rows, M);
+        int32_t rows = g_rows_per_strip ? g_rows_per_strip : (wmax <= 64 ? 8 : 16);
+        // A call that routes every pair one warp per pair (at most
+        // CK_CFG_WAVE_ALL_BELOW pairs, a band narrow enough for every pair to
+        // rotate) never runs lane-per-pair strips: the 8-row kernel's larger
+        // CTA gives its warp-per-pair phase 20 warps per SM instead of 16
+        // (search-shaped calls of 8 k and 32 k pairs: 9-18 % faster), unless
+        // the call has no more pairs than 16 warps per SM -- one pair per warp,
+        // where the 512-thread CTA's unspilled code is the faster.
+        const bool wave_only = !g_rows_per_strip && M <= (int64_t)g_wave_all_below && in.band_width >= 1 &&
+                               2 * in.band_width < 31 * 16 + 32;
+        if (wave_only) rows = 8;
+        int32_t nt = strip_threads(rows);
+        if (wave_only && !g_strip_threads && M <= 16 * (int64_t)sm_count()) nt = 512;
         wave_split_kernel<<<1, 32, 0, st>>>(dk.Current(), cnt, in.band_width, g_wave_all_below,
                                             g_wave_min_rows, g_wave_adaptive, (int64_t)sm_count() * nt);
         CK_CUDA(cudaGetLastError());

@@ -205,10 +205,10 @@ int32_t ck_sw_last_kernel_ms(float *out_ms);
  *   CK_CFG_STRIP_THREADS   threads of the strip kernel's one persistent CTA
  *                          per SM for strips of 8 rows: 512 (16 warps, up to
  *                          128 registers), 640 (20 warps, 96) or 768 (24, 80);
- *                          0 (default): 640, or 512 in calls with at most
- *                          CK_CFG_WAVE_ALL_BELOW pairs (the warp-per-pair code
- *                          spills at 96 registers).  Strips of 16 rows always
- *                          run 512 threads, of 24 or 32 rows 256.  (Key 8,
+ *                          0 (default): 640.  Strips of 16 rows always run
+ *                          512 threads, of 24 or 32 rows 256.  With the
+ *                          default rows per strip, a call whose pairs all run
+ *                          one warp per pair runs the 8-row kernel.  (Key 8,
  *                          CTAs of 256 threads per SM, is retired: one CTA of
  *                          512 threads measured at least as fast in every case.)
  *   CK_CFG_STRIP_KEY       0 (default): the strip kernel packs pairs of at

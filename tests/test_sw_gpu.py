@@ -158,6 +158,32 @@ def test_strip_key_forms_agree(ck, rows, variant, bw):
             set_config(k, v)
 
 
+@pytest.mark.parametrize("stream", [0, 2])
+@pytest.mark.parametrize("bw", [3, 40, 200])
+@pytest.mark.parametrize("fit", ["all_compact", "mixed"])
+def test_wave_key_forms_agree(ck, stream, bw, fit):
+    """Every pair one warp per pair, in both key forms: one pair per warp
+    picks the form per pair, the streamed schedule per call (compact only
+    when every pair has at most 2047 rows, as in the first set)."""
+    from clustkit_gb300._lib import CFG_STRIP_KEY, get_config, set_config
+    flat, offsets, lengths, pairs = _key_form_set(bw + stream)
+    sh = np.minimum(lengths[pairs[:, 0]], lengths[pairs[:, 1]])
+    if fit == "all_compact":
+        pairs = pairs[sh <= 2047]
+    ref = oracle.sw_batch(pairs, flat, offsets, lengths, bw, BLOSUM62)
+    keep = get_config(CFG_STRIP_KEY)
+    try:
+        with wave_config(all_below=1 << 30, min_rows=0, stream=stream):
+            for wide in (0, 1):
+                set_config(CFG_STRIP_KEY, wide)
+                r = batch_sw(pairs, flat, offsets, lengths, bw, BLOSUM62)
+                _same(r, ref)
+                c = ck.sw_counters()
+                assert c["wave"] == c["batched"] > 0
+    finally:
+        set_config(CFG_STRIP_KEY, keep)
+
+
 def test_strip_key_setting_rejects_other_values(ck):
     from clustkit_gb300._lib import CFG_STRIP_KEY, get_config, set_config
     assert get_config(CFG_STRIP_KEY) == 0
