@@ -980,7 +980,10 @@ __device__ __noinline__ void align_pair_wave_any(const SwIn &in, const SwOut &ou
 // below), so a lane never reads a neighbour's unrelated values.
 //
 // Per pair, a slot in shared memory holds its geometry, the running best
-// score (first-maximum trigger) and the best cell as one packed 64-bit value
+// score (first-maximum trigger; each lane compares with its own copy, taken
+// when its strip starts and refreshed when it triggers, which is never above
+// the slot's, so a copy that lags only adds trigger steps) and the best cell
+// as one packed 64-bit value
 // (score, then lower row, then match count), merged by atomicMax at each
 // strip's end; the pair's last strip ends last and writes the result.
 constexpr int WS_SLOTS = 16;
@@ -1042,6 +1045,9 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
     int32_t pend_slot = -1, pend_s = 0, pend_t0 = 0;
     int32_t F = -1;
     int32_t hout = 0, eout = K::NEG_E, hprev = 0;
+    // the held strip's pair's running best score as last seen by this lane: at
+    // most the slot's, so its trigger fires at least whenever the slot's would
+    int32_t gs_l = 1;
     const uint8_t *B = nullptr;
     StripRegs<R> S;
     for (;;) {
@@ -1107,6 +1113,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             cur_slot = pend_slot;
             cur_s = pend_s;
             pend_slot = -1;
+            gs_l = sl.gs;
             strip_bounds<R>(sl, cur_s, i0, lo0, J0, J1, alive);
             te = strip_te<R>(sl, cur_s);
             if (te < T) te = T;  // only after a late start: the strip still ends
@@ -1163,7 +1170,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
             }
         }
         // ---- first-maximum trackers: per-pair running best score
-        const bool trig = has && (cm >> 16) >= slots[cur_slot].gs;
+        const bool trig = has && (cm >> 16) >= gs_l;
         if (__any_sync(FULL, trig)) {
             if (has) {
 #pragma unroll
@@ -1171,7 +1178,7 @@ __device__ void wave_stream(const SwIn &in, const SwOut &out, const uint32_t *or
                     const int32_t b = s_best[r * 32];
                     if (S.hc[r] > (b | (KU - 1))) s_best[r * 32] = S.hc[r];
                 }
-                if (cm > 0) atomicMax(&slots[cur_slot].gs, cm >> 16);
+                if (cm > 0) gs_l = max(atomicMax(&slots[cur_slot].gs, cm >> 16), cm >> 16);
             }
         }
         // ---- strip end: merge its rows into the pair's best; the last strip writes
