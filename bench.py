@@ -52,7 +52,7 @@ OPS_PER_CELL = 6  # max-plus lane ops of the score recurrence: E, F: viaddmax+ad
 # cell of that launch; a run reports it scaled to its own cells and says so
 STRIP_PROFILE = "profiles/sw_strip_kernel_align50k.md"
 STRIP_PROFILE_CELLS = 46_229_358_568
-STRIP_DRAM_BYTES_PER_CELL = (24.657645e9 + 27.322653e9) / STRIP_PROFILE_CELLS
+STRIP_DRAM_BYTES_PER_CELL = (25.128211e9 + 27.463094e9) / STRIP_PROFILE_CELLS
 
 
 def log(*a):
