@@ -7,12 +7,13 @@
 //     (rows > 8191, residue codes > 20) go to a fallback list.
 //  2. sort: pairs are ordered by descending (rows, columns), so a warp's 32
 //     pairs have near-identical shapes and the longest work is issued first.
-//  3. strip kernel: persistent CTAs; each warp takes the next 32 sorted pairs
-//     from a global ticket counter and every lane aligns one pair.  A lane
-//     sweeps its pair in strips of R rows: the strip's R rows live in
-//     registers and advance one column at a time, so per column only the
-//     row above the strip is read from (and the strip's last row written to)
-//     a per-lane circular window in global scratch.
+//  3. strip kernel: one persistent CTA per SM (512 threads for 16-row strips,
+//     640 for 8-row ones); each warp takes the next 32 sorted pairs from a
+//     global ticket counter and every lane aligns one pair.  A lane sweeps
+//     its pair in strips of R rows: the strip's R rows live in registers and
+//     advance one column at a time, so per column only the row above the
+//     strip is read from (and the strip's last row written to) a per-lane
+//     circular window in global scratch.
 //  4. the plain kernel runs the fallback list, plus any pair whose score
 //     reached the packed lane's limit (re-run exactly in plain int32).
 //
@@ -22,15 +23,19 @@
 // E 1, F 0) and a tie bit (gap extension 1, gap opening 0).  Signed integer
 // max over keys then orders candidates exactly as clustkit's comparisons do
 // (score first, then H's 0 > diag > E > F priority, then E/F's preference for
-// extension on ties) and carries the match count of the winner for free.  The
-// BLOSUM62 increment of a cell is a table of keys: s(a,b) * 2^16 + 2 * 2^14 +
-// (a == b), looked up in shared memory, replicated per lane so that the 32
-// lanes of a warp always hit 32 different banks.  Per cell:
+// extension on ties) and carries the match count of the winner for free.
+// Pairs of at most 2047 rows use a compact form of the key (KeyCompact below:
+// an 11-bit match count and a gap-extension counter in place of the tie bit),
+// which needs fewer logic ops a cell.  The BLOSUM62 increment of a cell is a
+// table of keys: s(a,b) * 2^16 + 2 * 2^14 + (a == b), looked up in shared
+// memory, replicated per lane so that the 32 lanes of a warp always hit 32
+// different banks.  Per cell:
 //     diag = max(Hdiag + inc, ZERO)          (__viaddmax_s32)
 //     E    = max(E_up - 2^16, H_up + OPEN_E) (__viaddmax_s32)
 //     F    = max(F_left - 2^16, H_left + OPEN_F)
 //     H    = max(diag, E, F)                 (__vimax3_s32)
-// and H's priority/tie bits are cleared before it feeds other cells.
+// and H's priority/tie bits (or counter) are cleared before it feeds other
+// cells.
 // The first row-major cell holding the best score is tracked per row (strict
 // '>' along the row) and the rows are merged in row order after each strip;
 // a warp vote once per group of interior columns decides whether any lane's
@@ -615,6 +620,9 @@ __device__ __forceinline__ void align_pair_strips_k(const SwIn &in, const SwOut 
     const int32_t wmask = W - 1;
     const int32_t w2 = 2 * w;
 
+    // every slot reads as the boundary (H = 0, E = -inf) before the first strip;
+    // writing the whole window, not only the first strip's columns, measured
+    // faster (its lines are then in place for the strips that follow)
     for (int32_t s = 0; s < W; ++s) win[(size_t)s * 32] = make_int2(0, K::NEG_E);
 
     int32_t gbest = 0;

@@ -3,7 +3,11 @@
 strip_column): for random pair geometries, band widths, hints, strip heights
 and every variant, each band column of each strip is visited exactly once in
 order, the prefetch queue always holds the next columns, every window slot
-index stays below W and every residue read lies inside the sequence.  The
+index stays below W, every residue read lies inside the sequence, and every
+window entry a strip reads (its columns and its first row's diagonal input)
+holds that column's value: for the first strip that runs, the boundary the pair
+starts with; after it, a value the previous strip wrote or the boundary it
+filled past its end.  The
 kernel's own results are checked against the oracle on the GPU; this pins the
 index arithmetic, which a GPU run can only show by faulting."""
 import random
@@ -13,6 +17,8 @@ import pytest
 
 def _strip_loop(la, lb, w, h, R, U, P, aligned, W):
     wmask = W - 1
+    held = dict.fromkeys(range(W), "boundary")  # window slot -> whose entry it holds
+    fresh = True
     i0 = 1
     while i0 <= la:
         lo0 = i0 + h - w
@@ -22,6 +28,11 @@ def _strip_loop(la, lb, w, h, R, U, P, aligned, W):
         if J1 < J0:
             i0 += R
             continue
+        for c in range(J0 - 1 if J0 >= 2 else J0, J1 + 1):  # every entry the strip reads
+            # the first strip that runs reads the pair's initial boundary (its row
+            # above is row 0 or lies left of column 1); later ones what was written
+            assert held[c & wmask] == ("boundary" if fresh else c), (c, J0, J1)
+        fresh = False
         queue = [J0 + k for k in range(P)]
         for k in range(P):  # strip start: residues of J0 .. J0+P-1, clamped
             assert 0 <= min(J0 + k, lb) - 1 <= lb - 1
@@ -54,6 +65,10 @@ def _strip_loop(la, lb, w, h, R, U, P, aligned, W):
                 seen.append(j)
                 j += 1
         assert seen == list(range(J0, J1 + 1))
+        for c in seen:  # the strip's last row, then the boundary past its end
+            held[c & wmask] = c
+        for c in range(J1 + 1, min(J1 + R, lb) + 1):
+            held[c & wmask] = c
         i0 += R
 
 
