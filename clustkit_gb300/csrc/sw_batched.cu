@@ -343,33 +343,39 @@ __device__ __forceinline__ void strip_cells(uint32_t bcol, int32_t &hu, int32_t 
     using namespace key;
 #pragma unroll
     for (int r = RB; r < RE; ++r) {
-        // Ramp and clipped columns skip rows outside their band (bit r of
-        // rmask clear): a row that has not reached its band keeps H = 0,
-        // F = -inf; a row that has left it hands the out-of-band boundary
-        // (H = 0, E = -inf) to the row below and its last H as that row's
-        // diagonal input.
-        if (!MASKED || ((rmask >> r) & 1u)) {
-            const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
-            const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
-            // E's extension term comes from E of the row above, known before
-            // that row's H: only H_up + OPEN_E and the max-of-three sit on the
-            // row-to-row dependency chain.  E's tie bit plays no part in H
-            // (E, F, diag and zero differ in priority), so it is set off the chain.
-            const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, K::EXT, one));
-            int32_t fTn = __viaddmax_s32(S.fT[r], K::EXT, fadd(S.hc[r], OPEN_F, one));
-            if constexpr (!K::COMPACT) fTn |= TBIT;
-            const int32_t hn = __vimax3_s32(diagc, eR, fTn) & K::CLEAN;
-            hdiag = S.hc[r];
+        const int32_t inc = *(const int32_t *)(s_inc + fadd((int32_t)S.arow[r], (int32_t)bcol, one));
+        const int32_t diagc = __viaddmax_s32(hdiag, inc, ZKEY);
+        // E's extension term comes from E of the row above, known before that
+        // row's H: only H_up + OPEN_E and the max-of-three sit on the
+        // row-to-row dependency chain.  E's tie mark plays no part in H (E, F,
+        // diag and zero differ in priority), so it is set off the chain.
+        const int32_t eR = __viaddmax_s32(hu, OPEN_E, fadd(eu, K::EXT, one));
+        int32_t fTn = __viaddmax_s32(S.fT[r], K::EXT, fadd(S.hc[r], OPEN_F, one));
+        if constexpr (!K::COMPACT) fTn |= TBIT;
+        const int32_t hn = __vimax3_s32(diagc, eR, fTn) & K::CLEAN;
+        int32_t en;
+        if constexpr (K::COMPACT) en = (r % 6 == 5 || r == R - 1) ? (eR & ~K::CTR) : eR;
+        else en = eR | TBIT;
+        hdiag = S.hc[r];
+        if constexpr (MASKED) {
+            // A row outside its band at this column (bit r of rmask clear) is
+            // computed like the others and its results dropped by selects (no
+            // branch: the lanes of a warp are at different columns of their
+            // strips): a row that has not reached its band keeps H = 0 and its
+            // F; a row that has left it hands the out-of-band boundary (H = 0,
+            // E = -inf) to the row below and its last H as that row's diagonal
+            // input (hdiag above, as for a row inside its band).
+            const bool inb = (rmask >> r) & 1u;
+            const int32_t hs = inb ? hn : 0;
+            S.hc[r] = hs;
+            S.fT[r] = inb ? fTn : S.fT[r];
+            hu = hs;
+            eu = inb ? en : K::NEG_E;
+        } else {
             S.hc[r] = hn;
             S.fT[r] = fTn;
             hu = hn;
-            if constexpr (K::COMPACT) eu = (r % 6 == 5 || r == R - 1) ? (eR & ~K::CTR) : eR;
-            else eu = eR | TBIT;
-        } else {
-            hdiag = S.hc[r];
-            S.hc[r] = 0;
-            hu = 0;
-            eu = K::NEG_E;
+            eu = en;
         }
     }
 }
