@@ -88,6 +88,36 @@ def test_no_cpu_fallback_without_gpu():
                  np.array([2, 2], np.int32))
 
 
+def test_config_keys_validate_and_round_trip():
+    """The batched engine's settings (host-only setters, no GPU needed): each
+    key takes its documented values and reads them back, rejects others
+    without changing the setting, and the retired CTAs-per-SM key 8 is gone."""
+    from clustkit_gb300 import _lib
+    cases = {
+        _lib.CFG_ROWS_PER_STRIP: ([0, 8, 16, 24, 32], [4, 12, -1]),
+        _lib.CFG_STRIP_VARIANT: ([-1, 0, 1, 2, 3], [4, -2]),
+        _lib.CFG_STRIP_THREADS: ([0, 512, 640, 768], [256, 576, 1024, -1]),
+        _lib.CFG_STRIP_KEY: ([0, 1], [2, -1]),
+        _lib.CFG_WAVE_ROWS: ([0, 4, 8, 16], [2, 32]),
+    }
+    for key, (good, bad) in cases.items():
+        keep = _lib.get_config(key)
+        try:
+            for v in good:
+                _lib.set_config(key, v)
+                assert _lib.get_config(key) == v
+            for v in bad:
+                with pytest.raises(_lib.CkError):
+                    _lib.set_config(key, v)
+                assert _lib.get_config(key) == good[-1]
+        finally:
+            _lib.set_config(key, keep)
+    with pytest.raises(_lib.CkError):
+        _lib.set_config(8, 2)
+    with pytest.raises(_lib.CkError):
+        _lib.get_config(8)
+
+
 def test_band_cells_closed_form():
     from clustkit_gb300.cells import band_cells, band_cells_loop
     rng = np.random.default_rng(0)
