@@ -184,6 +184,47 @@ def test_wave_key_forms_agree(ck, stream, bw, fit):
         set_config(CFG_STRIP_KEY, keep)
 
 
+@pytest.mark.parametrize("route", ["strip", "wave_stream", "wave_per_pair"])
+def test_key_boundary_rows(ck, route):
+    """Pairs at the compact key's edge: self-alignments of 2,046-2,049
+    residues (a 2,047-residue self-alignment has 2,047 matches, the most the
+    11-bit count holds; 2,048 rows take the wide key), mutated copies, and
+    tryptophan-rich sequences whose scores approach the 16-bit limit, in one
+    call, on each route and under both key settings."""
+    from clustkit_gb300._lib import CFG_STRIP_KEY, get_config, set_config
+    rng = np.random.default_rng(2047)
+    seqs = []
+    for L in (2046, 2047, 2048, 2049):
+        base = rng.integers(0, 20, L).astype(np.uint8)
+        mut = base.copy()
+        idx = rng.choice(L, L // 10, replace=False)
+        mut[idx] = rng.integers(0, 20, idx.size).astype(np.uint8)
+        trp = np.where(rng.random(L) < 0.7, 18, rng.integers(0, 20, L)).astype(np.uint8)  # W is code 18
+        seqs += [base, mut, trp]
+    lengths = np.array([x.size for x in seqs], dtype=np.int32)
+    offsets = np.zeros(lengths.size, dtype=np.int64)
+    offsets[1:] = np.cumsum(lengths[:-1])
+    flat = np.concatenate(seqs)
+    n = lengths.size
+    pairs = np.array([(i, i) for i in range(n)] + [(3 * k, 3 * k + 1) for k in range(4)] +
+                     [(3 * k + 2, 3 * k + 2) for k in range(4)] +
+                     [(i, j) for i in range(0, n, 2) for j in range(1, n, 3)], dtype=np.int32)
+    keep = get_config(CFG_STRIP_KEY)
+    routes = {"strip": dict(all_below=0, min_rows=1 << 30),
+              "wave_stream": dict(all_below=1 << 30, min_rows=0, stream=2),
+              "wave_per_pair": dict(all_below=1 << 30, min_rows=0, stream=0)}
+    try:
+        for bw in (50, 200):
+            ref = oracle.sw_batch(pairs, flat, offsets, lengths, bw, BLOSUM62)
+            assert ref["matches"].max() == 2049  # the longest self-alignment
+            with wave_config(**routes[route]):
+                for wide in (0, 1):
+                    set_config(CFG_STRIP_KEY, wide)
+                    _same(batch_sw(pairs, flat, offsets, lengths, bw, BLOSUM62), ref)
+    finally:
+        set_config(CFG_STRIP_KEY, keep)
+
+
 def test_strip_key_setting_rejects_other_values(ck):
     from clustkit_gb300._lib import CFG_STRIP_KEY, get_config, set_config
     assert get_config(CFG_STRIP_KEY) == 0
