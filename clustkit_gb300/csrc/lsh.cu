@@ -15,8 +15,13 @@
 // put first, and this keeps the 1000 lowest ids.
 //
 // Layout: sketches are transposed once to [s][N] so a table's band columns are
-// read coalesced.  Two passes over the tables -- count, then emit -- size the
-// raw pair buffer exactly; one radix sort + unique de-duplicates all tables.
+// read coalesced.  Tables are processed in batches (as many as fit a few GB of
+// scratch; every table at once for moderate N): a batch's bucket ids are keyed
+// (table, id) and sorted together, stably, so each bucket is one run in table
+// order with its members in ascending sequence id, and the run-length, scan,
+// pair-count and emit steps cover the whole batch in one launch each.  Two
+// passes over the batches -- count, then emit -- size the raw pair buffer
+// exactly; one radix sort + unique de-duplicates all tables.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_run_length_encode.cuh>
 #include <cub/device/device_scan.cuh>
@@ -52,17 +57,42 @@ __global__ void transpose_sketch_kernel(const uint64_t *__restrict__ sk, int64_t
     }
 }
 
+// A batch's sort key: the table (within the batch) above the bucket id.
+struct LshKey {
+    uint64_t h;  // bucket id in its table
+    uint32_t t;  // table, counted from the batch's first
+    uint32_t pad;
+};
+__host__ __device__ inline bool operator==(const LshKey &a, const LshKey &b) { return a.h == b.h && a.t == b.t; }
+// radix-sort view of a key: (table, bucket id), most significant first
+struct LshKeyParts {
+    __host__ __device__ ::cuda::std::tuple<uint32_t &, uint64_t &> operator()(LshKey &k) const { return {k.t, k.h}; }
+};
+
+// bucket ids of tables t0 .. t0 + tb - 1 for every sequence, table-major
 __global__ void lsh_hash_kernel(const uint64_t *__restrict__ skT, int64_t n, const int32_t *__restrict__ band,
-                                int32_t nb, uint64_t seed, uint64_t *__restrict__ keys,
-                                int32_t *__restrict__ vals) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        uint64_t h = seed;
-        for (int32_t b = 0; b < nb; ++b) h = h * LSH_MUL + skT[(int64_t)band[b] * n + i];
+                                int32_t nb, const uint64_t *__restrict__ seeds, int32_t t0, int32_t tb,
+                                LshKey *__restrict__ keys, int32_t *__restrict__ vals) {
+    const int64_t total = (int64_t)tb * n;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t tl = (int32_t)(k / n);
+        const int64_t i = k - (int64_t)tl * n;
+        const int32_t t = t0 + tl;
+        const int32_t *bt = band + (int64_t)t * nb;
+        uint64_t h = seeds[t];
+        for (int32_t b = 0; b < nb; ++b) h = h * LSH_MUL + skT[(int64_t)bt[b] * n + i];
         h = (h ^ (h >> 33)) * LSH_FMIX;
         h ^= h >> 33;
-        keys[i] = h;
-        vals[i] = (int32_t)i;
+        keys[k] = LshKey{h, (uint32_t)tl, 0u};
+        vals[k] = (int32_t)i;
     }
+}
+
+// the batch's pair total, pair_off[runs], for the host
+__global__ void lsh_total_kernel(const int32_t *__restrict__ n_runs, const int64_t *__restrict__ pair_off,
+                                 int64_t *__restrict__ total) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *total = pair_off[*n_runs];
 }
 
 // pairs a bucket of `count` members contributes (first 1000 only)
@@ -127,87 +157,105 @@ static int32_t lsh_impl(void *pv) {
     cudaStream_t st = a.st;
     *a.out_count = 0;
     if (n < 2 || a.tables == 0) return CK_OK;
-    // band indices on the device
-    int32_t *d_band = (int32_t *)scratch(SLOT_SEARCH_TMP0, (size_t)a.tables * a.bands * 4, &status);
+    // tables per batch: about 4 GB of keys, values and run data (80 B an item),
+    // and fewer than 2^31 items (the run-length encoder counts in int)
+    int64_t tb64 = ((int64_t)4 << 30) / (80 * n);
+    if (tb64 * n > ((int64_t)1 << 30)) tb64 = ((int64_t)1 << 30) / n;
+    if (tb64 < 1) tb64 = 1;
+    if (tb64 > a.tables) tb64 = a.tables;
+    const int32_t TB = (int32_t)tb64;
+    const int64_t items = (int64_t)TB * n;
+    int tbits = 1;  // bits of a table index within a batch
+    while (tbits < 31 && ((int64_t)1 << tbits) < TB) ++tbits;
+    // band indices and seeds on the device
+    int32_t *d_band = (int32_t *)scratch(SLOT_SEARCH_TMP0, (size_t)a.tables * a.bands * 4 + (size_t)a.tables * 8 + 16,
+                                         &status);
     uint64_t *skT = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)n * a.s * 8, &status);
-    uint64_t *k0 = (uint64_t *)scratch(SLOT_SEARCH_TMP2, (size_t)n * 8 * 2, &status);
-    int32_t *v0 = (int32_t *)scratch(SLOT_SEARCH_TMP3, (size_t)n * 4 * 2, &status);
-    // run-length outputs: unique keys (discarded), counts, run count, starts, pair offsets
-    char *rle = (char *)scratch(SLOT_SEARCH_TMP4, (size_t)n * (8 + 4 + 4 + 8) + 64, &status);
-    if (!d_band || !skT || !k0 || !v0 || !rle) return status;
-    uint64_t *k1 = k0 + n;
-    int32_t *v1 = v0 + n;
-    uint64_t *uniq = (uint64_t *)rle;
-    int32_t *counts = (int32_t *)(uniq + n);
-    int32_t *starts = counts + n;
-    int64_t *pair_off = (int64_t *)(starts + n);  // n + 1 entries: 8-byte aligned (n*16 bytes before)
+    LshKey *k0 = (LshKey *)scratch(SLOT_SEARCH_TMP2, (size_t)items * sizeof(LshKey) * 2, &status);
+    int32_t *v0 = (int32_t *)scratch(SLOT_SEARCH_TMP3, (size_t)items * 4 * 2, &status);
+    // run data: unique keys (unused), counts, starts (int32), pair offsets (int64, items + 1)
+    char *rle = (char *)scratch(SLOT_SEARCH_TMP4, (size_t)items * (sizeof(LshKey) + 4 + 4 + 8) + 64, &status);
     int32_t *n_runs = (int32_t *)scratch(SLOT_MAXLEN, 64, &status);
-    if (!n_runs) return status;
+    if (!d_band || !skT || !k0 || !v0 || !rle || !n_runs) return status;
+    uint64_t *d_seeds = (uint64_t *)(((uintptr_t)(d_band + (size_t)a.tables * a.bands) + 15) & ~(uintptr_t)15);
+    LshKey *k1 = k0 + items;
+    int32_t *v1 = v0 + items;
+    LshKey *uniq = (LshKey *)rle;
+    int32_t *counts = (int32_t *)(uniq + items);
+    int32_t *starts = counts + items;
+    int64_t *pair_off = (int64_t *)(starts + items);  // 8-byte aligned: items * 24 bytes before
+    int64_t *d_total = (int64_t *)(n_runs + 4);
     CK_CUDA(cudaMemcpyAsync(d_band, a.band_idx_host, (size_t)a.tables * a.bands * 4, cudaMemcpyHostToDevice, st));
+    CK_CUDA(cudaMemcpyAsync(d_seeds, a.seeds_host, (size_t)a.tables * 8, cudaMemcpyHostToDevice, st));
     {
         dim3 grid((unsigned)((n + 31) / 32), (unsigned)((a.s + 31) / 32));
         transpose_sketch_kernel<<<grid, dim3(32, 8), 0, st>>>(a.sk, n, a.s, skT);
         CK_CUDA(cudaGetLastError());
     }
-    // temp storage sizes (the largest of the calls below)
+    // temp storage sizes (the largest of the calls below, at a full batch)
     size_t t_sort = 0, t_rle = 0, t_scan = 0, t_scan2 = 0;
     {
-        cub::DoubleBuffer<uint64_t> dk(k0, k1);
+        cub::DoubleBuffer<LshKey> dk(k0, k1);
         cub::DoubleBuffer<int32_t> dv(v0, v1);
-        CK_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, t_sort, dk, dv, (int)n, 0, 64, st));
-        CK_CUDA(cub::DeviceRunLengthEncode::Encode(nullptr, t_rle, k0, uniq, counts, n_runs, (int)n, st));
-        CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan, counts, starts, (int)n, st));
-        CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan2, pair_off, pair_off, (int)n + 1, st));
+        CK_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, t_sort, dk, dv, items, LshKeyParts{}, 0, 64 + tbits, st));
+        CK_CUDA(cub::DeviceRunLengthEncode::Encode(nullptr, t_rle, k0, uniq, counts,
+                                                   n_runs, (int)items, st));
+        CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan, counts, starts, (int)items, st));
+        CK_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan2, pair_off, pair_off, (int)items + 1, st));
     }
     const size_t t_max = std::max(std::max(t_sort, t_rle), std::max(t_scan, t_scan2));
     void *tmp = scratch(SLOT_SORT_TEMP, t_max, &status);
     if (!tmp) return status;
 
-    // one table: bucket ids, stable sort, runs, pair offsets; returns the pair total
-    auto table = [&](int32_t t, cub::DoubleBuffer<uint64_t> &dk, cub::DoubleBuffer<int32_t> &dv,
+    // one batch: bucket ids, stable sort, runs, pair offsets; *total its pair count
+    auto batch = [&](int32_t t0, int32_t tb, cub::DoubleBuffer<LshKey> &dk, cub::DoubleBuffer<int32_t> &dv,
                      int64_t *total) -> int32_t {
-        lsh_hash_kernel<<<grid_of(n, 256), 256, 0, st>>>(skT, n, d_band + (size_t)t * a.bands, a.bands,
-                                                         a.seeds_host[t], dk.Current(), dv.Current());
+        const int64_t m = (int64_t)tb * n;
+        lsh_hash_kernel<<<grid_of(m, 256), 256, 0, st>>>(skT, n, d_band, a.bands, d_seeds, t0, tb, dk.Current(),
+                                                         dv.Current());
         CK_CUDA(cudaGetLastError());
-        size_t tb = t_max;
-        CK_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, dk, dv, (int)n, 0, 64, st));
-        tb = t_max;
-        CK_CUDA(cub::DeviceRunLengthEncode::Encode(tmp, tb, dk.Current(), uniq, counts, n_runs, (int)n, st));
-        tb = t_max;
-        CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, counts, starts, (int)n, st));
-        lsh_bucket_pairs_kernel<<<grid_of(n + 1, 256), 256, 0, st>>>(counts, n_runs, n, pair_off);
+        size_t tbytes = t_max;
+        CK_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tbytes, dk, dv, m, LshKeyParts{}, 0, 64 + tbits, st));
+        tbytes = t_max;
+        CK_CUDA(cub::DeviceRunLengthEncode::Encode(tmp, tbytes, dk.Current(), uniq, counts,
+                                                   n_runs, (int)m, st));
+        tbytes = t_max;
+        CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tbytes, counts, starts, (int)m, st));
+        lsh_bucket_pairs_kernel<<<grid_of(m + 1, 256), 256, 0, st>>>(counts, n_runs, m, pair_off);
         CK_CUDA(cudaGetLastError());
-        tb = t_max;
-        CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tb, pair_off, pair_off, (int)n + 1, st));
-        // pair_off[R] (R = runs) is the table's total; runs <= n, entries past R are 0
-        int32_t R = 0;
-        CK_CUDA(cudaMemcpyAsync(&R, n_runs, 4, cudaMemcpyDeviceToHost, st));
-        CK_CUDA(cudaStreamSynchronize(st));
-        CK_CUDA(cudaMemcpyAsync(total, pair_off + R, 8, cudaMemcpyDeviceToHost, st));
+        tbytes = t_max;
+        CK_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tbytes, pair_off, pair_off, (int)m + 1, st));
+        // pair_off[R] (R = runs) is the batch's total; runs <= m, entries past R are 0
+        lsh_total_kernel<<<1, 32, 0, st>>>(n_runs, pair_off, d_total);
+        CK_CUDA(cudaGetLastError());
+        CK_CUDA(cudaMemcpyAsync(total, d_total, 8, cudaMemcpyDeviceToHost, st));
         CK_CUDA(cudaStreamSynchronize(st));
         return CK_OK;
     };
 
-    // pass 1: count every table's pairs
-    std::vector<int64_t> per_table((size_t)a.tables, 0);
+    // pass 1: count every batch's pairs
+    const int32_t n_batches = (a.tables + TB - 1) / TB;
+    std::vector<int64_t> per_batch((size_t)n_batches, 0);
     int64_t raw = 0;
-    for (int32_t t = 0; t < a.tables; ++t) {
-        cub::DoubleBuffer<uint64_t> dk(k0, k1);
+    for (int32_t b = 0; b < n_batches; ++b) {
+        const int32_t t0 = b * TB, tb = a.tables - t0 < TB ? a.tables - t0 : TB;
+        cub::DoubleBuffer<LshKey> dk(k0, k1);
         cub::DoubleBuffer<int32_t> dv(v0, v1);
-        CK_TRY(table(t, dk, dv, &per_table[t]));
-        raw += per_table[t];
+        CK_TRY(batch(t0, tb, dk, dv, &per_batch[b]));
+        raw += per_batch[b];
     }
     if (raw == 0) return CK_OK;
     // pass 2: emit into one raw buffer (double, for the de-duplicating sort)
     uint64_t *rk = (uint64_t *)scratch(SLOT_FALLBACK, (size_t)raw * 8 * 2, &status);
     if (!rk) return status;
     int64_t at = 0;
-    for (int32_t t = 0; t < a.tables; ++t) {
-        if (per_table[t] == 0) continue;
-        cub::DoubleBuffer<uint64_t> dk(k0, k1);
+    for (int32_t b = 0; b < n_batches; ++b) {
+        if (per_batch[b] == 0) continue;
+        const int32_t t0 = b * TB, tb = a.tables - t0 < TB ? a.tables - t0 : TB;
+        cub::DoubleBuffer<LshKey> dk(k0, k1);
         cub::DoubleBuffer<int32_t> dv(v0, v1);
         int64_t tot = 0;
-        CK_TRY(table(t, dk, dv, &tot));
+        CK_TRY(batch(t0, tb, dk, dv, &tot));
         lsh_emit_kernel<<<grid_of(tot, 256), 256, 0, st>>>(dv.Current(), starts, pair_off, n_runs, tot, n,
                                                            rk + at);
         CK_CUDA(cudaGetLastError());
