@@ -106,26 +106,57 @@ __global__ void lsh_bucket_pairs_kernel(const int32_t *__restrict__ counts, cons
     }
 }
 
-// one thread per output pair: find its bucket (binary search over the pair
-// offsets), decode its (x < y) member positions from the triangular index
-__global__ void lsh_emit_kernel(const int32_t *__restrict__ order, const int32_t *__restrict__ run_start,
-                                const int64_t *__restrict__ pair_off, const int32_t *__restrict__ n_runs,
-                                int64_t total, int64_t n, uint64_t *__restrict__ out) {
+// Emission by bucket: a thread writes the pairs of a bucket of at most 32
+// members (pair (x, y), x < y, at offset y(y - 1) / 2 + x of the bucket's
+// range), and lists larger buckets for lsh_emit_big_kernel.  The raw pairs
+// are sorted and de-duplicated afterwards, so only the set matters.
+constexpr int32_t LSH_SMALL_BUCKET = 32;
+__global__ void lsh_emit_runs_kernel(const int32_t *__restrict__ order, const int32_t *__restrict__ run_start,
+                                     const int32_t *__restrict__ counts, const int64_t *__restrict__ pair_off,
+                                     const int32_t *__restrict__ n_runs, int64_t n, uint64_t *__restrict__ out,
+                                     int32_t *__restrict__ big, int32_t *__restrict__ n_big) {
     const int32_t R = *n_runs;
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        int32_t lo = 0, hi = R - 1;  // last run with pair_off <= k
-        while (lo < hi) {
-            const int32_t mid = (lo + hi + 1) >> 1;
-            if (pair_off[mid] <= k) lo = mid; else hi = mid - 1;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < R; r += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = counts[r] < LSH_MAX_BUCKET ? counts[r] : LSH_MAX_BUCKET;
+        if (c < 2) continue;
+        if (c > LSH_SMALL_BUCKET) {
+            big[atomicAdd(n_big, 1)] = (int32_t)r;
+            continue;
         }
-        const int64_t u = k - pair_off[lo];
-        int64_t y = (int64_t)((1.0 + sqrt(1.0 + 8.0 * (double)u)) * 0.5);
-        while (y * (y - 1) / 2 > u) --y;
-        while ((y + 1) * y / 2 <= u) ++y;
-        const int64_t x = u - y * (y - 1) / 2;
-        const int64_t a = order[run_start[lo] + x], b = order[run_start[lo] + y];
-        out[k] = a < b ? (uint64_t)(a * n + b) : (uint64_t)(b * n + a);
+        const int32_t s0 = run_start[r];
+        uint64_t *o = out + pair_off[r];
+        for (int32_t y = 1; y < c; ++y) {
+            const int64_t b = order[s0 + y];
+            for (int32_t x = 0; x < y; ++x) {
+                const int64_t v = order[s0 + x];
+                *o++ = v < b ? (uint64_t)(v * n + b) : (uint64_t)(b * n + v);
+            }
+        }
+    }
+}
+
+// one warp per listed bucket (more than 32 members, at most 1000 taken): its
+// lanes split each member's pairs with the members before it
+__global__ void lsh_emit_big_kernel(const int32_t *__restrict__ order, const int32_t *__restrict__ run_start,
+                                    const int32_t *__restrict__ counts, const int64_t *__restrict__ pair_off,
+                                    const int32_t *__restrict__ big, const int32_t *__restrict__ n_big, int64_t n,
+                                    uint64_t *__restrict__ out) {
+    const int32_t lane = threadIdx.x & 31;
+    const int32_t nb = *n_big;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nb; w += warps) {
+        const int32_t r = big[w];
+        const int32_t c = counts[r] < LSH_MAX_BUCKET ? counts[r] : LSH_MAX_BUCKET;
+        const int32_t s0 = run_start[r];
+        uint64_t *o = out + pair_off[r];
+        for (int32_t y = 1; y < c; ++y) {
+            const int64_t b = order[s0 + y];
+            uint64_t *row = o + (int64_t)y * (y - 1) / 2;
+            for (int32_t x = lane; x < y; x += 32) {
+                const int64_t v = order[s0 + x];
+                row[x] = v < b ? (uint64_t)(v * n + b) : (uint64_t)(b * n + v);
+            }
+        }
     }
 }
 
@@ -173,10 +204,15 @@ static int32_t lsh_impl(void *pv) {
     uint64_t *skT = (uint64_t *)scratch(SLOT_SEARCH_TMP1, (size_t)n * a.s * 8, &status);
     LshKey *k0 = (LshKey *)scratch(SLOT_SEARCH_TMP2, (size_t)items * sizeof(LshKey) * 2, &status);
     int32_t *v0 = (int32_t *)scratch(SLOT_SEARCH_TMP3, (size_t)items * 4 * 2, &status);
-    // run data: unique keys (unused), counts, starts (int32), pair offsets (int64, items + 1)
-    char *rle = (char *)scratch(SLOT_SEARCH_TMP4, (size_t)items * (sizeof(LshKey) + 4 + 4 + 8) + 64, &status);
+    // run data: unique keys (unused), counts, starts (int32), pair offsets
+    // (int64, items + 1), then the list of buckets of more than 32 members (at
+    // most items / 33 of them)
+    const int64_t n_big_max = items / (LSH_SMALL_BUCKET + 1) + 1;
+    char *rle = (char *)scratch(SLOT_SEARCH_TMP4, (size_t)items * (sizeof(LshKey) + 4 + 4 + 8) + 64 + (size_t)n_big_max * 4,
+                                &status);
     int32_t *n_runs = (int32_t *)scratch(SLOT_MAXLEN, 64, &status);
     if (!d_band || !skT || !k0 || !v0 || !rle || !n_runs) return status;
+    int32_t *n_big = n_runs + 8;
     uint64_t *d_seeds = (uint64_t *)(((uintptr_t)(d_band + (size_t)a.tables * a.bands) + 15) & ~(uintptr_t)15);
     LshKey *k1 = k0 + items;
     int32_t *v1 = v0 + items;
@@ -184,6 +220,7 @@ static int32_t lsh_impl(void *pv) {
     int32_t *counts = (int32_t *)(uniq + items);
     int32_t *starts = counts + items;
     int64_t *pair_off = (int64_t *)(starts + items);  // 8-byte aligned: items * 24 bytes before
+    int32_t *big = (int32_t *)(pair_off + items + 1);
     int64_t *d_total = (int64_t *)(n_runs + 4);
     CK_CUDA(cudaMemcpyAsync(d_band, a.band_idx_host, (size_t)a.tables * a.bands * 4, cudaMemcpyHostToDevice, st));
     CK_CUDA(cudaMemcpyAsync(d_seeds, a.seeds_host, (size_t)a.tables * 8, cudaMemcpyHostToDevice, st));
@@ -256,8 +293,13 @@ static int32_t lsh_impl(void *pv) {
         cub::DoubleBuffer<int32_t> dv(v0, v1);
         int64_t tot = 0;
         CK_TRY(batch(t0, tb, dk, dv, &tot));
-        lsh_emit_kernel<<<grid_of(tot, 256), 256, 0, st>>>(dv.Current(), starts, pair_off, n_runs, tot, n,
-                                                           rk + at);
+        const int64_t m = (int64_t)tb * n;
+        CK_CUDA(cudaMemsetAsync(n_big, 0, 4, st));
+        lsh_emit_runs_kernel<<<grid_of(m, 256), 256, 0, st>>>(dv.Current(), starts, counts, pair_off, n_runs, n,
+                                                              rk + at, big, n_big);
+        CK_CUDA(cudaGetLastError());
+        lsh_emit_big_kernel<<<(int)sm_count() * 8, 256, 0, st>>>(dv.Current(), starts, counts, pair_off, big, n_big,
+                                                                n, rk + at);
         CK_CUDA(cudaGetLastError());
         at += tot;
     }

@@ -124,7 +124,11 @@ def lsh_candidates_device(sketches, num_tables: int, num_bands: int, seed: int =
     idx = np.ascontiguousarray(idx, np.int32)
     seeds_u = np.ascontiguousarray(seeds.astype(np.uint64))
     stream = torch.cuda.current_stream(sk.device).cuda_stream
-    cap = max(64 * n, 1 << 20)
+    # room for tables x N pairs (each sequence in one multi-member bucket per
+    # table), within a quarter of the free device memory: a call that finds
+    # more reports the count, and is repeated once with room for all of them
+    free_bytes, _ = torch.cuda.mem_get_info(sk.device)
+    cap = max(min(num_tables * n, free_bytes // 32), 1 << 20)
     count = np.zeros(1, np.int64)
     for _ in range(2):
         out = torch.empty((cap, 2), dtype=torch.int32, device=sk.device)
