@@ -74,6 +74,10 @@ def build_workload(use_gpu: bool, quick: bool = False):
         import oracle
         sk = oracle.sketches(s.flat, s.offsets, s.lengths, 5, 128)
     lp = auto_lsh_params(THRESHOLD, "high", 5)
+    # the host restatement, not the device LSH: with b = 1 this set has buckets
+    # of more than 1,000 members, where clustkit keeps the first 1,000 of numpy's
+    # unstable argsort (reproduced on the host) and the device the 1,000 lowest
+    # ids -- the workload must be clustkit's own
     cand = lsh_candidates(sk, lp["num_tables"], lp["num_bands"], 42)
     t2 = time.time()
     floor = max(0.001, 0.3 * THRESHOLD ** 5)
